@@ -1,0 +1,239 @@
+/*
+ * gb_prover.h -- C ABI of the GB300 (sm_103a) BLS12-381 prover library,
+ * libgbprover.so.
+ *
+ * Drop-in boundary: every `midnight_sppark_*` entry point below has the
+ * symbol name, argument list, argument meaning and error behaviour of the
+ * function of the same name that the reference's Rust crate binds in
+ * midnight-sppark-msm/src/lib.rs:763-1362 (implemented there in
+ * midnight-sppark-msm/src/bls12_381_g1_msm.cu).  Linking this library in
+ * place of the reference's sppark-built archive needs no change on the Rust
+ * side.  Entries prefixed `gb_` are additions of this library.
+ *
+ * Data layout (all little-endian, Montgomery form, blst-compatible):
+ *   RawFr           = Bls12_381Fr           (lib.rs:17-21)  4 x u64, R = 2^256
+ *   RawG1Affine     = Bls12_381G1Affine     (lib.rs:23-28)  x[6], y[6]; infinity = all zero
+ *   RawG1Projective = Bls12_381G1Projective (lib.rs:30-36)  Jacobian x[6], y[6], z[6]; infinity z = 0
+ *
+ * Errors: RustError is returned by value; code 0 = success, otherwise a
+ * cudaError_t value or -1; `message` is NULL or a strdup()'d string the
+ * caller releases with free() (vendor/sppark-0.1.15/src/lib.rs:8-23).
+ * Invalid arguments give cudaErrorInvalidValue (1) with a message, as in
+ * bls12_381_g1_msm.cu:6318-6331.  There is no CPU fallback: without a CUDA
+ * device every compute entry point returns an error.
+ *
+ * Threading and ordering: work runs on the calling thread's execution lane
+ * (one CUDA stream per lane, midnight_sppark_execution_lane_set).  Calls that
+ * take or return host buffers are synchronous.  Calls that produce a device
+ * vector return once the work is queued; a consumer on any lane waits for it
+ * (each device vector carries a completion event).
+ */
+#ifndef GB_PROVER_H
+#define GB_PROVER_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GB_API __attribute__((visibility("default")))
+#else
+#define GB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { uint64_t limbs[4]; } RawFr;
+typedef struct { uint64_t x[6]; uint64_t y[6]; } RawG1Affine;
+typedef struct { uint64_t x[6]; uint64_t y[6]; uint64_t z[6]; } RawG1Projective;
+typedef struct { int code; char *message; } RustError;
+
+/* bls12_381_g1_msm.cu:50-61; Rust mirror Bls12_381MsmConfig lib.rs:126-160.
+ * window_bits 0 = chosen by the library; this library accepts 0 or 8..16. */
+typedef struct {
+    uint32_t domain_k;
+    uint32_t min_msm_scalars;
+    uint32_t unfiltered_min_scalars;
+    uint32_t window_bits;
+    uint32_t sort_grid_divisor;
+    uint32_t sort_window_lanes;
+    uint32_t integration_blocks;
+    uint32_t batch_lanes;
+    uint32_t reuse_event;
+    uint32_t device_reduce;
+} RawMsmConfig;
+
+/* bls12_381_g1_msm.cu:63-68 */
+typedef struct {
+    size_t scalar_offset;
+    size_t point_offset;
+    size_t len;
+    size_t nonzero_len;
+} RawMsmSlice;
+
+/* ---- lanes ---------------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:134-146: 0 = shared lane, 1..8 private lanes */
+GB_API RustError midnight_sppark_execution_lane_set(uint32_t lane);
+
+/* ---- G1 multiexp ------------------------------------------------------------ */
+/* bls12_381_g1_msm.cu:6164-6200: out = sum_i scalars[i] * points[i] */
+GB_API RustError midnight_sppark_bls12_381_g1_msm(RawG1Projective *out, const RawG1Affine *points,
+                                                  const RawFr *scalars, size_t len);
+/* bls12_381_g1_msm.cu:6202-6245: scalars laid out [nmsms][npoints] */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_batch(RawG1Projective *out, const RawG1Affine *points,
+                                                        const RawFr *scalars, size_t npoints, size_t nmsms);
+/* bls12_381_g1_msm.cu:6247-6281: resident bases (and their per-window
+ * shifted copies, computed here once) */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_create(void **out, const RawG1Affine *points,
+                                                                 size_t npoints);
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_create_with_config(void **out,
+                                                                             const RawG1Affine *points,
+                                                                             size_t npoints,
+                                                                             RawMsmConfig config);
+/* bls12_381_g1_msm.cu:6283-6286 */
+GB_API void midnight_sppark_bls12_381_g1_msm_context_free(void *context);
+/* bls12_381_g1_msm.cu:6288-6308: host scalars [nmsms][npoints] */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_batch(RawG1Projective *out, void *context,
+                                                                const RawFr *scalars, size_t npoints,
+                                                                size_t nmsms);
+/* bls12_381_g1_msm.cu:6310-6344: scalars from a device vector */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_device_batch(RawG1Projective *out, void *context,
+                                                                       const void *device_vec,
+                                                                       size_t scalar_offset, size_t npoints,
+                                                                       size_t nmsms);
+/* bls12_381_g1_msm.cu:6346-6377 */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_device_ragged(RawG1Projective *out, void *context,
+                                                                        const void *device_vec,
+                                                                        const RawMsmSlice *slices, size_t count);
+/* bls12_381_g1_msm.cu:6426-6486: per batch entry, MSM(scalars + mask)
+ * (mask_device_vec holds npoints values); as in the reference, the caller
+ * subtracts its precomputed MSM(mask, bases) (lib.rs:3302-3354) */
+GB_API RustError midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch(
+    RawG1Projective *out, void *context, const void *device_vec, size_t scalar_offset, size_t npoints,
+    size_t nmsms, const void *mask_device_vec);
+
+/* ---- NTT / coset LDE -------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:6488-6502: in place, natural order; inverse includes 1/n */
+GB_API RustError midnight_sppark_bls12_381_fr_ntt(RawFr *values, uint32_t log_n, bool inverse);
+/* bls12_381_g1_msm.cu:3447-3495: NTT, then *scale, then *{1,first,second}[i mod 3] */
+GB_API RustError midnight_sppark_bls12_381_fr_ntt_zeta(RawFr *values, uint32_t log_n, bool inverse, RawFr scale,
+                                                       RawFr first, RawFr second);
+/* bls12_381_g1_msm.cu:3497-3556: *factors[i mod m], inverse NTT, *scale, zeta */
+GB_API RustError midnight_sppark_bls12_381_fr_divide_ntt_zeta(RawFr *values, uint32_t log_n,
+                                                              const RawFr *factors, size_t factor_len,
+                                                              RawFr scale, RawFr first, RawFr second);
+/* bls12_381_g1_msm.cu:2542-2602: zeta-distribute, zero-pad, forward NTT */
+GB_API RustError midnight_sppark_bls12_381_fr_coeff_to_extended_batch(RawFr *out, const RawFr *inputs,
+                                                                      size_t input_len, size_t count,
+                                                                      uint32_t extended_log_n, RawFr first,
+                                                                      RawFr second);
+/* bls12_381_g1_msm.cu:2604-2740: same, result resident */
+GB_API RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_batch(void **out, const RawFr *inputs,
+                                                                             size_t input_len, size_t count,
+                                                                             uint32_t extended_log_n,
+                                                                             RawFr first, RawFr second);
+GB_API RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_from_device_batch(
+    void **out, const void *source, size_t input_len, size_t count, uint32_t extended_log_n, RawFr first,
+    RawFr second);
+/* bls12_381_g1_msm.cu:3280-3440 */
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(void *device_vec, uint32_t log_n, bool inverse,
+                                                                  RawFr scale, RawFr first, RawFr second);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(void *device_vec, uint32_t log_n,
+                                                                        size_t count, bool inverse, RawFr scale,
+                                                                        RawFr first, RawFr second);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_vec, uint32_t log_n,
+                                                                         const RawFr *factors, size_t factor_len,
+                                                                         RawFr scale, RawFr first,
+                                                                         RawFr second);
+
+/* ---- vector ops ------------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:1188-1231 kernels behind lib.rs:1000-1140 */
+GB_API RustError midnight_sppark_bls12_381_fr_mul_assign(RawFr *values, RawFr scalar, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_mul_assign_zeta(RawFr *values, RawFr first, RawFr second,
+                                                              size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_mul_assign_repeating(RawFr *values, const RawFr *factors,
+                                                                   size_t factor_len, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_invert_assign(RawFr *values, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_sort_canonical(RawFr *values, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_poly_lincomb(RawFr *out, const RawFr *polys, size_t poly_len,
+                                                           size_t poly_count, const RawFr *scalars);
+/* bls12_381_g1_msm.cu:4303-4340 (permutation/prover.rs:36-43) */
+GB_API RustError midnight_sppark_bls12_381_fr_shifted_prefix_product(RawFr *values, RawFr initial, size_t len);
+
+/* ---- grand products --------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:4342-4449: out = device vector [sets][len] */
+GB_API RustError midnight_sppark_bls12_381_fr_permutation_products(
+    void **out, const RawFr *columns, const RawFr *permutations, size_t len, size_t column_count,
+    size_t chunk_len, RawFr beta, RawFr gamma, RawFr omega, const RawFr *delta_powers,
+    const RawFr *blind_values, size_t blinding_factors);
+/* bls12_381_g1_msm.cu:4451-4548: out = device vector [lookup_count][len] */
+GB_API RustError midnight_sppark_bls12_381_fr_lookup_products(
+    void **out, const RawFr *compressed_inputs, const RawFr *compressed_tables, const RawFr *permuted_inputs,
+    const RawFr *permuted_tables, size_t len, size_t lookup_count, RawFr beta, RawFr gamma,
+    const RawFr *blind_values, size_t blinding_factors);
+/* bls12_381_g1_msm.cu:4550-4634 */
+GB_API RustError midnight_sppark_bls12_381_fr_lookup_products_device(void **out, const void *trace_lagrange,
+                                                                     size_t len, size_t lookup_count, RawFr beta,
+                                                                     RawFr gamma, const RawFr *blind_values,
+                                                                     size_t blinding_factors);
+
+/* ---- quotient --------------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:3181-3240 (vanishing/prover.rs:141-220,304-318) */
+GB_API RustError midnight_sppark_bls12_381_fr_device_quotient_pieces(void **out, const void *quotient_vec,
+                                                                     size_t poly_len, size_t piece_count,
+                                                                     const RawFr *blinds, size_t blind_count);
+/* bls12_381_g1_msm.cu:3242-3278 */
+GB_API RustError midnight_sppark_bls12_381_fr_device_poly_lincomb(void **out, const void *polys_vec,
+                                                                  size_t poly_len, size_t poly_count,
+                                                                  const RawFr *scalars, size_t scalar_count);
+
+/* ---- device vectors --------------------------------------------------------- */
+/* bls12_381_g1_msm.cu:2741-3442 */
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_upload(void **out, const RawFr *values, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_upload_many(void **out, const RawFr *const *values,
+                                                                     const size_t *lengths, size_t count);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_download(RawFr *out, const void *device_vec, size_t len);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_scatter_host(void *device_vec, const uint32_t *indices,
+                                                                      const RawFr *values, size_t count);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_concat_host(void **out, const void *prefix_device_vec,
+                                                                     const RawFr *suffix, size_t suffix_len);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_concat_many_host(void **out,
+                                                                          const void *const *source_device_vecs,
+                                                                          size_t source_count,
+                                                                          const RawFr *suffix, size_t suffix_len);
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_gather_polys(void **out, const void *source_device_vec,
+                                                                      size_t poly_len, const uint32_t *indices,
+                                                                      size_t index_count);
+GB_API void midnight_sppark_bls12_381_fr_device_vec_free(void *device_vec);
+
+/* ---- library additions (no reference counterpart) ---------------------------- */
+/* number of Fr elements held by a device vector */
+GB_API size_t gb_fr_device_vec_len(const void *device_vec);
+/* out[i] = affine([scalars[i]] G), host buffers (SRS bases [tau^i] G) */
+GB_API RustError gb_g1_generator_mul(RawG1Affine *out, const RawFr *scalars, size_t n);
+/* same with device pointers; queued on the calling lane's stream */
+GB_API RustError gb_g1_generator_mul_device(RawG1Affine *d_out, const RawFr *d_scalars, size_t n);
+/* measured device throughput of 32x32->64 multiply-adds per second */
+GB_API RustError gb_imad_peak(double *out_per_sec);
+/* cumulative host<->device bytes moved by this library */
+GB_API void gb_transfer_counters(uint64_t *h2d_bytes, uint64_t *d2h_bytes);
+GB_API void gb_transfer_counters_reset(void);
+/* kernel launches issued by the library since it was loaded */
+GB_API uint64_t gb_launch_counter(void);
+/* the calling thread's lane stream (a cudaStream_t) */
+GB_API void *gb_lane_stream(void);
+/* CUDA-event timing of individual kernels on their launching stream;
+ * slot 0 = MSM bucket accumulation, 1 = whole MSM, 2 = NTT passes */
+GB_API void gb_profile_enable(int on);
+GB_API void gb_profile_read(int slot, double *total_ms, uint64_t *launches);
+GB_API void gb_profile_reset(void);
+/* releases a RustError message for callers without access to free() */
+GB_API void gb_error_free(char *message);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB_PROVER_H */

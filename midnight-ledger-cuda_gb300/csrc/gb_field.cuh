@@ -1,0 +1,392 @@
+// Montgomery arithmetic for the two BLS12-381 fields, written for sm_103a.
+//
+//   fp_t : base field Fp, 381-bit modulus, 12 x 32-bit limbs, R = 2^384
+//   fr_t : scalar field Fr, 255-bit modulus, 8 x 32-bit limbs, R = 2^256
+//
+// The memory image of each type is byte-identical to blst's 64-bit-limb
+// Montgomery representation (blst_fp / blst_fr), which is what the reference
+// FFI passes across the boundary (midnight-sppark-msm/src/lib.rs:17-36,
+// vendor/midnight-curves-0.3.1/src/bls12_381/fq.rs:25-29): little-endian
+// limbs, Montgomery form, every stored value fully reduced into [0, m).
+//
+// Multiplication is CIOS Montgomery multiplication.  On the device the
+// carry chains are written as inline PTX (mad.lo.cc / madc.hi.cc on 32-bit
+// limbs, split into even and odd partial-product rows so the two carry chains
+// are independent); a portable C version of the same algorithm is kept for
+// host builds of this header, which the CPU test suite uses to check the
+// limb logic against the oracle without a GPU.
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define GB_HD __host__ __device__ __forceinline__
+#define GB_D __device__ __forceinline__
+// out-of-line on the device: for operations off the hot loops, so each kernel
+// does not inline hundreds of carry-chain field products
+#define GB_COLD inline __host__ __device__ __noinline__
+#else
+#define GB_HD inline
+#define GB_D inline
+#define GB_COLD inline
+#endif
+
+namespace gb {
+
+struct FpCfg {
+    static constexpr int N = 12;
+    static constexpr uint32_t INV = 0xfffcfffdu;  // -p^-1 mod 2^32
+    GB_HD static uint32_t mod(int i)
+    {
+        constexpr uint32_t P[12] = {0xffffaaabu, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu,
+                                    0xf6b0f624u, 0x6730d2a0u, 0xf38512bfu, 0x64774b84u,
+                                    0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
+        return P[i];
+    }
+    GB_HD static uint32_t one(int i)
+    {
+        constexpr uint32_t O[12] = {0x0002fffdu, 0x76090000u, 0xc40c0002u, 0xebf4000bu,
+                                    0x53c758bau, 0x5f489857u, 0x70525745u, 0x77ce5853u,
+                                    0xa256ec6du, 0x5c071a97u, 0xfa80e493u, 0x15f65ec3u};
+        return O[i];
+    }
+    GB_HD static uint32_t r2(int i)
+    {
+        constexpr uint32_t R2[12] = {0x1c341746u, 0xf4df1f34u, 0x09d104f1u, 0x0a76e6a6u,
+                                     0x4c95b6d5u, 0x8de5476cu, 0x939d83c0u, 0x67eb88a9u,
+                                     0xb519952du, 0x9a793e85u, 0x92cae3aau, 0x11988fe5u};
+        return R2[i];
+    }
+};
+
+struct FrCfg {
+    static constexpr int N = 8;
+    static constexpr uint32_t INV = 0xffffffffu;  // -r^-1 mod 2^32
+    GB_HD static uint32_t mod(int i)
+    {
+        constexpr uint32_t P[8] = {0x00000001u, 0xffffffffu, 0xfffe5bfeu, 0x53bda402u,
+                                   0x09a1d805u, 0x3339d808u, 0x299d7d48u, 0x73eda753u};
+        return P[i];
+    }
+    GB_HD static uint32_t one(int i)
+    {
+        constexpr uint32_t O[8] = {0xfffffffeu, 0x00000001u, 0x00034802u, 0x5884b7fau,
+                                   0xecbc4ff5u, 0x998c4fefu, 0xacc5056fu, 0x1824b159u};
+        return O[i];
+    }
+    GB_HD static uint32_t r2(int i)
+    {
+        constexpr uint32_t R2[8] = {0xf3f29c6du, 0xc999e990u, 0x87925c23u, 0x2b6cedcbu,
+                                    0x7254398fu, 0x05d31496u, 0x9f59ff11u, 0x0748d9d9u};
+        return R2[i];
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Multi-limb primitives.  Device versions use PTX carry flags; host versions
+// use 64-bit intermediates.  Both compute the same function.
+// ---------------------------------------------------------------------------
+
+#if defined(__CUDA_ARCH__)
+#define GB_ADDC_FIRST(d, a, b) asm("add.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#define GB_ADDC(d, a, b) asm("addc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#define GB_ADDC_LAST(d, a, b) asm("addc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#define GB_SUBC_FIRST(d, a, b) asm("sub.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#define GB_SUBC(d, a, b) asm("subc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#define GB_SUBC_LAST(d, a, b) asm("subc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
+#endif
+
+// out = a + b over N limbs; returns the carry out.
+template <int N>
+GB_HD uint32_t mp_add(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+#if defined(__CUDA_ARCH__)
+    uint32_t c;
+    GB_ADDC_FIRST(out[0], a[0], b[0]);
+#pragma unroll
+    for (int i = 1; i < N; i++) GB_ADDC(out[i], a[i], b[i]);
+    GB_ADDC_LAST(c, 0u, 0u);
+    return c;
+#else
+    uint64_t c = 0;
+    for (int i = 0; i < N; i++) {
+        uint64_t v = (uint64_t)a[i] + b[i] + c;
+        out[i] = (uint32_t)v;
+        c = v >> 32;
+    }
+    return (uint32_t)c;
+#endif
+}
+
+// out = a - b over N limbs; returns the borrow (1 if a < b).
+template <int N>
+GB_HD uint32_t mp_sub(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+#if defined(__CUDA_ARCH__)
+    uint32_t br;
+    GB_SUBC_FIRST(out[0], a[0], b[0]);
+#pragma unroll
+    for (int i = 1; i < N; i++) GB_SUBC(out[i], a[i], b[i]);
+    GB_SUBC_LAST(br, 0u, 0u);
+    return br & 1u;
+#else
+    uint64_t br = 0;
+    for (int i = 0; i < N; i++) {
+        uint64_t v = (uint64_t)a[i] - b[i] - br;
+        out[i] = (uint32_t)v;
+        br = (v >> 32) & 1;
+    }
+    return (uint32_t)br;
+#endif
+}
+
+template <class Cfg>
+struct mont_t {
+    static constexpr int N = Cfg::N;
+    uint32_t v[N];
+
+    GB_HD static mont_t zero()
+    {
+        mont_t r;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.v[i] = 0;
+        return r;
+    }
+    GB_HD static mont_t one()
+    {
+        mont_t r;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.v[i] = Cfg::one(i);
+        return r;
+    }
+    GB_HD static mont_t modulus()
+    {
+        mont_t r;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.v[i] = Cfg::mod(i);
+        return r;
+    }
+    GB_HD bool is_zero() const
+    {
+        uint32_t x = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) x |= v[i];
+        return x == 0;
+    }
+    GB_HD bool operator==(const mont_t &o) const
+    {
+        uint32_t x = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) x |= v[i] ^ o.v[i];
+        return x == 0;
+    }
+    GB_HD bool operator!=(const mont_t &o) const { return !(*this == o); }
+
+    // conditional subtraction of the modulus: r = a >= m ? a - m : a,
+    // for a < 2m.  `carry` is an extra top bit of a.
+    GB_HD static void reduce_once(uint32_t *a, uint32_t carry)
+    {
+        uint32_t t[N], m[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) m[i] = Cfg::mod(i);
+        uint32_t br = mp_sub<N>(t, a, m);
+        // keep t when a >= m, i.e. carry set or no borrow
+        bool take = carry || !br;
+#pragma unroll
+        for (int i = 0; i < N; i++) a[i] = take ? t[i] : a[i];
+    }
+
+    GB_HD friend mont_t operator+(const mont_t &a, const mont_t &b)
+    {
+        mont_t r;
+        uint32_t c = mp_add<N>(r.v, a.v, b.v);
+        reduce_once(r.v, c);
+        return r;
+    }
+    GB_HD friend mont_t operator-(const mont_t &a, const mont_t &b)
+    {
+        mont_t r;
+        uint32_t br = mp_sub<N>(r.v, a.v, b.v);
+        if (br) {
+            uint32_t m[N];
+#pragma unroll
+            for (int i = 0; i < N; i++) m[i] = Cfg::mod(i);
+            mp_add<N>(r.v, r.v, m);
+        }
+        return r;
+    }
+    GB_HD mont_t operator-() const
+    {
+        if (is_zero()) return *this;
+        mont_t r, m = modulus();
+        mp_sub<N>(r.v, m.v, v);
+        return r;
+    }
+    GB_HD mont_t dbl() const { return *this + *this; }
+    GB_HD mont_t &operator+=(const mont_t &o) { return *this = *this + o; }
+    GB_HD mont_t &operator-=(const mont_t &o) { return *this = *this - o; }
+
+    // Montgomery product a * b * 2^(-32N) mod m (CIOS), fully reduced.
+    GB_HD friend mont_t operator*(const mont_t &a, const mont_t &b)
+    {
+        mont_t r;
+        mont_mul(r.v, a.v, b.v);
+        return r;
+    }
+    GB_HD mont_t &operator*=(const mont_t &o) { return *this = *this * o; }
+    GB_HD mont_t sqr() const { return *this * *this; }
+
+    GB_HD static void mont_mul(uint32_t *out, const uint32_t *a, const uint32_t *b);
+
+    GB_HD mont_t to_mont() const
+    {
+        mont_t r2;
+#pragma unroll
+        for (int i = 0; i < N; i++) r2.v[i] = Cfg::r2(i);
+        return *this * r2;
+    }
+    GB_HD mont_t from_mont() const
+    {
+        mont_t o = zero();
+        o.v[0] = 1;
+        return *this * o;
+    }
+    // this^(m-2): Fermat inverse; zero maps to zero
+    GB_COLD mont_t inverse() const
+    {
+        uint32_t e[N], two[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) { e[i] = Cfg::mod(i); two[i] = 0; }
+        two[0] = 2;
+        mp_sub<N>(e, e, two);
+        mont_t acc = one();
+        for (int i = 32 * N - 1; i >= 0; i--) {
+            acc = acc.sqr();
+            if ((e[i >> 5] >> (i & 31)) & 1u) acc = acc * *this;
+        }
+        return acc;
+    }
+    // this^e for a 64-bit exponent
+    GB_COLD mont_t pow_u64(uint64_t e) const
+    {
+        mont_t acc = one(), base = *this;
+        while (e) {
+            if (e & 1) acc = acc * base;
+            base = base.sqr();
+            e >>= 1;
+        }
+        return acc;
+    }
+};
+
+#if defined(__CUDA_ARCH__)
+// Device CIOS: for each limb b[i], accumulate a*b[i] and m*p into the running
+// sum using two interleaved carry chains (even-indexed products land on even
+// limbs with their high halves on odd limbs, and vice versa).
+template <class Cfg>
+GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+    constexpr int N = Cfg::N;
+    uint32_t even[N + 1], odd[N + 1];
+#pragma unroll
+    for (int i = 0; i < N + 1; i++) { even[i] = 0; odd[i] = 0; }
+
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t bi = b[i];
+        // even += a[2j]*bi (lo at 2j, hi at 2j+1)
+        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[0]) : "r"(a[0]), "r"(bi));
+        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[1]) : "r"(a[0]), "r"(bi));
+#pragma unroll
+        for (int j = 2; j < N; j += 2) {
+            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[j]) : "r"(a[j]), "r"(bi));
+            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[j + 1]) : "r"(a[j]), "r"(bi));
+        }
+        asm("addc.u32 %0, %0, 0;" : "+r"(even[N]));
+        // odd += a[2j+1]*bi (lo at 2j+1 -> stored at odd[2j], hi at odd[2j+1])
+        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[0]) : "r"(a[1]), "r"(bi));
+        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[1]) : "r"(a[1]), "r"(bi));
+#pragma unroll
+        for (int j = 2; j < N; j += 2) {
+            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j]) : "r"(a[j + 1]), "r"(bi));
+            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j + 1]) : "r"(a[j + 1]), "r"(bi));
+        }
+        asm("addc.u32 %0, %0, 0;" : "+r"(odd[N]));
+        // Here the value is even[0..N] + odd[0..N] * 2^32.
+        // Montgomery step: m = even[0] * inv; add m*p (even limbs of p into
+        // even, odd limbs of p into odd), after which even[0] == 0.
+        const uint32_t m = even[0] * Cfg::INV;
+        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[0]) : "r"(m), "r"(Cfg::mod(0)));
+        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[1]) : "r"(m), "r"(Cfg::mod(0)));
+#pragma unroll
+        for (int j = 2; j < N; j += 2) {
+            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[j]) : "r"(m), "r"(Cfg::mod(j)));
+            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[j + 1]) : "r"(m), "r"(Cfg::mod(j)));
+        }
+        asm("addc.u32 %0, %0, 0;" : "+r"(even[N]));
+        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[0]) : "r"(m), "r"(Cfg::mod(1)));
+        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[1]) : "r"(m), "r"(Cfg::mod(1)));
+#pragma unroll
+        for (int j = 2; j < N; j += 2) {
+            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j]) : "r"(m), "r"(Cfg::mod(j + 1)));
+            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j + 1]) : "r"(m), "r"(Cfg::mod(j + 1)));
+        }
+        asm("addc.u32 %0, %0, 0;" : "+r"(odd[N]));
+        // Divide by 2^32: the new value is odd[0..N] + even[1..N] * 2^0 ...
+        // value = even + odd*2^32 with even[0] == 0, so
+        // value / 2^32 = even[1..N] + odd[0..N]; fold into `even` as the
+        // running sum and clear `odd`.
+        asm("add.cc.u32 %0, %1, %2;" : "=r"(even[0]) : "r"(even[1]), "r"(odd[0]));
+#pragma unroll
+        for (int j = 1; j < N; j++)
+            asm("addc.cc.u32 %0, %1, %2;" : "=r"(even[j]) : "r"(even[j + 1]), "r"(odd[j]));
+        asm("addc.u32 %0, %1, 0;" : "=r"(even[N]) : "r"(odd[N]));
+#pragma unroll
+        for (int j = 0; j < N + 1; j++) odd[j] = 0;
+    }
+    // even[0..N] < 2m; final conditional subtraction
+    mont_t<Cfg>::reduce_once(even, even[N]);
+#pragma unroll
+    for (int i = 0; i < N; i++) out[i] = even[i];
+}
+#endif
+
+template <class Cfg>
+GB_HD void mont_t<Cfg>::mont_mul(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+#if defined(__CUDA_ARCH__)
+    mont_mul_device<Cfg>(out, a, b);
+#else
+    uint32_t t[N + 2];
+    for (int i = 0; i < N + 2; i++) t[i] = 0;
+    for (int i = 0; i < N; i++) {
+        uint64_t c = 0;
+        for (int j = 0; j < N; j++) {
+            uint64_t v = (uint64_t)a[j] * b[i] + t[j] + c;
+            t[j] = (uint32_t)v;
+            c = v >> 32;
+        }
+        uint64_t v = (uint64_t)t[N] + c;
+        t[N] = (uint32_t)v;
+        t[N + 1] = (uint32_t)(v >> 32);
+        uint32_t m = t[0] * Cfg::INV;
+        v = (uint64_t)m * Cfg::mod(0) + t[0];
+        c = v >> 32;
+        for (int j = 1; j < N; j++) {
+            v = (uint64_t)m * Cfg::mod(j) + t[j] + c;
+            t[j - 1] = (uint32_t)v;
+            c = v >> 32;
+        }
+        v = (uint64_t)t[N] + c;
+        t[N - 1] = (uint32_t)v;
+        t[N] = t[N + 1] + (uint32_t)(v >> 32);
+    }
+    reduce_once(t, t[N]);
+    for (int i = 0; i < N; i++) out[i] = t[i];
+#endif
+}
+
+using fp_t = mont_t<FpCfg>;
+using fr_t = mont_t<FrCfg>;
+
+}  // namespace gb

@@ -1,0 +1,200 @@
+// Fixed-base G1 scalar multiplication by the generator ([s_i] G, affine out)
+// and the integer multiply-add peak probe.
+//
+// [s]G is what an SRS needs (g_i = [tau^i] G, params.rs:38-129) and what the
+// synthetic MSM inputs need (bases [r_i] G).  The generator table holds
+// d * 2^(8w) G for w < 32, d < 256 (786 KB, built once per device on the
+// device), so one [s]G costs at most 32 mixed additions and one inversion.
+#include <mutex>
+
+#include "gb_runtime.cuh"
+
+namespace gb {
+
+// The generator is supplied by the host in canonical form and converted here
+// (keeps the constant in one readable place: the canonical hex of the
+// BLS12-381 G1 generator).
+__global__ void gen_table_bases_kernel(affine_t gen_canonical, xyzz_t *bases)
+{
+    // thread w: 2^(8w) G
+    int w = threadIdx.x;
+    if (w >= 32) return;
+    affine_t g;
+    g.x = gen_canonical.x.to_mont();
+    g.y = gen_canonical.y.to_mont();
+    xyzz_t acc = xyzz_t::from_affine(g);
+    for (int k = 0; k < 8 * w; k++) acc = acc.dbl();
+    bases[w] = acc;
+}
+
+__global__ void gen_table_fill_kernel(const xyzz_t *bases, affine_t *table)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 32 * 256) return;
+    int w = t >> 8, d = t & 255;
+    xyzz_t p = xyzz_mul_small(bases[w], (uint32_t)d);
+    table[t] = p.to_affine();
+}
+
+__global__ void generator_mul_kernel(const fr_t *__restrict__ scalars, size_t n, const affine_t *__restrict__ table,
+                                     affine_t *__restrict__ out)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    fr_t s = scalars[i].from_mont();
+    xyzz_t acc = xyzz_t::inf();
+    for (int w = 0; w < 32; w++) {
+        uint32_t d = (s.v[w >> 2] >> (8 * (w & 3))) & 0xffu;
+        if (d) acc.add_affine(table[w * 256 + d], false);
+    }
+    out[i] = acc.to_affine();
+}
+
+static affine_t host_generator_canonical()
+{
+    // x, y of the BLS12-381 G1 generator, canonical little-endian u32 limbs
+    static const char *X = "17f1d3a73197d7942695638c4fa9ac0fc3688c4f9774b905a14e3a3f171bac586c55e83ff97a1aeffb3af00adb22c6bb";
+    static const char *Y = "08b3f481e3aaa0f1a09e30ed741d8ae4fcf5e095d5d00af600db18cb2c04b3edd03cc744a2888ae40caa232946c5e7e1";
+    affine_t g;
+    auto parse = [](const char *hex, fp_t &out) {
+        for (int i = 0; i < 12; i++) out.v[i] = 0;
+        size_t len = strlen(hex);
+        for (size_t k = 0; k < len; k++) {
+            char ch = hex[len - 1 - k];
+            uint32_t v = (ch >= '0' && ch <= '9') ? (uint32_t)(ch - '0') : (uint32_t)(ch - 'a' + 10);
+            out.v[k / 8] |= v << (4 * (k % 8));
+        }
+    };
+    parse(X, g.x);
+    parse(Y, g.y);
+    return g;
+}
+
+namespace {
+std::mutex g_gen_mu;
+affine_t *g_gen_table[64];
+}  // namespace
+
+const affine_t *generator_table(cudaStream_t s)
+{
+    int dev = current_device();
+    std::lock_guard<std::mutex> lk(g_gen_mu);
+    if (g_gen_table[dev]) return g_gen_table[dev];
+    affine_t *table = nullptr;
+    xyzz_t *bases = nullptr;
+    GB_CUDA_OK(cudaMalloc(&table, 32 * 256 * sizeof(affine_t)));
+    GB_CUDA_OK(cudaMalloc(&bases, 32 * sizeof(xyzz_t)));
+    gen_table_bases_kernel<<<1, 32, 0, s>>>(host_generator_canonical(), bases);
+    GB_CHECK_LAUNCH();
+    gen_table_fill_kernel<<<32, 256, 0, s>>>(bases, table);
+    GB_CHECK_LAUNCH();
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    cudaFree(bases);
+    g_gen_table[dev] = table;
+    return table;
+}
+
+void generator_mul_device(affine_t *d_out, const fr_t *d_scalars, size_t n, cudaStream_t s)
+{
+    if (!n) return;
+    const affine_t *t = generator_table(s);
+    generator_mul_kernel<<<blocks_for(n, 128), 128, 0, s>>>(d_scalars, n, t, d_out);
+    GB_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------- peak probe
+// Throughput of independent 32x32->64 multiply-adds (mad.wide.u32), the unit
+// in which the MSM's algorithmic work is counted (one Fp Montgomery product =
+// 2*12^2 + 12 = 300 such multiply-adds).  8 independent accumulators per
+// thread keep the pipe full; the result is folded into `sink` so nothing is
+// dead code.
+__global__ void imad_peak_kernel(uint32_t a0, uint32_t b0, int iters, unsigned long long *sink)
+{
+    uint64_t acc[8];
+    uint32_t a = a0 + threadIdx.x, b = b0 ^ blockIdx.x;
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc[k] = (uint64_t)(a + k) << 7;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc[k]) : "r"(a + (uint32_t)k), "r"(b));
+        }
+    }
+    uint64_t r = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) r ^= acc[k];
+    if (r == 0x123456789ull) atomicAdd(sink, r);
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+// out[i] = affine([scalars[i]] G); host buffers.  Used to build SRS bases.
+RustError gb_g1_generator_mul(RawG1Affine *out_raw, const RawFr *scalars_raw, size_t n)
+{
+    affine_t *out = reinterpret_cast<affine_t *>(out_raw);
+    const fr_t *scalars = reinterpret_cast<const fr_t *>(scalars_raw);
+    if (n == 0) return ok();
+    if (!out || !scalars) return make_error((int)cudaErrorInvalidValue, "invalid generator mul arguments");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    dev_buf<fr_t> ds(n, s);
+    dev_buf<affine_t> dout(n, s);
+    h2d(ds, scalars, n * sizeof(fr_t), s);
+    generator_mul_device(dout, ds, n, s);
+    d2h(out, dout, n * sizeof(affine_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+// Device-pointer variant (both pointers are device memory), async on the lane.
+RustError gb_g1_generator_mul_device(RawG1Affine *d_out_raw, const RawFr *d_scalars_raw, size_t n)
+{
+    affine_t *d_out = reinterpret_cast<affine_t *>(d_out_raw);
+    const fr_t *d_scalars = reinterpret_cast<const fr_t *>(d_scalars_raw);
+    if (n == 0) return ok();
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    generator_mul_device(d_out, d_scalars, n, s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// Measured multiply-add peak: runs the probe and returns multiply-adds per
+// second (whole device) in *out_per_sec.
+RustError gb_imad_peak(double *out_per_sec)
+{
+    if (!out_per_sec) return make_error((int)cudaErrorInvalidValue, "null output");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    int dev = current_device(), sms = 0;
+    GB_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    unsigned long long *sink = nullptr;
+    GB_CUDA_OK(cudaMallocAsync((void **)&sink, sizeof(*sink), s));
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    imad_peak_kernel<<<blocks, threads, 0, s>>>(1, 3, 64, sink);  // warm-up
+    GB_CHECK_LAUNCH();
+    cudaEvent_t e0, e1;
+    GB_CUDA_OK(cudaEventCreate(&e0));
+    GB_CUDA_OK(cudaEventCreate(&e1));
+    GB_CUDA_OK(cudaEventRecord(e0, s));
+    imad_peak_kernel<<<blocks, threads, 0, s>>>(1, 3, iters, sink);
+    GB_CHECK_LAUNCH();
+    GB_CUDA_OK(cudaEventRecord(e1, s));
+    GB_CUDA_OK(cudaEventSynchronize(e1));
+    float ms = 0;
+    GB_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(sink, s);
+    double ops = (double)blocks * threads * iters * 8.0;
+    *out_per_sec = ops / (ms * 1e-3);
+    return ok();
+    GB_ENTRY_END
+}
+
+}  // extern "C"

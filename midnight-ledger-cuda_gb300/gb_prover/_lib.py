@@ -1,0 +1,162 @@
+"""ctypes loader for libgbprover.so and the C ABI declarations."""
+import ctypes
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+REPO_ROOT = os.path.dirname(PKG_ROOT)
+HEADER = os.path.join(REPO_ROOT, "include", "gb_prover.h")
+
+if PKG_ROOT not in sys.path:
+    sys.path.insert(0, PKG_ROOT)
+
+import build_lib as _build_lib  # noqa: E402
+
+
+class MsmError(RuntimeError):
+    """Error returned by the library (mirrors lib.rs MsmError::Sppark)."""
+
+    def __init__(self, code, message):
+        super().__init__("gb prover call failed (code %d): %s" % (code, message))
+        self.code = code
+        self.message = message
+
+
+class RustError(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int), ("message", ctypes.c_void_p)]
+
+
+class RawMsmConfig(ctypes.Structure):
+    """bls12_381_g1_msm.cu:50-61 / lib.rs Bls12_381MsmConfig"""
+    _fields_ = [(name, ctypes.c_uint32) for name in (
+        "domain_k", "min_msm_scalars", "unfiltered_min_scalars", "window_bits", "sort_grid_divisor",
+        "sort_window_lanes", "integration_blocks", "batch_lanes", "reuse_event", "device_reduce")]
+
+    @classmethod
+    def default(cls, npoints, window_bits=0):
+        k = max(0, (max(npoints, 1) - 1).bit_length())
+        return cls(k, 100000, 32768, window_bits, 3, 2, 1, 4, 0, 3)
+
+
+class RawMsmSlice(ctypes.Structure):
+    _fields_ = [("scalar_offset", ctypes.c_size_t), ("point_offset", ctypes.c_size_t),
+                ("len", ctypes.c_size_t), ("nonzero_len", ctypes.c_size_t)]
+
+
+class RawFr(ctypes.Structure):
+    _fields_ = [("limbs", ctypes.c_uint64 * 4)]
+
+
+_lib = None
+_libc = ctypes.CDLL(None)
+_libc.free.argtypes = [ctypes.c_void_p]
+
+
+def library_path():
+    return _build_lib.LIB
+
+
+def build(force=False, verbose=False):
+    return _build_lib.build(force=force, verbose=verbose)
+
+
+def _declare(L):
+    vp, sz, u32, b = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_bool
+    fr = RawFr
+    E = RustError
+    sigs = {
+        "midnight_sppark_execution_lane_set": (E, [u32]),
+        "midnight_sppark_bls12_381_g1_msm": (E, [vp, vp, vp, sz]),
+        "midnight_sppark_bls12_381_g1_msm_batch": (E, [vp, vp, vp, sz, sz]),
+        "midnight_sppark_bls12_381_g1_msm_context_create": (E, [vp, vp, sz]),
+        "midnight_sppark_bls12_381_g1_msm_context_create_with_config": (E, [vp, vp, sz, RawMsmConfig]),
+        "midnight_sppark_bls12_381_g1_msm_context_free": (None, [vp]),
+        "midnight_sppark_bls12_381_g1_msm_context_batch": (E, [vp, vp, vp, sz, sz]),
+        "midnight_sppark_bls12_381_g1_msm_context_device_batch": (E, [vp, vp, vp, sz, sz, sz]),
+        "midnight_sppark_bls12_381_g1_msm_context_device_ragged": (E, [vp, vp, vp, vp, sz]),
+        "midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch": (E, [vp, vp, vp, sz, sz, sz, vp]),
+        "midnight_sppark_bls12_381_fr_ntt": (E, [vp, u32, b]),
+        "midnight_sppark_bls12_381_fr_ntt_zeta": (E, [vp, u32, b, fr, fr, fr]),
+        "midnight_sppark_bls12_381_fr_divide_ntt_zeta": (E, [vp, u32, vp, sz, fr, fr, fr]),
+        "midnight_sppark_bls12_381_fr_coeff_to_extended_batch": (E, [vp, vp, sz, sz, u32, fr, fr]),
+        "midnight_sppark_bls12_381_fr_device_coeff_to_extended_batch": (E, [vp, vp, sz, sz, u32, fr, fr]),
+        "midnight_sppark_bls12_381_fr_device_coeff_to_extended_from_device_batch": (E, [vp, vp, sz, sz, u32, fr, fr]),
+        "midnight_sppark_bls12_381_fr_device_vec_ntt_zeta": (E, [vp, u32, b, fr, fr, fr]),
+        "midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch": (E, [vp, u32, sz, b, fr, fr, fr]),
+        "midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta": (E, [vp, u32, vp, sz, fr, fr, fr]),
+        "midnight_sppark_bls12_381_fr_mul_assign": (E, [vp, fr, sz]),
+        "midnight_sppark_bls12_381_fr_mul_assign_zeta": (E, [vp, fr, fr, sz]),
+        "midnight_sppark_bls12_381_fr_mul_assign_repeating": (E, [vp, vp, sz, sz]),
+        "midnight_sppark_bls12_381_fr_invert_assign": (E, [vp, sz]),
+        "midnight_sppark_bls12_381_fr_sort_canonical": (E, [vp, sz]),
+        "midnight_sppark_bls12_381_fr_poly_lincomb": (E, [vp, vp, sz, sz, vp]),
+        "midnight_sppark_bls12_381_fr_shifted_prefix_product": (E, [vp, fr, sz]),
+        "midnight_sppark_bls12_381_fr_permutation_products": (E, [vp, vp, vp, sz, sz, sz, fr, fr, fr, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_lookup_products": (E, [vp, vp, vp, vp, vp, sz, sz, fr, fr, vp, sz]),
+        "midnight_sppark_bls12_381_fr_lookup_products_device": (E, [vp, vp, sz, sz, fr, fr, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_quotient_pieces": (E, [vp, vp, sz, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_poly_lincomb": (E, [vp, vp, sz, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_upload": (E, [vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_upload_many": (E, [vp, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_download": (E, [vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_scatter_host": (E, [vp, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_concat_host": (E, [vp, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_concat_many_host": (E, [vp, vp, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_gather_polys": (E, [vp, vp, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_device_vec_free": (None, [vp]),
+        "gb_fr_device_vec_len": (sz, [vp]),
+        "gb_g1_generator_mul": (E, [vp, vp, sz]),
+        "gb_g1_generator_mul_device": (E, [vp, vp, sz]),
+        "gb_imad_peak": (E, [ctypes.POINTER(ctypes.c_double)]),
+        "gb_transfer_counters": (None, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+        "gb_transfer_counters_reset": (None, []),
+        "gb_error_free": (None, [vp]),
+        "gb_launch_counter": (ctypes.c_uint64, []),
+        "gb_lane_stream": (vp, []),
+        "gb_profile_enable": (None, [ctypes.c_int]),
+        "gb_profile_read": (None, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
+        "gb_profile_reset": (None, []),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return sigs
+
+
+def header_symbols():
+    """Every function name declared GB_API in include/gb_prover.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"GB_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
+
+
+def lib(build_if_stale=False):
+    """Load libgbprover.so (rebuilding it first if asked and out of date);
+    raise MsmError if it is absent -- there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if build_if_stale:
+        build()
+    if not os.path.exists(path):
+        raise MsmError(-1, "libgbprover.so not built at %s (run __graft_entry__.build())" % path)
+    L = ctypes.CDLL(path)
+    _declare(L)
+    _lib = L
+    return L
+
+
+def check(err):
+    """Turn a RustError into MsmError, freeing its message (lib.rs From<Error>)."""
+    if err.code == 0:
+        if err.message:
+            _libc.free(err.message)
+        return
+    msg = ""
+    if err.message:
+        msg = ctypes.string_at(err.message).decode("utf-8", "replace")
+        _libc.free(err.message)
+    raise MsmError(err.code, msg or ("sppark::Error #%d" % err.code))

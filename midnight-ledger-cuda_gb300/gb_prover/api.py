@@ -1,0 +1,406 @@
+"""Safe wrappers over the C ABI, named after midnight-sppark-msm/src/lib.rs.
+
+Each function validates shapes like its Rust counterpart (lib.rs:1470-4555)
+and raises MsmError on a non-zero RustError.  numpy uint64 arrays in the
+reference layout are used throughout: Fr (n, 4), affine (n, 12),
+projective (n, 18).
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import MsmError, RawFr, RawMsmConfig, RawMsmSlice, check, lib
+
+__all__ = [
+    "execution_lane_set", "bls12_381_g1_msm", "bls12_381_g1_msm_batch", "Bls12_381G1MsmContext",
+    "Bls12_381FrDeviceVec", "bls12_381_fr_ntt", "bls12_381_fr_ntt_zeta", "bls12_381_fr_divide_ntt_zeta",
+    "bls12_381_fr_coeff_to_extended_batch", "bls12_381_fr_device_coeff_to_extended_batch",
+    "bls12_381_fr_mul_assign", "bls12_381_fr_mul_assign_zeta", "bls12_381_fr_mul_assign_repeating",
+    "bls12_381_fr_invert_assign", "bls12_381_fr_sort_canonical", "bls12_381_fr_poly_lincomb",
+    "bls12_381_fr_shifted_prefix_product", "bls12_381_fr_permutation_products", "bls12_381_fr_lookup_products",
+    "bls12_381_fr_lookup_products_device", "bls12_381_fr_device_quotient_pieces",
+    "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "transfer_counters",
+    "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
+    "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT",
+]
+
+PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
+
+
+def _fr_arr(a):
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    return a.reshape(-1, 4)
+
+
+def _aff_arr(a):
+    return np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 12)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+def _fr(v):
+    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(4)
+    r = RawFr()
+    for i in range(4):
+        r.limbs[i] = int(v[i])
+    return r
+
+
+def execution_lane_set(lane):
+    check(lib().midnight_sppark_execution_lane_set(lane))
+
+
+# ---------------------------------------------------------------- MSM
+
+def bls12_381_g1_msm(points, scalars):
+    """lib.rs bls12_381_g1_msm: sum_i scalars[i] * points[i] (projective)."""
+    p, s = _aff_arr(points), _fr_arr(scalars)
+    if len(p) != len(s):
+        raise MsmError(-1, "point/scalar length mismatch: %d points, %d scalars" % (len(p), len(s)))
+    out = np.zeros(18, dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_g1_msm(_ptr(out), _ptr(p), _ptr(s), len(s)))
+    return out
+
+
+def bls12_381_g1_msm_batch(points, scalars_batch):
+    p = _aff_arr(points)
+    s = np.ascontiguousarray(scalars_batch, dtype=np.uint64).reshape(-1, len(p), 4)
+    out = np.zeros((len(s), 18), dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_g1_msm_batch(_ptr(out), _ptr(p), _ptr(s), len(p), len(s)))
+    return out
+
+
+class Bls12_381G1MsmContext:
+    """lib.rs Bls12_381G1MsmContext: bases uploaded once, reused per call."""
+
+    def __init__(self, points, config=None):
+        p = _aff_arr(points)
+        self.npoints = len(p)
+        cfg = config if config is not None else RawMsmConfig.default(self.npoints)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_g1_msm_context_create_with_config(ctypes.byref(h), _ptr(p),
+                                                                                len(p), cfg))
+        self.raw = h
+
+    def close(self):
+        if self.raw:
+            lib().midnight_sppark_bls12_381_g1_msm_context_free(self.raw)
+            self.raw = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def batch(self, scalars_batch, npoints=None):
+        n = self.npoints if npoints is None else npoints
+        s = np.ascontiguousarray(scalars_batch, dtype=np.uint64).reshape(-1, n, 4)
+        out = np.zeros((len(s), 18), dtype=np.uint64)
+        check(lib().midnight_sppark_bls12_381_g1_msm_context_batch(_ptr(out), self.raw, _ptr(s), n, len(s)))
+        return out
+
+    def msm(self, scalars):
+        return self.batch(_fr_arr(scalars)[None], npoints=len(_fr_arr(scalars)))[0]
+
+    def device_batch(self, devvec, scalar_offset, npoints, nmsms):
+        out = np.zeros((max(nmsms, 1), 18), dtype=np.uint64)
+        check(lib().midnight_sppark_bls12_381_g1_msm_context_device_batch(_ptr(out), self.raw, devvec.raw,
+                                                                         scalar_offset, npoints, nmsms))
+        return out[:nmsms]
+
+    def device_ragged(self, devvec, slices):
+        arr = (RawMsmSlice * max(len(slices), 1))()
+        for i, (so, po, ln) in enumerate(slices):
+            arr[i] = RawMsmSlice(so, po, ln, ln)
+        out = np.zeros((max(len(slices), 1), 18), dtype=np.uint64)
+        check(lib().midnight_sppark_bls12_381_g1_msm_context_device_ragged(_ptr(out), self.raw, devvec.raw,
+                                                                          ctypes.cast(arr, ctypes.c_void_p),
+                                                                          len(slices)))
+        return out[:len(slices)]
+
+    def device_scrambled_batch(self, devvec, scalar_offset, nmsms, mask_devvec):
+        out = np.zeros((max(nmsms, 1), 18), dtype=np.uint64)
+        check(lib().midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch(
+            _ptr(out), self.raw, devvec.raw, scalar_offset, self.npoints, nmsms, mask_devvec.raw))
+        return out[:nmsms]
+
+
+# ---------------------------------------------------------------- device vectors
+
+class Bls12_381FrDeviceVec:
+    """lib.rs Bls12_381FrDeviceVec: an opaque resident vector of Fr."""
+
+    def __init__(self, raw):
+        self.raw = ctypes.c_void_p(raw) if not isinstance(raw, ctypes.c_void_p) else raw
+        self.len = lib().gb_fr_device_vec_len(self.raw)
+
+    @classmethod
+    def upload(cls, values):
+        v = _fr_arr(values)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_upload(ctypes.byref(h), _ptr(v), len(v)))
+        return cls(h)
+
+    @classmethod
+    def upload_many(cls, slices):
+        arrs = [_fr_arr(s) for s in slices]
+        ptrs = (ctypes.c_void_p * max(len(arrs), 1))(*[_ptr(a) for a in arrs])
+        lens = (ctypes.c_size_t * max(len(arrs), 1))(*[len(a) for a in arrs])
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_upload_many(ctypes.byref(h), ptrs, lens, len(arrs)))
+        return cls(h)
+
+    def download(self, length=None):
+        n = self.len if length is None else length
+        out = np.zeros((n, 4), dtype=np.uint64)
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_download(_ptr(out), self.raw, n))
+        return out
+
+    def scatter_host(self, indices, values):
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        v = _fr_arr(values)
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_scatter_host(self.raw, _ptr(idx), _ptr(v), len(idx)))
+
+    def concat_host(self, suffix):
+        v = _fr_arr(suffix)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_concat_host(ctypes.byref(h), self.raw, _ptr(v), len(v)))
+        return Bls12_381FrDeviceVec(h)
+
+    @staticmethod
+    def concat_many_host(sources, suffix):
+        v = _fr_arr(suffix)
+        srcs = (ctypes.c_void_p * max(len(sources), 1))(*[s.raw.value for s in sources])
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_concat_many_host(ctypes.byref(h), srcs, len(sources),
+                                                                             _ptr(v), len(v)))
+        return Bls12_381FrDeviceVec(h)
+
+    def gather_polys(self, poly_len, indices):
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_gather_polys(ctypes.byref(h), self.raw, poly_len,
+                                                                         _ptr(idx), len(idx)))
+        return Bls12_381FrDeviceVec(h)
+
+    def ntt_zeta(self, log_n, inverse, scale, first, second):
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(self.raw, log_n, inverse, _fr(scale),
+                                                                      _fr(first), _fr(second)))
+
+    def ntt_zeta_batch(self, log_n, count, inverse, scale, first, second):
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(self.raw, log_n, count, inverse,
+                                                                            _fr(scale), _fr(first), _fr(second)))
+
+    def divide_ntt_zeta(self, log_n, factors, scale, first, second):
+        f = _fr_arr(factors)
+        check(lib().midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(self.raw, log_n, _ptr(f), len(f),
+                                                                             _fr(scale), _fr(first), _fr(second)))
+
+    def free(self):
+        if self.raw:
+            lib().midnight_sppark_bls12_381_fr_device_vec_free(self.raw)
+            self.raw = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- NTT
+
+def _log2_exact(n):
+    if n == 0 or n & (n - 1):
+        raise MsmError(-1, "NTT input length must be a power of two, got %d" % n)
+    return n.bit_length() - 1
+
+
+def bls12_381_fr_ntt(values, inverse=False):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_ntt(_ptr(v), _log2_exact(len(v)), inverse))
+    return v
+
+
+def bls12_381_fr_ntt_zeta(values, inverse, scale, first, second):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_ntt_zeta(_ptr(v), _log2_exact(len(v)), inverse, _fr(scale), _fr(first),
+                                                      _fr(second)))
+    return v
+
+
+def bls12_381_fr_divide_ntt_zeta(values, factors, scale, first, second):
+    v = _fr_arr(values).copy()
+    f = _fr_arr(factors)
+    check(lib().midnight_sppark_bls12_381_fr_divide_ntt_zeta(_ptr(v), _log2_exact(len(v)), _ptr(f), len(f),
+                                                             _fr(scale), _fr(first), _fr(second)))
+    return v
+
+
+def bls12_381_fr_coeff_to_extended_batch(inputs, extended_log_n, first, second):
+    a = np.ascontiguousarray(inputs, dtype=np.uint64)
+    a = a.reshape(a.shape[0], -1, 4) if a.ndim == 3 else a.reshape(1, -1, 4)
+    count, input_len = a.shape[0], a.shape[1]
+    out = np.zeros((count, 1 << extended_log_n, 4), dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_fr_coeff_to_extended_batch(_ptr(out), _ptr(a), input_len, count,
+                                                                      extended_log_n, _fr(first), _fr(second)))
+    return out
+
+
+def bls12_381_fr_device_coeff_to_extended_batch(inputs, extended_log_n, first, second):
+    a = np.ascontiguousarray(inputs, dtype=np.uint64)
+    a = a.reshape(a.shape[0], -1, 4) if a.ndim == 3 else a.reshape(1, -1, 4)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_device_coeff_to_extended_batch(ctypes.byref(h), _ptr(a), a.shape[1],
+                                                                            a.shape[0], extended_log_n, _fr(first),
+                                                                            _fr(second)))
+    return Bls12_381FrDeviceVec(h)
+
+
+# ---------------------------------------------------------------- vector ops
+
+def bls12_381_fr_mul_assign(values, scalar):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_mul_assign(_ptr(v), _fr(scalar), len(v)))
+    return v
+
+
+def bls12_381_fr_mul_assign_zeta(values, first, second):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_mul_assign_zeta(_ptr(v), _fr(first), _fr(second), len(v)))
+    return v
+
+
+def bls12_381_fr_mul_assign_repeating(values, factors):
+    v = _fr_arr(values).copy()
+    f = _fr_arr(factors)
+    check(lib().midnight_sppark_bls12_381_fr_mul_assign_repeating(_ptr(v), _ptr(f), len(f), len(v)))
+    return v
+
+
+def bls12_381_fr_invert_assign(values):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_invert_assign(_ptr(v), len(v)))
+    return v
+
+
+def bls12_381_fr_sort_canonical(values):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_sort_canonical(_ptr(v), len(v)))
+    return v
+
+
+def bls12_381_fr_poly_lincomb(polys, scalars):
+    p = np.ascontiguousarray(polys, dtype=np.uint64)
+    count = p.shape[0]
+    p = p.reshape(count, -1, 4)
+    k = _fr_arr(scalars)
+    out = np.zeros((p.shape[1], 4), dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_fr_poly_lincomb(_ptr(out), _ptr(p), p.shape[1], count, _ptr(k)))
+    return out
+
+
+def bls12_381_fr_shifted_prefix_product(values, initial):
+    v = _fr_arr(values).copy()
+    check(lib().midnight_sppark_bls12_381_fr_shifted_prefix_product(_ptr(v), _fr(initial), len(v)))
+    return v
+
+
+# ---------------------------------------------------------------- products
+
+def bls12_381_fr_permutation_products(columns, permutations, length, column_count, chunk_len, beta, gamma, omega,
+                                      delta_powers, blind_values, blinding_factors):
+    c = _fr_arr(columns)
+    p = _fr_arr(permutations)
+    d = _fr_arr(delta_powers)
+    b = _fr_arr(blind_values) if blind_values is not None and len(blind_values) else None
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_permutation_products(
+        ctypes.byref(h), _ptr(c), _ptr(p), length, column_count, chunk_len, _fr(beta), _fr(gamma), _fr(omega),
+        _ptr(d), _ptr(b), blinding_factors))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_lookup_products(ci, ct, pi, pt, length, lookup_count, beta, gamma, blind_values, blinding_factors):
+    arrs = [_fr_arr(x) for x in (ci, ct, pi, pt)]
+    b = _fr_arr(blind_values) if blind_values is not None and len(blind_values) else None
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_lookup_products(ctypes.byref(h), *[_ptr(a) for a in arrs], length,
+                                                             lookup_count, _fr(beta), _fr(gamma), _ptr(b),
+                                                             blinding_factors))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_lookup_products_device(trace, length, lookup_count, beta, gamma, blind_values, blinding_factors):
+    b = _fr_arr(blind_values) if blind_values is not None and len(blind_values) else None
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_lookup_products_device(ctypes.byref(h), trace.raw, length, lookup_count,
+                                                                    _fr(beta), _fr(gamma), _ptr(b), blinding_factors))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_device_quotient_pieces(quotient, poly_len, piece_count, blinds):
+    b = _fr_arr(blinds)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_device_quotient_pieces(ctypes.byref(h), quotient.raw, poly_len,
+                                                                    piece_count, _ptr(b), len(b)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_device_poly_lincomb(polys, poly_len, poly_count, scalars):
+    k = _fr_arr(scalars)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_device_poly_lincomb(ctypes.byref(h), polys.raw, poly_len, poly_count,
+                                                                 _ptr(k), len(k)))
+    return Bls12_381FrDeviceVec(h)
+
+
+# ---------------------------------------------------------------- additions
+
+def g1_generator_mul(scalars):
+    s = _fr_arr(scalars)
+    out = np.zeros((len(s), 12), dtype=np.uint64)
+    check(lib().gb_g1_generator_mul(_ptr(out), _ptr(s), len(s)))
+    return out
+
+
+def imad_peak():
+    v = ctypes.c_double()
+    check(lib().gb_imad_peak(ctypes.byref(v)))
+    return v.value
+
+
+def transfer_counters():
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    lib().gb_transfer_counters(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def transfer_counters_reset():
+    lib().gb_transfer_counters_reset()
+
+
+def launch_counter():
+    return lib().gb_launch_counter()
+
+
+def lane_stream():
+    """cudaStream_t of the calling thread's lane (as an int)."""
+    return lib().gb_lane_stream() or 0
+
+
+def profile_enable(on=True):
+    lib().gb_profile_enable(1 if on else 0)
+
+
+def profile_read(slot):
+    ms, n = ctypes.c_double(), ctypes.c_uint64()
+    lib().gb_profile_read(slot, ctypes.byref(ms), ctypes.byref(n))
+    return ms.value, n.value
+
+
+def profile_reset():
+    lib().gb_profile_reset()

@@ -1,0 +1,417 @@
+"""ctypes bindings of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as
+the checker.  Arrays are numpy uint64 with the reference's memory layout:
+Fr (n, 4), G1 affine (n, 12), G1 Jacobian (n, 18), all Montgomery form.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+R_MOD = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+P_MOD = int(
+    "1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab",
+    16,
+)
+FR_R = pow(2, 256, R_MOD)
+FR_RINV = pow(FR_R, -1, R_MOD)
+FP_R = pow(2, 384, P_MOD)
+FP_RINV = pow(FP_R, -1, P_MOD)
+
+CONST_ONE, CONST_GENERATOR, CONST_ROOT, CONST_ROOT_INV, CONST_DELTA, CONST_ZETA, CONST_TWO_INV = range(7)
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = ctypes.CDLL(path)
+        _declare(_lib)
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _declare(L):
+    vp, sz, u32, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int
+    sigs = {
+        "orc_fr_mul": (None, [vp, vp, vp]),
+        "orc_fr_add": (None, [vp, vp, vp]),
+        "orc_fr_sub": (None, [vp, vp, vp]),
+        "orc_fr_inv": (None, [vp, vp]),
+        "orc_fr_constant": (i32, [vp, i32]),
+        "orc_fr_from_uniform_bytes": (None, [vp, vp]),
+        "orc_fr_cmp_canonical": (i32, [vp, vp]),
+        "orc_fp_sqrt": (i32, [vp, vp]),
+        "orc_g1_generator": (None, [vp]),
+        "orc_g1_is_on_curve": (i32, [vp]),
+        "orc_g1_to_affine": (None, [vp, vp]),
+        "orc_g1_jac_to_affine_batch": (None, [vp, vp, sz]),
+        "orc_g1_from_affine": (None, [vp, vp]),
+        "orc_g1_add": (None, [vp, vp, vp]),
+        "orc_g1_add_affine": (None, [vp, vp, vp]),
+        "orc_g1_double": (None, [vp, vp]),
+        "orc_g1_neg": (None, [vp, vp]),
+        "orc_g1_mul": (None, [vp, vp, vp]),
+        "orc_g1_generator_mul_batch": (None, [vp, vp, sz, i32]),
+        "orc_g1_decompress": (i32, [vp, vp]),
+        "orc_g1_compress": (None, [vp, vp]),
+        "orc_g1_from_uncompressed": (i32, [vp, vp]),
+        "orc_g1_to_uncompressed": (None, [vp, vp]),
+        "orc_booth_index": (ctypes.c_int32, [sz, sz, vp]),
+        "orc_g1_msm_naive": (None, [vp, vp, vp, sz]),
+        "orc_g1_msm": (None, [vp, vp, vp, sz, i32, i32]),
+        "orc_fr_fft": (None, [vp, u32, vp, i32]),
+        "orc_fr_omega": (None, [vp, u32]),
+        "orc_fr_ntt": (None, [vp, u32, i32, i32]),
+        "orc_fr_mul_assign_zeta": (None, [vp, vp, vp, sz]),
+        "orc_fr_mul_assign": (None, [vp, vp, sz]),
+        "orc_fr_mul_assign_repeating": (None, [vp, vp, sz, sz]),
+        "orc_fr_ntt_zeta": (None, [vp, u32, i32, vp, vp, vp, i32]),
+        "orc_fr_divide_ntt_zeta": (None, [vp, u32, vp, sz, vp, vp, vp, i32]),
+        "orc_fr_coeff_to_extended_batch": (i32, [vp, vp, sz, sz, u32, vp, vp, i32]),
+        "orc_domain_extended_k": (u32, [u32, u32]),
+        "orc_domain_t_evaluations": (None, [vp, u32, u32]),
+        "orc_fr_batch_invert": (None, [vp, sz]),
+        "orc_fr_shifted_prefix_product": (None, [vp, vp, sz]),
+        "orc_fr_permutation_products": (i32, [vp, vp, vp, sz, sz, sz, vp, vp, vp, vp, vp, sz]),
+        "orc_fr_lookup_products": (i32, [vp, vp, vp, vp, vp, sz, sz, vp, vp, vp, sz]),
+        "orc_fr_poly_lincomb": (None, [vp, vp, sz, sz, vp]),
+        "orc_fr_quotient_pieces": (i32, [vp, vp, sz, sz, sz, vp, sz]),
+        "orc_fr_sort_canonical": (None, [vp, sz]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def threads_default():
+    return max(1, os.cpu_count() or 1)
+
+
+# ---------------------------------------------------------------- conversions
+
+def int_to_limbs(v, n):
+    return [(v >> (64 * i)) & 0xFFFFFFFFFFFFFFFF for i in range(n)]
+
+
+def limbs_to_int(row):
+    return sum(int(x) << (64 * i) for i, x in enumerate(row))
+
+
+def fr_from_ints(vals):
+    """canonical ints -> Montgomery Fr array (n, 4)"""
+    out = np.empty((len(vals), 4), dtype=np.uint64)
+    for i, v in enumerate(vals):
+        out[i] = int_to_limbs((int(v) % R_MOD) * FR_R % R_MOD, 4)
+    return out
+
+
+def fr_to_ints(arr):
+    arr = np.asarray(arr, dtype=np.uint64).reshape(-1, 4)
+    return [limbs_to_int(r) * FR_RINV % R_MOD for r in arr]
+
+
+def fp_from_int(v):
+    return np.array(int_to_limbs((v % P_MOD) * FP_R % P_MOD, 6), dtype=np.uint64)
+
+
+def fp_to_int(row):
+    return limbs_to_int(row) * FP_RINV % P_MOD
+
+
+def fr_random(n, rng):
+    """Uniform Fr elements (Fq::random-style rejection, fq.rs:373-387),
+    returned as Montgomery limbs; a uniform canonical value read as a
+    Montgomery representation is itself uniform in Fr."""
+    out = np.empty((n, 4), dtype=np.uint64)
+    filled = 0
+    top = np.uint64(0x7FFFFFFFFFFFFFFF)
+    rl = np.array(int_to_limbs(R_MOD, 4), dtype=np.uint64)
+    while filled < n:
+        k = int((n - filled) * 1.3) + 16
+        cand = rng.integers(0, 2**64, size=(k, 4), dtype=np.uint64)
+        cand[:, 3] &= top
+        # keep cand < r (lexicographic on limbs from the top)
+        lt = np.zeros(k, dtype=bool)
+        eq = np.ones(k, dtype=bool)
+        for i in (3, 2, 1, 0):
+            lt |= eq & (cand[:, i] < rl[i])
+            eq &= cand[:, i] == rl[i]
+        cand = cand[lt]
+        take = min(len(cand), n - filled)
+        out[filled:filled + take] = cand[:take]
+        filled += take
+    return out
+
+
+# ---------------------------------------------------------------- wrappers
+
+def fr_const(which):
+    o = np.zeros(4, dtype=np.uint64)
+    lib().orc_fr_constant(_p(o), which)
+    return o
+
+
+def fr_mul(a, b):
+    o = np.zeros(4, dtype=np.uint64)
+    lib().orc_fr_mul(_p(o), _p(np.ascontiguousarray(a, dtype=np.uint64)),
+                     _p(np.ascontiguousarray(b, dtype=np.uint64)))
+    return o
+
+
+def fr_inv(a):
+    o = np.zeros(4, dtype=np.uint64)
+    lib().orc_fr_inv(_p(o), _p(np.ascontiguousarray(a, dtype=np.uint64)))
+    return o
+
+
+def fr_omega(k):
+    o = np.zeros(4, dtype=np.uint64)
+    lib().orc_fr_omega(_p(o), k)
+    return o
+
+
+def g1_generator():
+    o = np.zeros(12, dtype=np.uint64)
+    lib().orc_g1_generator(_p(o))
+    return o
+
+
+def g1_generator_mul_batch(scalars, threads=None):
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros((len(s), 12), dtype=np.uint64)
+    lib().orc_g1_generator_mul_batch(_p(o), _p(s), len(s), threads or threads_default())
+    return o
+
+
+def g1_to_affine(jac):
+    j = np.ascontiguousarray(jac, dtype=np.uint64).reshape(-1, 18)
+    o = np.zeros((len(j), 12), dtype=np.uint64)
+    lib().orc_g1_jac_to_affine_batch(_p(o), _p(j), len(j))
+    return o
+
+
+def g1_is_on_curve(aff):
+    return bool(lib().orc_g1_is_on_curve(_p(np.ascontiguousarray(aff, dtype=np.uint64))))
+
+
+def g1_msm(bases, scalars, threads=None, window_bits=0):
+    b = np.ascontiguousarray(bases, dtype=np.uint64).reshape(-1, 12)
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    assert len(b) == len(s)
+    o = np.zeros(18, dtype=np.uint64)
+    lib().orc_g1_msm(_p(o), _p(b), _p(s), len(s), threads or threads_default(), window_bits)
+    return o
+
+
+def g1_msm_naive(bases, scalars):
+    b = np.ascontiguousarray(bases, dtype=np.uint64).reshape(-1, 12)
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros(18, dtype=np.uint64)
+    lib().orc_g1_msm_naive(_p(o), _p(b), _p(s), len(s))
+    return o
+
+
+def g1_add(a, b):
+    o = np.zeros(18, dtype=np.uint64)
+    lib().orc_g1_add(_p(o), _p(np.ascontiguousarray(a, dtype=np.uint64)),
+                     _p(np.ascontiguousarray(b, dtype=np.uint64)))
+    return o
+
+
+def g1_from_affine(a):
+    o = np.zeros(18, dtype=np.uint64)
+    lib().orc_g1_from_affine(_p(o), _p(np.ascontiguousarray(a, dtype=np.uint64)))
+    return o
+
+
+def g1_mul(p_aff, scalar):
+    o = np.zeros(18, dtype=np.uint64)
+    lib().orc_g1_mul(_p(o), _p(np.ascontiguousarray(p_aff, dtype=np.uint64)),
+                     _p(np.ascontiguousarray(scalar, dtype=np.uint64)))
+    return o
+
+
+def g1_decompress(b48):
+    buf = np.frombuffer(bytes(b48), dtype=np.uint8).copy()
+    o = np.zeros(12, dtype=np.uint64)
+    rc = lib().orc_g1_decompress(_p(o), _p(buf))
+    if rc:
+        raise ValueError("invalid compressed point (code %d)" % rc)
+    return o
+
+
+def g1_compress(aff):
+    o = np.zeros(48, dtype=np.uint8)
+    lib().orc_g1_compress(_p(o), _p(np.ascontiguousarray(aff, dtype=np.uint64)))
+    return o.tobytes()
+
+
+def g1_from_uncompressed(b96):
+    buf = np.frombuffer(bytes(b96), dtype=np.uint8).copy()
+    o = np.zeros(12, dtype=np.uint64)
+    rc = lib().orc_g1_from_uncompressed(_p(o), _p(buf))
+    if rc:
+        raise ValueError("invalid uncompressed point (code %d)" % rc)
+    return o
+
+
+def g1_to_uncompressed(aff):
+    o = np.zeros(96, dtype=np.uint8)
+    lib().orc_g1_to_uncompressed(_p(o), _p(np.ascontiguousarray(aff, dtype=np.uint64)))
+    return o.tobytes()
+
+
+def booth_index(window_index, window_size, scalar_le32):
+    buf = np.frombuffer(bytes(scalar_le32), dtype=np.uint8).copy()
+    return lib().orc_booth_index(window_index, window_size, _p(buf))
+
+
+def fr_fft(a, log_n, omega, threads=None):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_fft(_p(a), log_n, _p(np.ascontiguousarray(omega, dtype=np.uint64)),
+                     threads or threads_default())
+    return a
+
+
+def fr_ntt(a, log_n, inverse, threads=None):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_ntt(_p(a), log_n, int(inverse), threads or threads_default())
+    return a
+
+
+def fr_ntt_zeta(a, log_n, inverse, scale, first, second, threads=None):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_ntt_zeta(_p(a), log_n, int(inverse), _p(np.ascontiguousarray(scale, dtype=np.uint64)),
+                          _p(np.ascontiguousarray(first, dtype=np.uint64)),
+                          _p(np.ascontiguousarray(second, dtype=np.uint64)), threads or threads_default())
+    return a
+
+
+def fr_divide_ntt_zeta(a, log_n, factors, scale, first, second, threads=None):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    f = np.ascontiguousarray(factors, dtype=np.uint64).reshape(-1, 4)
+    lib().orc_fr_divide_ntt_zeta(_p(a), log_n, _p(f), len(f),
+                                 _p(np.ascontiguousarray(scale, dtype=np.uint64)),
+                                 _p(np.ascontiguousarray(first, dtype=np.uint64)),
+                                 _p(np.ascontiguousarray(second, dtype=np.uint64)),
+                                 threads or threads_default())
+    return a
+
+
+def fr_coeff_to_extended_batch(inputs, input_len, count, ext_log_n, first, second, threads=None):
+    i = np.ascontiguousarray(inputs, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros((count << ext_log_n, 4), dtype=np.uint64)
+    rc = lib().orc_fr_coeff_to_extended_batch(_p(o), _p(i), input_len, count, ext_log_n,
+                                              _p(np.ascontiguousarray(first, dtype=np.uint64)),
+                                              _p(np.ascontiguousarray(second, dtype=np.uint64)),
+                                              threads or threads_default())
+    if rc:
+        raise ValueError("coeff_to_extended: input longer than the extended domain")
+    return o
+
+
+def fr_mul_assign_zeta(a, first, second):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_mul_assign_zeta(_p(a), _p(np.ascontiguousarray(first, dtype=np.uint64)),
+                                 _p(np.ascontiguousarray(second, dtype=np.uint64)), len(a))
+    return a
+
+
+def fr_mul_assign(a, s):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_mul_assign(_p(a), _p(np.ascontiguousarray(s, dtype=np.uint64)), len(a))
+    return a
+
+
+def fr_mul_assign_repeating(a, factors):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    f = np.ascontiguousarray(factors, dtype=np.uint64).reshape(-1, 4)
+    lib().orc_fr_mul_assign_repeating(_p(a), _p(f), len(f), len(a))
+    return a
+
+
+def domain_extended_k(j, k):
+    return lib().orc_domain_extended_k(j, k)
+
+
+def domain_t_evaluations(j, k):
+    ek = domain_extended_k(j, k)
+    o = np.zeros((1 << (ek - k), 4), dtype=np.uint64)
+    lib().orc_domain_t_evaluations(_p(o), j, k)
+    return o
+
+
+def fr_batch_invert(a):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_batch_invert(_p(a), len(a))
+    return a
+
+
+def fr_shifted_prefix_product(a, initial):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_shifted_prefix_product(_p(a), _p(np.ascontiguousarray(initial, dtype=np.uint64)), len(a))
+    return a
+
+
+def fr_permutation_products(columns, permutations, length, column_count, chunk_len, beta, gamma,
+                            omega, delta_powers, blinds, blinding_factors):
+    sets = (column_count + chunk_len - 1) // chunk_len
+    o = np.zeros((sets * length, 4), dtype=np.uint64)
+    c = np.ascontiguousarray(columns, dtype=np.uint64)
+    pm = np.ascontiguousarray(permutations, dtype=np.uint64)
+    d = np.ascontiguousarray(delta_powers, dtype=np.uint64)
+    b = np.ascontiguousarray(blinds if blinds is not None else np.zeros((1, 4)), dtype=np.uint64)
+    rc = lib().orc_fr_permutation_products(_p(o), _p(c), _p(pm), length, column_count, chunk_len,
+                                           _p(np.ascontiguousarray(beta, dtype=np.uint64)),
+                                           _p(np.ascontiguousarray(gamma, dtype=np.uint64)),
+                                           _p(np.ascontiguousarray(omega, dtype=np.uint64)),
+                                           _p(d), _p(b), blinding_factors)
+    if rc:
+        raise ValueError("invalid permutation product arguments")
+    return o
+
+
+def fr_lookup_products(ci, ct, pi, pt, length, lookup_count, beta, gamma, blinds, blinding_factors):
+    o = np.zeros((lookup_count * length, 4), dtype=np.uint64)
+    arrs = [np.ascontiguousarray(x, dtype=np.uint64) for x in (ci, ct, pi, pt)]
+    b = np.ascontiguousarray(blinds if blinds is not None else np.zeros((1, 4)), dtype=np.uint64)
+    rc = lib().orc_fr_lookup_products(_p(o), *[_p(x) for x in arrs], length, lookup_count,
+                                      _p(np.ascontiguousarray(beta, dtype=np.uint64)),
+                                      _p(np.ascontiguousarray(gamma, dtype=np.uint64)),
+                                      _p(b), blinding_factors)
+    if rc:
+        raise ValueError("invalid lookup product arguments")
+    return o
+
+
+def fr_poly_lincomb(polys, poly_len, poly_count, scalars):
+    o = np.zeros((poly_len, 4), dtype=np.uint64)
+    lib().orc_fr_poly_lincomb(_p(o), _p(np.ascontiguousarray(polys, dtype=np.uint64)), poly_len,
+                              poly_count, _p(np.ascontiguousarray(scalars, dtype=np.uint64)))
+    return o
+
+
+def fr_quotient_pieces(quotient, poly_len, piece_count, blinds):
+    q = np.ascontiguousarray(quotient, dtype=np.uint64).reshape(-1, 4)
+    b = np.ascontiguousarray(blinds, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros((poly_len * piece_count, 4), dtype=np.uint64)
+    rc = lib().orc_fr_quotient_pieces(_p(o), _p(q), len(q), poly_len, piece_count, _p(b), len(b))
+    if rc:
+        raise ValueError("invalid quotient piece arguments")
+    return o
+
+
+def fr_sort_canonical(a):
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_sort_canonical(_p(a), len(a))
+    return a

@@ -1,0 +1,173 @@
+"""G1 multiexp on the GPU through the C ABI, bit-exact (affine) against the
+oracle: the reference's own test shapes, edge cases, every context entry
+point and the real-SRS known answers."""
+import numpy as np
+import pytest
+
+from conftest import affine_of
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_batch_scalars(orc, n, batch):
+    # midnight-sppark-msm/src/lib.rs:5033-5079: 1 / ((29i + 43b + 11) mod 65521 + 1)
+    R = orc.R_MOD
+    return orc.fr_from_ints([pow((i * 29 + batch * 43 + 11) % 65521 + 1, -1, R) for i in range(n)])
+
+
+def _check(orc, got_jac, bases, scalars):
+    want = affine_of(orc, orc.g1_msm(bases, scalars))
+    assert (affine_of(orc, got_jac) == want).all()
+
+
+def test_generator_mul_matches_oracle(gb, orc):
+    rng = np.random.default_rng(1)
+    s = orc.fr_random(1000, rng)
+    s[0] = 0
+    s[1] = orc.fr_from_ints([1])[0]
+    s[2] = orc.fr_from_ints([orc.R_MOD - 1])[0]
+    got = gb.g1_generator_mul(s)
+    assert (got == orc.g1_generator_mul_batch(s)).all()
+
+
+def test_msm_reference_shape_4096(gb, orc):
+    n = 4096
+    bases = orc.g1_generator_mul_batch(orc.fr_from_ints(list(range(1, n + 1))))
+    for b in range(2):
+        s = _ref_batch_scalars(orc, n, b)
+        _check(orc, gb.bls12_381_g1_msm(bases, s), bases, s)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 255, 1000, 1 << 12])
+def test_msm_random_sizes(gb, orc, n):
+    rng = np.random.default_rng(n)
+    s = orc.fr_random(n, rng)
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    _check(orc, gb.bls12_381_g1_msm(b, s), b, s)
+
+
+def test_msm_edge_cases(gb, orc):
+    rng = np.random.default_rng(7)
+    n = 3000
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    # all-zero scalars -> infinity
+    z = np.zeros((n, 4), dtype=np.uint64)
+    out = gb.bls12_381_g1_msm(b, z)
+    assert (out[12:18] == 0).all()
+    # empty input -> infinity
+    out = gb.bls12_381_g1_msm(np.zeros((0, 12), np.uint64), np.zeros((0, 4), np.uint64))
+    assert (out[12:18] == 0).all()
+    # max scalars, small scalars, repeated bases (bucket collisions: doubling
+    # and cancellation inside buckets), P and -P style cancellations
+    s = orc.fr_random(n, rng)
+    s[:100] = orc.fr_from_ints([orc.R_MOD - 1] * 100)
+    s[100:200] = orc.fr_from_ints([1] * 100)
+    s[200:300] = 0
+    b2 = b.copy()
+    b2[300:700] = b[0]
+    s[300:700] = orc.fr_from_ints([5] * 400)
+    s[700:800] = orc.fr_from_ints([orc.R_MOD - 5] * 100)
+    b2[700:800] = b[0]
+    _check(orc, gb.bls12_381_g1_msm(b2, s), b2, s)
+    # infinity among the bases
+    b3 = b.copy()
+    b3[10] = 0
+    _check(orc, gb.bls12_381_g1_msm(b3, s), b3, s)
+    # a sum that cancels to infinity exactly: s*P + (r-s)*P
+    pair_b = np.stack([b[1], b[1]])
+    pair_s = orc.fr_from_ints([12345, orc.R_MOD - 12345])
+    out = gb.bls12_381_g1_msm(pair_b, pair_s)
+    assert (out[12:18] == 0).all()
+
+
+def test_msm_batch_and_contexts(gb, orc):
+    rng = np.random.default_rng(9)
+    n = 5000
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
+    want = [affine_of(orc, orc.g1_msm(b, sb[i])) for i in range(3)]
+    got = gb.bls12_381_g1_msm_batch(b, sb)
+    for i in range(3):
+        assert (affine_of(orc, got[i]) == want[i]).all()
+    for window in (0, 9, 13, 16):
+        ctx = gb.Bls12_381G1MsmContext(b, gb.RawMsmConfig.default(n, window))
+        got = ctx.batch(sb)
+        for i in range(3):
+            assert (affine_of(orc, got[i]) == want[i]).all(), window
+        ctx.close()
+    ctx = gb.Bls12_381G1MsmContext(b)
+    dv = gb.Bls12_381FrDeviceVec.upload(np.concatenate([np.zeros((7, 4), np.uint64), sb.reshape(-1, 4)]))
+    got = ctx.device_batch(dv, 7, n, 3)
+    for i in range(3):
+        assert (affine_of(orc, got[i]) == want[i]).all()
+    # ragged slices: a prefix of the bases and a full-length slice
+    got = ctx.device_ragged(dv, [(7, 0, n), (7 + n, 0, 1000), (7 + 2 * n + 10, 10, 3000)])
+    assert (affine_of(orc, got[0]) == want[0]).all()
+    assert (affine_of(orc, got[1]) == affine_of(orc, orc.g1_msm(b[:1000], sb[1][:1000]))).all()
+    assert (affine_of(orc, got[2]) == affine_of(orc, orc.g1_msm(b[10:3010], sb[2][10:3010]))).all()
+    # scrambled: MSM(s + mask)
+    mask = orc.fr_random(n, rng)
+    mv = gb.Bls12_381FrDeviceVec.upload(mask)
+    got = ctx.device_scrambled_batch(dv, 7, 3, mv)
+    R = orc.R_MOD
+    mi = orc.fr_to_ints(mask)
+    for i in range(3):
+        si = orc.fr_to_ints(sb[i])
+        masked = orc.fr_from_ints([(x + y) % R for x, y in zip(si, mi)])
+        assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, masked))).all()
+    ctx.close()
+
+
+def test_msm_2p16(gb, orc):
+    """The 2^16 configuration: uniform scalars, bases [r_i]G."""
+    rng = np.random.default_rng(16)
+    n = 1 << 16
+    s = orc.fr_random(n, rng)
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    want = affine_of(orc, orc.g1_msm(b, s))
+    assert (affine_of(orc, gb.bls12_381_g1_msm(b, s)) == want).all()
+    ctx = gb.Bls12_381G1MsmContext(b)
+    assert (affine_of(orc, ctx.msm(s)) == want).all()
+    ctx.close()
+
+
+def test_msm_real_srs_known_answers(gb, orc, srs):
+    """Real bases from the reference's k=14 SRS: MSM(g_lagrange, 1) = G and
+    MSM(g_lagrange, v) = MSM(g, iNTT(v)) with the NTT also on the GPU."""
+    k, g, gl = srs
+    n = 1 << k
+    ones = orc.fr_from_ints([1] * n)
+    assert (affine_of(orc, gb.bls12_381_g1_msm(gl, ones))[0] == g[0]).all()
+    rng = np.random.default_rng(14)
+    v = orc.fr_random(n, rng)
+    coeffs = gb.bls12_381_fr_ntt(v, inverse=True)
+    assert (coeffs == orc.fr_ntt(v, k, True)).all()
+    ctx_g = gb.Bls12_381G1MsmContext(g)
+    ctx_l = gb.Bls12_381G1MsmContext(gl)
+    a = affine_of(orc, ctx_l.msm(v))
+    b = affine_of(orc, ctx_g.msm(coeffs))
+    assert (a == b).all()
+    assert (a == affine_of(orc, orc.g1_msm(gl, v))).all()
+    ctx_g.close()
+    ctx_l.close()
+
+
+def test_msm_2p20_linearity(gb, orc):
+    """Full-size property: MSM(s + t) = MSM(s) + MSM(t) at n = 2^20 on the
+    GPU (both context and plain paths), one oracle check of MSM(s)."""
+    rng = np.random.default_rng(20)
+    n = 1 << 20
+    s = orc.fr_random(n, rng)
+    t = orc.fr_random(n, rng)
+    R = orc.R_MOD
+    st = orc.fr_from_ints([(x + y) % R for x, y in zip(orc.fr_to_ints(s), orc.fr_to_ints(t))])
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    ctx = gb.Bls12_381G1MsmContext(b)
+    res = ctx.batch(np.stack([s, t, st]))
+    lhs = affine_of(orc, res[2])
+    rhs = affine_of(orc, orc.g1_add(res[0], res[1]))
+    assert (lhs == rhs).all()
+    assert (affine_of(orc, res[0]) == affine_of(orc, orc.g1_msm(b, s))).all()
+    plain = gb.bls12_381_g1_msm(b, t)
+    assert (affine_of(orc, plain) == affine_of(orc, res[1])).all()
+    ctx.close()
