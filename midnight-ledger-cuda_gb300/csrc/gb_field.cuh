@@ -9,12 +9,13 @@
 // vendor/midnight-curves-0.3.1/src/bls12_381/fq.rs:25-29): little-endian
 // limbs, Montgomery form, every stored value fully reduced into [0, m).
 //
-// Multiplication is CIOS Montgomery multiplication.  On the device the
-// carry chains are written as inline PTX (mad.lo.cc / madc.hi.cc on 32-bit
-// limbs, split into even and odd partial-product rows so the two carry chains
-// are independent); a portable C version of the same algorithm is kept for
-// host builds of this header, which the CPU test suite uses to check the
-// limb logic against the oracle without a GPU.
+// Multiplication is CIOS Montgomery multiplication.  On the device each
+// multiply-accumulate row is one inline-PTX carry chain (mad.lo.cc /
+// madc.hi.cc on 32-bit limbs) in a single asm statement, with the partial
+// products split into an even-limb row and an odd-limb row; a portable C
+// version of the same algorithm is kept for host builds of this header, which
+// the CPU test suite uses to check the limb logic against the oracle without
+// a GPU.
 #pragma once
 
 #include <stdint.h>
@@ -87,58 +88,98 @@ struct FrCfg {
 // use 64-bit intermediates.  Both compute the same function.
 // ---------------------------------------------------------------------------
 
-#if defined(__CUDA_ARCH__)
-#define GB_ADDC_FIRST(d, a, b) asm("add.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#define GB_ADDC(d, a, b) asm("addc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#define GB_ADDC_LAST(d, a, b) asm("addc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#define GB_SUBC_FIRST(d, a, b) asm("sub.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#define GB_SUBC(d, a, b) asm("subc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#define GB_SUBC_LAST(d, a, b) asm("subc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b))
-#endif
-
-// out = a + b over N limbs; returns the carry out.
+// out = a + b over N limbs; returns the carry out.  Plain C with 64-bit
+// intermediates: the compiler owns the carry propagation.
 template <int N>
 GB_HD uint32_t mp_add(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
-#if defined(__CUDA_ARCH__)
-    uint32_t c;
-    GB_ADDC_FIRST(out[0], a[0], b[0]);
-#pragma unroll
-    for (int i = 1; i < N; i++) GB_ADDC(out[i], a[i], b[i]);
-    GB_ADDC_LAST(c, 0u, 0u);
-    return c;
-#else
     uint64_t c = 0;
+#pragma unroll
     for (int i = 0; i < N; i++) {
         uint64_t v = (uint64_t)a[i] + b[i] + c;
         out[i] = (uint32_t)v;
         c = v >> 32;
     }
     return (uint32_t)c;
-#endif
 }
 
 // out = a - b over N limbs; returns the borrow (1 if a < b).
 template <int N>
 GB_HD uint32_t mp_sub(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
-#if defined(__CUDA_ARCH__)
-    uint32_t br;
-    GB_SUBC_FIRST(out[0], a[0], b[0]);
-#pragma unroll
-    for (int i = 1; i < N; i++) GB_SUBC(out[i], a[i], b[i]);
-    GB_SUBC_LAST(br, 0u, 0u);
-    return br & 1u;
-#else
     uint64_t br = 0;
+#pragma unroll
     for (int i = 0; i < N; i++) {
         uint64_t v = (uint64_t)a[i] - b[i] - br;
         out[i] = (uint32_t)v;
         br = (v >> 32) & 1;
     }
     return (uint32_t)br;
-#endif
 }
+
+#if defined(__CUDA_ARCH__)
+// acc[0..N] += sum_k x[k] * y * 2^(64k) over 32-bit limbs: the low half of
+// x[k]*y lands on limb 2k, the high half on limb 2k+1, one carry chain,
+// final carry into acc[N].  The whole chain is ONE asm statement so nothing
+// can be scheduled between its carry-flag producers and consumers.
+GB_D void row_mac12(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, uint32_t x4,
+                    uint32_t x5, uint32_t y)
+{
+    asm volatile(
+        "mad.lo.cc.u32 %0, %13, %19, %0;\n\t"
+        "madc.hi.cc.u32 %1, %13, %19, %1;\n\t"
+        "madc.lo.cc.u32 %2, %14, %19, %2;\n\t"
+        "madc.hi.cc.u32 %3, %14, %19, %3;\n\t"
+        "madc.lo.cc.u32 %4, %15, %19, %4;\n\t"
+        "madc.hi.cc.u32 %5, %15, %19, %5;\n\t"
+        "madc.lo.cc.u32 %6, %16, %19, %6;\n\t"
+        "madc.hi.cc.u32 %7, %16, %19, %7;\n\t"
+        "madc.lo.cc.u32 %8, %17, %19, %8;\n\t"
+        "madc.hi.cc.u32 %9, %17, %19, %9;\n\t"
+        "madc.lo.cc.u32 %10, %18, %19, %10;\n\t"
+        "madc.hi.cc.u32 %11, %18, %19, %11;\n\t"
+        "addc.u32 %12, %12, 0;"
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+          "+r"(acc[7]), "+r"(acc[8]), "+r"(acc[9]), "+r"(acc[10]), "+r"(acc[11]), "+r"(acc[12])
+        : "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(x4), "r"(x5), "r"(y));
+}
+
+GB_D void row_mac8(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, uint32_t y)
+{
+    asm volatile(
+        "mad.lo.cc.u32 %0, %9, %13, %0;\n\t"
+        "madc.hi.cc.u32 %1, %9, %13, %1;\n\t"
+        "madc.lo.cc.u32 %2, %10, %13, %2;\n\t"
+        "madc.hi.cc.u32 %3, %10, %13, %3;\n\t"
+        "madc.lo.cc.u32 %4, %11, %13, %4;\n\t"
+        "madc.hi.cc.u32 %5, %11, %13, %5;\n\t"
+        "madc.lo.cc.u32 %6, %12, %13, %6;\n\t"
+        "madc.hi.cc.u32 %7, %12, %13, %7;\n\t"
+        "addc.u32 %8, %8, 0;"
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+          "+r"(acc[7]), "+r"(acc[8])
+        : "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(y));
+}
+
+// acc += x * y where x is given by its even (parity 0) or odd (parity 1)
+// limbs: x[parity + 2k] for k < N/2
+template <int N>
+GB_D void row_mac(uint32_t *acc, const uint32_t *x, int parity, uint32_t y);
+
+template <>
+GB_D void row_mac<12>(uint32_t *acc, const uint32_t *x, int parity, uint32_t y)
+{
+    if (parity == 0) row_mac12(acc, x[0], x[2], x[4], x[6], x[8], x[10], y);
+    else row_mac12(acc, x[1], x[3], x[5], x[7], x[9], x[11], y);
+}
+
+template <>
+GB_D void row_mac<8>(uint32_t *acc, const uint32_t *x, int parity, uint32_t y)
+{
+    if (parity == 0) row_mac8(acc, x[0], x[2], x[4], x[6], y);
+    else row_mac8(acc, x[1], x[3], x[5], x[7], y);
+}
+#endif
 
 template <class Cfg>
 struct mont_t {
@@ -281,66 +322,38 @@ struct mont_t {
 
 #if defined(__CUDA_ARCH__)
 // Device CIOS: for each limb b[i], accumulate a*b[i] and m*p into the running
-// sum using two interleaved carry chains (even-indexed products land on even
-// limbs with their high halves on odd limbs, and vice versa).
+// sum held as two rows, `even` (products of even-indexed limbs) and `odd`
+// (products of odd-indexed limbs, stored one limb lower), so each row is a
+// single uninterrupted carry chain; the rows are folded once per iteration
+// while dividing by 2^32.
 template <class Cfg>
 GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
     constexpr int N = Cfg::N;
-    uint32_t even[N + 1], odd[N + 1];
+    uint32_t even[N + 1], odd[N + 1], mod[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) mod[i] = Cfg::mod(i);
 #pragma unroll
     for (int i = 0; i < N + 1; i++) { even[i] = 0; odd[i] = 0; }
 
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t bi = b[i];
-        // even += a[2j]*bi (lo at 2j, hi at 2j+1)
-        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[0]) : "r"(a[0]), "r"(bi));
-        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[1]) : "r"(a[0]), "r"(bi));
-#pragma unroll
-        for (int j = 2; j < N; j += 2) {
-            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[j]) : "r"(a[j]), "r"(bi));
-            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[j + 1]) : "r"(a[j]), "r"(bi));
-        }
-        asm("addc.u32 %0, %0, 0;" : "+r"(even[N]));
-        // odd += a[2j+1]*bi (lo at 2j+1 -> stored at odd[2j], hi at odd[2j+1])
-        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[0]) : "r"(a[1]), "r"(bi));
-        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[1]) : "r"(a[1]), "r"(bi));
-#pragma unroll
-        for (int j = 2; j < N; j += 2) {
-            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j]) : "r"(a[j + 1]), "r"(bi));
-            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j + 1]) : "r"(a[j + 1]), "r"(bi));
-        }
-        asm("addc.u32 %0, %0, 0;" : "+r"(odd[N]));
-        // Here the value is even[0..N] + odd[0..N] * 2^32.
-        // Montgomery step: m = even[0] * inv; add m*p (even limbs of p into
-        // even, odd limbs of p into odd), after which even[0] == 0.
+        row_mac<N>(even, a, 0, bi);
+        row_mac<N>(odd, a, 1, bi);
+        // value = even + odd * 2^32; Montgomery step makes even[0] zero
         const uint32_t m = even[0] * Cfg::INV;
-        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[0]) : "r"(m), "r"(Cfg::mod(0)));
-        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[1]) : "r"(m), "r"(Cfg::mod(0)));
+        row_mac<N>(even, mod, 0, m);
+        row_mac<N>(odd, mod, 1, m);
+        // value / 2^32 = even[1..N] + odd[0..N]
+        uint64_t c = 0;
 #pragma unroll
-        for (int j = 2; j < N; j += 2) {
-            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(even[j]) : "r"(m), "r"(Cfg::mod(j)));
-            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(even[j + 1]) : "r"(m), "r"(Cfg::mod(j)));
+        for (int j = 0; j < N; j++) {
+            uint64_t v = (uint64_t)even[j + 1] + odd[j] + c;
+            even[j] = (uint32_t)v;
+            c = v >> 32;
         }
-        asm("addc.u32 %0, %0, 0;" : "+r"(even[N]));
-        asm("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[0]) : "r"(m), "r"(Cfg::mod(1)));
-        asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[1]) : "r"(m), "r"(Cfg::mod(1)));
-#pragma unroll
-        for (int j = 2; j < N; j += 2) {
-            asm("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j]) : "r"(m), "r"(Cfg::mod(j + 1)));
-            asm("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(odd[j + 1]) : "r"(m), "r"(Cfg::mod(j + 1)));
-        }
-        asm("addc.u32 %0, %0, 0;" : "+r"(odd[N]));
-        // Divide by 2^32: the new value is odd[0..N] + even[1..N] * 2^0 ...
-        // value = even + odd*2^32 with even[0] == 0, so
-        // value / 2^32 = even[1..N] + odd[0..N]; fold into `even` as the
-        // running sum and clear `odd`.
-        asm("add.cc.u32 %0, %1, %2;" : "=r"(even[0]) : "r"(even[1]), "r"(odd[0]));
-#pragma unroll
-        for (int j = 1; j < N; j++)
-            asm("addc.cc.u32 %0, %1, %2;" : "=r"(even[j]) : "r"(even[j + 1]), "r"(odd[j]));
-        asm("addc.u32 %0, %1, 0;" : "=r"(even[N]) : "r"(odd[N]));
+        even[N] = odd[N] + (uint32_t)c;
 #pragma unroll
         for (int j = 0; j < N + 1; j++) odd[j] = 0;
     }
