@@ -229,6 +229,20 @@ GB_API void *gb_lane_stream(void);
 GB_API void gb_profile_enable(int on);
 GB_API void gb_profile_read(int slot, double *total_ms, uint64_t *launches);
 GB_API void gb_profile_reset(void);
+/* Allocation-free shifted prefix product; no counterpart in the reference.
+ * For callers that cannot allocate device memory when they need it (a
+ * server that reserved its HBM budget up front, or a prover lane that must
+ * not trigger the device-wide synchronisation of cudaMalloc/cudaFree): in
+ * place on caller-owned device memory, z[0] = initial,
+ * z[i] = initial * prod_{j<i} values[j], same result as
+ * midnight_sppark_bls12_381_fr_shifted_prefix_product.  Scratch is a fixed
+ * 64 KiB device array per GPU (held until exit), so len <= 4194304 (2^22);
+ * longer inputs get cudaErrorInvalidValue.  Queued on `stream` (NULL = the
+ * calling thread's lane) and returns without waiting.  All calls share the
+ * scratch: calls that overlap on the GPU (unordered streams) race.  The first
+ * call on a device looks up the scratch address; make it before any stream
+ * capture on that device. */
+GB_API RustError gb_fr_shifted_prefix_product_noalloc(RawFr *d_values, RawFr initial, size_t len, void *stream);
 /* releases a RustError message for callers without access to free() */
 GB_API void gb_error_free(char *message);
 

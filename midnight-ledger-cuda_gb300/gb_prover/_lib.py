@@ -118,6 +118,7 @@ def _declare(L):
         "gb_profile_enable": (None, [ctypes.c_int]),
         "gb_profile_read": (None, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
         "gb_profile_reset": (None, []),
+        "gb_fr_shifted_prefix_product_noalloc": (E, [vp, fr, sz, vp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
