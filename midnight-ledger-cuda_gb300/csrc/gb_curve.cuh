@@ -200,8 +200,11 @@ struct xyzz_t {
 // scalar multiplication by a small unsigned integer k (double-and-add)
 GB_COLD xyzz_t xyzz_mul_small(const xyzz_t &p, uint32_t k)
 {
-    xyzz_t acc = xyzz_t::inf();
-    for (int i = 31; i >= 0; i--) {
+    if (k == 0) return xyzz_t::inf();
+    int top = 31;
+    while (!((k >> top) & 1u)) top--;
+    xyzz_t acc = p;
+    for (int i = top - 1; i >= 0; i--) {
         acc = acc.dbl();
         if ((k >> i) & 1u) acc.add(p);
     }

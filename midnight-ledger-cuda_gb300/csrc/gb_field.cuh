@@ -37,6 +37,9 @@ namespace gb {
 struct FpCfg {
     static constexpr int N = 12;
     static constexpr uint32_t INV = 0xfffcfffdu;  // -p^-1 mod 2^32
+    static constexpr uint32_t M0 = 0xffffaaabu, M1 = 0xb9feffffu, M2 = 0xb153ffffu, M3 = 0x1eabfffeu,
+                              M4 = 0xf6b0f624u, M5 = 0x6730d2a0u, M6 = 0xf38512bfu, M7 = 0x64774b84u,
+                              M8 = 0x434bacd7u, M9 = 0x4b1ba7b6u, M10 = 0x397fe69au, M11 = 0x1a0111eau;
     GB_HD static uint32_t mod(int i)
     {
         constexpr uint32_t P[12] = {0xffffaaabu, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu,
@@ -63,6 +66,8 @@ struct FpCfg {
 struct FrCfg {
     static constexpr int N = 8;
     static constexpr uint32_t INV = 0xffffffffu;  // -r^-1 mod 2^32
+    static constexpr uint32_t M0 = 0x00000001u, M1 = 0xffffffffu, M2 = 0xfffe5bfeu, M3 = 0x53bda402u,
+                              M4 = 0x09a1d805u, M5 = 0x3339d808u, M6 = 0x299d7d48u, M7 = 0x73eda753u;
     GB_HD static uint32_t mod(int i)
     {
         constexpr uint32_t P[8] = {0x00000001u, 0xffffffffu, 0xfffe5bfeu, 0x53bda402u,
@@ -120,12 +125,14 @@ GB_HD uint32_t mp_sub(uint32_t *out, const uint32_t *a, const uint32_t *b)
 #if defined(__CUDA_ARCH__)
 // acc[0..N] += sum_k x[k] * y * 2^(64k) over 32-bit limbs: the low half of
 // x[k]*y lands on limb 2k, the high half on limb 2k+1, one carry chain,
-// final carry into acc[N].  The whole chain is ONE asm statement so nothing
-// can be scheduled between its carry-flag producers and consumers.
+// final carry into acc[N].  The whole chain is ONE asm statement that starts
+// without a carry-in and ends by absorbing its carry, so no carry crosses a
+// statement boundary and the compiler may freely interleave independent
+// chains (the statements are deliberately not volatile).
 GB_D void row_mac12(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, uint32_t x4,
                     uint32_t x5, uint32_t y)
 {
-    asm volatile(
+    asm(
         "mad.lo.cc.u32 %0, %13, %19, %0;\n\t"
         "madc.hi.cc.u32 %1, %13, %19, %1;\n\t"
         "madc.lo.cc.u32 %2, %14, %19, %2;\n\t"
@@ -146,7 +153,7 @@ GB_D void row_mac12(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32
 
 GB_D void row_mac8(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, uint32_t y)
 {
-    asm volatile(
+    asm(
         "mad.lo.cc.u32 %0, %9, %13, %0;\n\t"
         "madc.hi.cc.u32 %1, %9, %13, %1;\n\t"
         "madc.lo.cc.u32 %2, %10, %13, %2;\n\t"
@@ -160,6 +167,105 @@ GB_D void row_mac8(uint32_t *acc, uint32_t x0, uint32_t x1, uint32_t x2, uint32_
           "+r"(acc[7]), "+r"(acc[8])
         : "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(y));
 }
+
+// acc += modulus * m, modulus limbs as immediates (no registers held for them)
+#define GB_ROW12_IMM(acc, x0, x1, x2, x3, x4, x5, y)                                                    \
+    asm("mad.lo.cc.u32 %0, %13, %14, %0;\n\t"                                                         \
+        "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"                                                        \
+        "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"                                                        \
+        "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"                                                        \
+        "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"                                                        \
+        "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"                                                        \
+        "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"                                                        \
+        "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"                                                        \
+        "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"                                                        \
+        "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"                                                        \
+        "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"                                                      \
+        "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"                                                      \
+        "addc.u32 %12, %12, 0;"                                                                         \
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]),          \
+          "+r"(acc[6]), "+r"(acc[7]), "+r"(acc[8]), "+r"(acc[9]), "+r"(acc[10]), "+r"(acc[11]),        \
+          "+r"(acc[12])                                                                                 \
+        : "r"(y), "n"(x0), "n"(x1), "n"(x2), "n"(x3), "n"(x4), "n"(x5))
+
+#define GB_ROW8_IMM(acc, x0, x1, x2, x3, y)                                                             \
+    asm("mad.lo.cc.u32 %0, %9, %10, %0;\n\t"                                                          \
+        "madc.hi.cc.u32 %1, %9, %10, %1;\n\t"                                                         \
+        "madc.lo.cc.u32 %2, %9, %11, %2;\n\t"                                                         \
+        "madc.hi.cc.u32 %3, %9, %11, %3;\n\t"                                                         \
+        "madc.lo.cc.u32 %4, %9, %12, %4;\n\t"                                                         \
+        "madc.hi.cc.u32 %5, %9, %12, %5;\n\t"                                                         \
+        "madc.lo.cc.u32 %6, %9, %13, %6;\n\t"                                                         \
+        "madc.hi.cc.u32 %7, %9, %13, %7;\n\t"                                                         \
+        "addc.u32 %8, %8, 0;"                                                                           \
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]),          \
+          "+r"(acc[6]), "+r"(acc[7]), "+r"(acc[8])                                                      \
+        : "r"(y), "n"(x0), "n"(x1), "n"(x2), "n"(x3))
+
+template <class Cfg>
+GB_D void row_mac_mod(uint32_t *acc, int parity, uint32_t m);
+
+template <>
+GB_D void row_mac_mod<FpCfg>(uint32_t *acc, int parity, uint32_t m)
+{
+    typedef FpCfg C;
+    if (parity == 0) GB_ROW12_IMM(acc, C::M0, C::M2, C::M4, C::M6, C::M8, C::M10, m);
+    else GB_ROW12_IMM(acc, C::M1, C::M3, C::M5, C::M7, C::M9, C::M11, m);
+}
+
+template <>
+GB_D void row_mac_mod<FrCfg>(uint32_t *acc, int parity, uint32_t m)
+{
+    typedef FrCfg C;
+    if (parity == 0) GB_ROW8_IMM(acc, C::M0, C::M2, C::M4, C::M6, m);
+    else GB_ROW8_IMM(acc, C::M1, C::M3, C::M5, C::M7, m);
+}
+
+// even[0..N-1] = even[1..N] + odd[0..N-1], even[N] = odd[N] + carry: the
+// division by 2^32 that ends each CIOS step, as one carry chain
+GB_D void fold12(uint32_t *e, const uint32_t *o)
+{
+    asm("add.cc.u32 %0, %1, %13;\n\t"
+        "addc.cc.u32 %1, %2, %14;\n\t"
+        "addc.cc.u32 %2, %3, %15;\n\t"
+        "addc.cc.u32 %3, %4, %16;\n\t"
+        "addc.cc.u32 %4, %5, %17;\n\t"
+        "addc.cc.u32 %5, %6, %18;\n\t"
+        "addc.cc.u32 %6, %7, %19;\n\t"
+        "addc.cc.u32 %7, %8, %20;\n\t"
+        "addc.cc.u32 %8, %9, %21;\n\t"
+        "addc.cc.u32 %9, %10, %22;\n\t"
+        "addc.cc.u32 %10, %11, %23;\n\t"
+        "addc.cc.u32 %11, %12, %24;\n\t"
+        "addc.u32 %12, %25, 0;"
+        : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]),
+          "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "+r"(e[12])
+        : "r"(o[0]), "r"(o[1]), "r"(o[2]), "r"(o[3]), "r"(o[4]), "r"(o[5]), "r"(o[6]), "r"(o[7]), "r"(o[8]),
+          "r"(o[9]), "r"(o[10]), "r"(o[11]), "r"(o[12]));
+}
+
+GB_D void fold8(uint32_t *e, const uint32_t *o)
+{
+    asm("add.cc.u32 %0, %1, %9;\n\t"
+        "addc.cc.u32 %1, %2, %10;\n\t"
+        "addc.cc.u32 %2, %3, %11;\n\t"
+        "addc.cc.u32 %3, %4, %12;\n\t"
+        "addc.cc.u32 %4, %5, %13;\n\t"
+        "addc.cc.u32 %5, %6, %14;\n\t"
+        "addc.cc.u32 %6, %7, %15;\n\t"
+        "addc.cc.u32 %7, %8, %16;\n\t"
+        "addc.u32 %8, %17, 0;"
+        : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]),
+          "+r"(e[8])
+        : "r"(o[0]), "r"(o[1]), "r"(o[2]), "r"(o[3]), "r"(o[4]), "r"(o[5]), "r"(o[6]), "r"(o[7]), "r"(o[8]));
+}
+
+template <int N>
+GB_D void fold(uint32_t *e, const uint32_t *o);
+template <>
+GB_D void fold<12>(uint32_t *e, const uint32_t *o) { fold12(e, o); }
+template <>
+GB_D void fold<8>(uint32_t *e, const uint32_t *o) { fold8(e, o); }
 
 // acc += x * y where x is given by its even (parity 0) or odd (parity 1)
 // limbs: x[parity + 2k] for k < N/2
@@ -327,36 +433,46 @@ struct mont_t {
 // single uninterrupted carry chain; the rows are folded once per iteration
 // while dividing by 2^32.
 template <class Cfg>
+GB_D void mont_step(uint32_t *even, uint32_t *odd, const uint32_t *a, uint32_t bi)
+{
+    constexpr int N = Cfg::N;
+#pragma unroll
+    for (int j = 0; j < N + 1; j++) odd[j] = 0;
+    row_mac<N>(even, a, 0, bi);
+    row_mac<N>(odd, a, 1, bi);
+    // value = even + odd * 2^32; the Montgomery step makes even[0] zero
+    const uint32_t m = even[0] * Cfg::INV;
+    row_mac_mod<Cfg>(even, 0, m);
+    row_mac_mod<Cfg>(odd, 1, m);
+    // value / 2^32 = even[1..N] + odd[0..N]
+    fold<N>(even, odd);
+}
+
+template <class Cfg>
 GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
     constexpr int N = Cfg::N;
-    uint32_t even[N + 1], odd[N + 1], mod[N];
+    uint32_t even[N + 1], odd[N + 1];
 #pragma unroll
-    for (int i = 0; i < N; i++) mod[i] = Cfg::mod(i);
+    for (int i = 0; i < N + 1; i++) even[i] = 0;
+#if defined(GB_MUL_ROLLED)
+    // rolled outer loop: b's limbs are shifted down each step, so the code
+    // of one product stays a few hundred instructions (instruction-cache
+    // friendly when many products are inlined into one kernel)
+    uint32_t bb[N];
 #pragma unroll
-    for (int i = 0; i < N + 1; i++) { even[i] = 0; odd[i] = 0; }
-
-#pragma unroll
+    for (int i = 0; i < N; i++) bb[i] = b[i];
+#pragma unroll 1
     for (int i = 0; i < N; i++) {
-        const uint32_t bi = b[i];
-        row_mac<N>(even, a, 0, bi);
-        row_mac<N>(odd, a, 1, bi);
-        // value = even + odd * 2^32; Montgomery step makes even[0] zero
-        const uint32_t m = even[0] * Cfg::INV;
-        row_mac<N>(even, mod, 0, m);
-        row_mac<N>(odd, mod, 1, m);
-        // value / 2^32 = even[1..N] + odd[0..N]
-        uint64_t c = 0;
+        const uint32_t bi = bb[0];
 #pragma unroll
-        for (int j = 0; j < N; j++) {
-            uint64_t v = (uint64_t)even[j + 1] + odd[j] + c;
-            even[j] = (uint32_t)v;
-            c = v >> 32;
-        }
-        even[N] = odd[N] + (uint32_t)c;
-#pragma unroll
-        for (int j = 0; j < N + 1; j++) odd[j] = 0;
+        for (int j = 0; j + 1 < N; j++) bb[j] = bb[j + 1];
+        mont_step<Cfg>(even, odd, a, bi);
     }
+#else
+#pragma unroll
+    for (int i = 0; i < N; i++) mont_step<Cfg>(even, odd, a, b[i]);
+#endif
     // even[0..N] < 2m; final conditional subtraction
     mont_t<Cfg>::reduce_once(even, even[N]);
 #pragma unroll
@@ -367,13 +483,16 @@ GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 template <class Cfg>
 GB_HD void mont_t<Cfg>::mont_mul(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
-#if defined(__CUDA_ARCH__)
+#if defined(__CUDA_ARCH__) && !defined(GB_PORTABLE_MUL)
     mont_mul_device<Cfg>(out, a, b);
 #else
     uint32_t t[N + 2];
+#pragma unroll
     for (int i = 0; i < N + 2; i++) t[i] = 0;
+#pragma unroll
     for (int i = 0; i < N; i++) {
         uint64_t c = 0;
+#pragma unroll
         for (int j = 0; j < N; j++) {
             uint64_t v = (uint64_t)a[j] * b[i] + t[j] + c;
             t[j] = (uint32_t)v;
@@ -385,6 +504,7 @@ GB_HD void mont_t<Cfg>::mont_mul(uint32_t *out, const uint32_t *a, const uint32_
         uint32_t m = t[0] * Cfg::INV;
         v = (uint64_t)m * Cfg::mod(0) + t[0];
         c = v >> 32;
+#pragma unroll
         for (int j = 1; j < N; j++) {
             v = (uint64_t)m * Cfg::mod(j) + t[j] + c;
             t[j - 1] = (uint32_t)v;
@@ -395,6 +515,7 @@ GB_HD void mont_t<Cfg>::mont_mul(uint32_t *out, const uint32_t *a, const uint32_
         t[N] = t[N + 1] + (uint32_t)(v >> 32);
     }
     reduce_once(t, t[N]);
+#pragma unroll
     for (int i = 0; i < N; i++) out[i] = t[i];
 #endif
 }

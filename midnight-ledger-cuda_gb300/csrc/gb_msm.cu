@@ -45,7 +45,16 @@ struct msm_plan {
     size_t per_block;  // digits per sort block
     uint32_t L;        // sorted entries per accumulate thread
     uint32_t S;        // reduction sub-segments per segment
+    int acc_variant;   // accumulate kernel instantiation (0: 256x1, 1: 256x2, 2: 128x3);
+                       // GB_MSM_ACC_VARIANT overrides the default for tuning runs
 };
+
+static int default_acc_variant()
+{
+    const char *e = getenv("GB_MSM_ACC_VARIANT");
+    if (e && e[0] >= '0' && e[0] <= '2') return e[0] - '0';
+    return 1;  // 256 threads, 2 blocks per SM: the fastest on GB300 at n = 2^20
+}
 
 static int windows_for(int c) { return 255 / c + 1; }
 
@@ -72,8 +81,9 @@ static msm_plan make_plan(size_t n, int c, bool precomputed)
     double avg = (double)total / (double)p.G;
     uint32_t L = (uint32_t)std::max(8.0, std::min(64.0, avg * 0.5));
     p.L = L;
-    uint32_t S = std::min<uint32_t>(p.K, precomputed ? 4096u : 256u);
+    uint32_t S = std::min<uint32_t>(p.K, precomputed ? 8192u : 256u);
     p.S = S;
+    p.acc_variant = default_acc_variant();
     return p;
 }
 
@@ -174,10 +184,22 @@ __global__ void msm_colscan_kernel(uint32_t *__restrict__ hist, uint32_t bps, ui
     if (g >= G) return;
     uint32_t seg = g / K, k = g % K;
     uint32_t run = 0;
-    for (uint32_t w = 0; w < bps; w++) {
-        size_t idx = ((size_t)(seg * bps + w)) * K + k;
-        uint32_t v = hist[idx];
-        hist[idx] = run;
+    uint32_t *col = hist + (size_t)seg * bps * K + k;
+    uint32_t w = 0;
+    // batches of 16 independent loads keep the column walk off the latency path
+    for (; w + 16 <= bps; w += 16) {
+        uint32_t v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) v[u] = col[(size_t)(w + u) * K];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            col[(size_t)(w + u) * K] = run;
+            run += v[u];
+        }
+    }
+    for (; w < bps; w++) {
+        uint32_t v = col[(size_t)w * K];
+        col[(size_t)w * K] = run;
         run += v;
     }
     counts[g] = run;
@@ -241,8 +263,11 @@ __global__ void msm_scatter_kernel(const uint32_t *__restrict__ digits, size_t n
     }
 }
 
-// 6. accumulate L sorted entries per thread
-__global__ void __launch_bounds__(256) msm_accumulate_kernel(
+// 6. accumulate L sorted entries per thread.  Instantiated for several
+//    (block size, min blocks per SM) pairs: the register cap trades
+//    occupancy against spills, and the plan picks one.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) msm_accumulate_kernel(
     const uint32_t *__restrict__ sorted, const uint32_t *__restrict__ starts, uint32_t G, uint32_t L,
     size_t nchunks, const affine_t *__restrict__ points, xyzz_t *__restrict__ buckets,
     xyzz_t *__restrict__ head, xyzz_t *__restrict__ tail)
@@ -323,17 +348,20 @@ __global__ void msm_reduce_partial_kernel(const xyzz_t *__restrict__ buckets, ui
     partial[t] = sum;
 }
 
-// 8b. per segment: tree-sum the S partials (one block of 256 threads)
-__global__ void msm_reduce_segment_kernel(const xyzz_t *__restrict__ partial, uint32_t S,
-                                          xyzz_t *__restrict__ seg_sum)
+// 8b. tree sum: out[seg * gridDim.x + b] = sum of the 512-element slice b of
+//     in[seg * n .. seg * n + n), one block of 256 threads per slice
+__global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__restrict__ in, uint32_t n,
+                                                            xyzz_t *__restrict__ out)
 {
     __shared__ xyzz_t sh[256];
-    const uint32_t seg = blockIdx.x;
-    xyzz_t acc = xyzz_t::inf();
-    for (uint32_t s = threadIdx.x; s < S; s += blockDim.x) acc.add(partial[(size_t)seg * S + s]);
+    const uint32_t seg = blockIdx.y;
+    const xyzz_t *src = in + (size_t)seg * n;
+    uint32_t i0 = blockIdx.x * 512 + threadIdx.x, i1 = i0 + 256;
+    xyzz_t acc = i0 < n ? src[i0] : xyzz_t::inf();
+    if (i1 < n) acc.add(src[i1]);
     sh[threadIdx.x] = acc;
     __syncthreads();
-    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+    for (uint32_t off = 128; off > 0; off >>= 1) {
         if (threadIdx.x < off) {
             xyzz_t v = sh[threadIdx.x];
             v.add(sh[threadIdx.x + off]);
@@ -341,7 +369,7 @@ __global__ void msm_reduce_segment_kernel(const xyzz_t *__restrict__ partial, ui
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) seg_sum[seg] = sh[0];
+    if (threadIdx.x == 0) out[(size_t)seg * gridDim.x + blockIdx.x] = sh[0];
 }
 
 // 8c. combine windows (Horner) and emit a Jacobian point
@@ -440,8 +468,16 @@ static void msm_run(const msm_plan &p, const affine_t *d_points, const fr_t *d_s
                                                    p.precomputed ? 1 : 0, w.hist, w.starts, w.sorted);
     GB_CHECK_LAUNCH();
     int tok = timed_begin(s);
-    msm_accumulate_kernel<<<blocks_for(nchunks, 256), 256, 0, s>>>(
-        w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+    if (p.acc_variant == 1) {
+        msm_accumulate_kernel<256, 2><<<blocks_for(nchunks, 256), 256, 0, s>>>(
+            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+    } else if (p.acc_variant == 2) {
+        msm_accumulate_kernel<128, 3><<<blocks_for(nchunks, 128), 128, 0, s>>>(
+            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+    } else {
+        msm_accumulate_kernel<256, 1><<<blocks_for(nchunks, 256), 256, 0, s>>>(
+            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+    }
     GB_CHECK_LAUNCH();
     timed_end(tok, s, GB_SLOT_MSM_ACCUMULATE);
     msm_fixup_kernel<<<blocks_for(p.G, 128), 128, 0, s>>>(w.starts, p.G, p.L, w.head, w.tail, w.buckets);
@@ -449,8 +485,24 @@ static void msm_run(const msm_plan &p, const affine_t *d_points, const fr_t *d_s
     msm_reduce_partial_kernel<<<blocks_for((size_t)p.nseg * p.S, 128), 128, 0, s>>>(
         w.buckets, p.K, p.S, p.nseg, w.partial);
     GB_CHECK_LAUNCH();
-    msm_reduce_segment_kernel<<<p.nseg, 256, 0, s>>>(w.partial, p.S, w.segsum);
-    GB_CHECK_LAUNCH();
+    // tree-sum each segment's S partials down to one point
+    {
+        const xyzz_t *src = w.partial;
+        uint32_t len = p.S;
+        dev_buf<xyzz_t> tmp_a, tmp_b;
+        bool use_a = true;
+        while (len > 1) {
+            uint32_t blocks = (len + 511) / 512;
+            dev_buf<xyzz_t> &dst = use_a ? tmp_a : tmp_b;
+            dst = dev_buf<xyzz_t>((size_t)p.nseg * blocks, s);
+            xyzz_tree_sum_kernel<<<dim3(blocks, p.nseg), 256, 0, s>>>(src, len, dst);
+            GB_CHECK_LAUNCH();
+            src = dst;
+            len = blocks;
+            use_a = !use_a;
+        }
+        GB_CUDA_OK(cudaMemcpyAsync(w.segsum, src, (size_t)p.nseg * sizeof(xyzz_t), cudaMemcpyDeviceToDevice, s));
+    }
     msm_combine_kernel<<<1, 32, 0, s>>>(w.segsum, p.nseg, p.c, d_out);
     GB_CHECK_LAUNCH();
     timed_end(tok_all, s, GB_SLOT_MSM_TOTAL);
