@@ -73,6 +73,38 @@ typedef struct {
     size_t nonzero_len;
 } RawMsmSlice;
 
+/* Compiled gate graph (lib.rs:38-79; bls12_381_g1_msm.cu:351-381), the
+ * flattened form of midnight-proofs' GraphEvaluator (evaluation.rs:47-241).
+ * ValueSource kinds: 0 constant[a], 1 intermediate[a], 2 fixed[a] at
+ * rotation rotations[b], 3 advice[a]@b, 4 instance[a]@b, 5 challenge[a],
+ * 6 beta, 7 gamma, 8 theta, 9 trash challenge, 10 y, 11 previous value.
+ * Calculation ops: 0 add, 1 sub, 2 mul, 3 square, 4 double, 5 negate,
+ * 6 Horner (v = lhs; v = v * rhs + part for each of the parts_len parts
+ * starting at horner_parts[parts_offset]), 7 store.  Each result goes to
+ * intermediates[target]; the graph's value is the last calculation's. */
+typedef struct { uint32_t kind; uint32_t a; uint32_t b; } RawValueSource;
+typedef struct {
+    uint32_t op;
+    uint32_t target;
+    uint32_t parts_offset;
+    uint32_t parts_len;
+    RawValueSource lhs;
+    RawValueSource rhs;
+} RawCalculation;
+typedef struct {
+    const RawFr *constants;
+    size_t constants_len;
+    const int32_t *rotations;
+    size_t rotations_len;
+    const RawCalculation *calculations;
+    size_t calculations_len;
+    const RawValueSource *horner_parts;
+    size_t horner_parts_len;
+    uint32_t num_intermediates;
+} RawGraph;
+/* permutation column: kind 0 fixed, 1 advice, 2 instance (lib.rs:81-86) */
+typedef struct { uint32_t kind; uint32_t index; } RawColumnRef;
+
 /* ---- lanes ---------------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:134-146: 0 = shared lane, 1..8 private lanes */
 GB_API RustError midnight_sppark_execution_lane_set(uint32_t lane);
@@ -188,6 +220,33 @@ GB_API RustError midnight_sppark_bls12_381_fr_device_quotient_pieces(void **out,
 GB_API RustError midnight_sppark_bls12_381_fr_device_poly_lincomb(void **out, const void *polys_vec,
                                                                   size_t poly_len, size_t poly_count,
                                                                   const RawFr *scalars, size_t scalar_count);
+
+/* bls12_381_g1_msm.cu:5196-5432 (evaluation.rs:3114-3528): the quotient
+ * numerator nu on the extended coset, len rows.  If run_custom, out starts
+ * from the custom-gate graph, else from initial_out; then, folded with
+ * v = v*y + term: the permutation terms (permutation_sets products of len
+ * values, columns chunked by chunk_len, cosets of the sigma polynomials),
+ * lookup_count lookups (product / permuted input / permuted table cosets and
+ * each lookup's table graph) and trash_count trash arguments.  Columns are
+ * laid out [column][len]. */
+GB_API RustError midnight_sppark_bls12_381_eval_numerator(
+    RawFr *out, size_t len, const RawFr *initial_out, uint32_t run_custom, const RawFr *fixed, size_t fixed_cols,
+    const RawFr *advice, size_t advice_cols, const RawFr *instance, size_t instance_cols, const RawFr *challenges,
+    size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, RawFr omega,
+    RawFr delta_start, RawFr delta_const, int32_t rot_scale, int32_t last_rotation, uint32_t chunk_len,
+    const RawFr *l0, const RawFr *l_last, const RawFr *l_active, const RawFr *permutation_products,
+    size_t permutation_sets, const RawColumnRef *permutation_columns, size_t permutation_columns_len,
+    const RawFr *permutation_pk_cosets, size_t permutation_pk_cosets_len, const RawFr *lookup_product_cosets,
+    const RawFr *lookup_input_cosets, const RawFr *lookup_table_cosets, size_t lookup_count,
+    const RawFr *trash_cosets, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs);
+/* bls12_381_g1_msm.cu:5434-5515: graph_count graphs evaluated over len rows,
+ * out laid out [graph][len] */
+GB_API RustError midnight_sppark_bls12_381_eval_graph_batch(
+    RawFr *out, size_t len, const RawFr *fixed, size_t fixed_cols, const RawFr *advice, size_t advice_cols,
+    const RawFr *instance, size_t instance_cols, const RawFr *challenges, size_t challenge_len, RawFr beta,
+    RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, int32_t rot_scale, const RawGraph *graphs,
+    size_t graph_count);
 
 /* ---- device vectors --------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:2741-3442 */

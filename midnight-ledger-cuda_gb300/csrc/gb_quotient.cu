@@ -1,0 +1,489 @@
+// Quotient numerator on the extended coset for sm_103a, and its C ABI
+// (midnight-sppark-msm/src/bls12_381_g1_msm.cu:5196-5515, semantics of
+// vendor/midnight-proofs-0.8.1/src/plonk/evaluation.rs:3114-3528).
+//
+// One fused kernel per call: each thread owns one extended-domain row and
+// evaluates the custom-gate graph, then folds in the permutation, lookup and
+// trash constraints (v = v*y + term), writing the row once.  The compiled
+// graph is interpreted: every thread of a warp walks the same calculation
+// list (uniform control flow, broadcast loads), with its intermediates in a
+// per-thread local array sized to the graph.
+#include <algorithm>
+#include <vector>
+
+#include "gb_vec.cuh"
+
+namespace gb {
+
+struct dgraph {
+    const fr_t *constants;
+    uint32_t nconst;
+    const int32_t *rotations;
+    uint32_t nrot;
+    const RawCalculation *calcs;
+    uint32_t ncalc;
+    const RawValueSource *parts;
+    uint32_t nparts;
+    uint32_t ninter;
+};
+
+struct num_params {
+    fr_t *out;
+    size_t len;
+    int32_t rot_scale;
+    const fr_t *fixed;
+    size_t fixed_cols;
+    const fr_t *advice;
+    size_t advice_cols;
+    const fr_t *instance;
+    size_t instance_cols;
+    const fr_t *challenges;
+    size_t challenge_len;
+    fr_t beta, gamma, theta, trash, y;
+    int run_custom;
+    const fr_t *initial;
+    dgraph custom;
+    size_t perm_sets;
+    const fr_t *perm_products;
+    const RawColumnRef *perm_columns;
+    size_t perm_columns_len;
+    const fr_t *perm_pk_cosets;
+    const fr_t *omega_powers;
+    fr_t delta_start, delta_const;
+    int32_t last_rotation;
+    uint32_t chunk_len;
+    const fr_t *l0, *l_last, *l_active;
+    size_t lookup_count;
+    const fr_t *lk_product, *lk_input, *lk_table;
+    const dgraph *lookup_graphs;
+    size_t trash_count;
+    const fr_t *trash_cosets;
+    const uint32_t *trash_sel;
+    const dgraph *trash_graphs;
+};
+
+// (idx + rot * rot_scale) mod len, Euclidean (evaluation.rs:40-45)
+__device__ __forceinline__ size_t rot_index(size_t idx, int32_t rot, int32_t rot_scale, size_t len)
+{
+    int64_t v = (int64_t)idx + (int64_t)rot * rot_scale;
+    int64_t m = (int64_t)len;
+    v %= m;
+    if (v < 0) v += m;
+    return (size_t)v;
+}
+
+__device__ __forceinline__ const fr_t *column_base(const num_params &p, uint32_t kind, uint32_t index)
+{
+    if (kind == 0 && index < p.fixed_cols) return p.fixed + (size_t)index * p.len;
+    if (kind == 1 && index < p.advice_cols) return p.advice + (size_t)index * p.len;
+    if (kind == 2 && index < p.instance_cols) return p.instance + (size_t)index * p.len;
+    return nullptr;
+}
+
+// ValueSource::get (evaluation.rs:83-129); out-of-range references read zero
+template <int MAX>
+__device__ fr_t source_value(const RawValueSource &src, const dgraph &g, const num_params &p, size_t idx,
+                             const fr_t *inter, const fr_t &prev)
+{
+    switch (src.kind) {
+    case 0:
+        return src.a < g.nconst ? g.constants[src.a] : fr_t::zero();
+    case 1:
+        return src.a < MAX ? inter[src.a] : fr_t::zero();
+    case 2:
+    case 3:
+    case 4: {
+        const fr_t *base = column_base(p, src.kind - 2, src.a);
+        if (!base || src.b >= g.nrot) return fr_t::zero();
+        return base[rot_index(idx, g.rotations[src.b], p.rot_scale, p.len)];
+    }
+    case 5:
+        return src.a < p.challenge_len ? p.challenges[src.a] : fr_t::zero();
+    case 6:
+        return p.beta;
+    case 7:
+        return p.gamma;
+    case 8:
+        return p.theta;
+    case 9:
+        return p.trash;
+    case 10:
+        return p.y;
+    case 11:
+        return prev;
+    default:
+        return fr_t::zero();
+    }
+}
+
+// GraphEvaluator::evaluate (evaluation.rs:3797-3846): every calculation in
+// order, results cached as intermediates; the value of the last one
+template <int MAX>
+__device__ fr_t evaluate_graph(const dgraph &g, const num_params &p, size_t idx, const fr_t &prev)
+{
+    fr_t inter[MAX];
+    const uint32_t nint = g.ninter < MAX ? g.ninter : MAX;
+    for (uint32_t i = 0; i < nint; i++) inter[i] = fr_t::zero();
+    fr_t last = fr_t::zero();
+    for (uint32_t c = 0; c < g.ncalc; c++) {
+        const RawCalculation calc = g.calcs[c];
+        fr_t v;
+        switch (calc.op) {
+        case 0:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev) + source_value<MAX>(calc.rhs, g, p, idx, inter, prev);
+            break;
+        case 1:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev) - source_value<MAX>(calc.rhs, g, p, idx, inter, prev);
+            break;
+        case 2:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev) * source_value<MAX>(calc.rhs, g, p, idx, inter, prev);
+            break;
+        case 3:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev).sqr();
+            break;
+        case 4:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev).dbl();
+            break;
+        case 5:
+            v = -source_value<MAX>(calc.lhs, g, p, idx, inter, prev);
+            break;
+        case 6: {
+            fr_t factor = source_value<MAX>(calc.rhs, g, p, idx, inter, prev);
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev);
+            for (uint32_t k = 0; k < calc.parts_len; k++) {
+                uint32_t pi = calc.parts_offset + k;
+                fr_t part = pi < g.nparts ? source_value<MAX>(g.parts[pi], g, p, idx, inter, prev) : fr_t::zero();
+                v = v * factor + part;
+            }
+            break;
+        }
+        case 7:
+            v = source_value<MAX>(calc.lhs, g, p, idx, inter, prev);
+            break;
+        default:
+            v = fr_t::zero();
+            break;
+        }
+        if (calc.target < MAX) inter[calc.target] = v;
+        last = v;
+    }
+    return last;
+}
+
+template <int MAX>
+__global__ void numerator_kernel(num_params p)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= p.len) return;
+    const fr_t one = fr_t::one();
+    const fr_t zero = fr_t::zero();
+    fr_t value = p.run_custom ? evaluate_graph<MAX>(p.custom, p, idx, zero) : p.initial[idx];
+
+    if (p.perm_sets && p.chunk_len) {
+        // permutation argument (evaluation.rs:3282-3352)
+        const size_t len = p.len;
+        const size_t r_next = rot_index(idx, 1, p.rot_scale, len);
+        const size_t r_last = rot_index(idx, p.last_rotation, p.rot_scale, len);
+        const fr_t *first = p.perm_products;
+        const fr_t *lastp = p.perm_products + (p.perm_sets - 1) * len;
+        const fr_t l0 = p.l0[idx];
+        value = value * p.y + (one - first[idx]) * l0;
+        value = value * p.y + (lastp[idx].sqr() - lastp[idx]) * p.l_last[idx];
+        for (size_t s = 1; s < p.perm_sets; s++)
+            value = value * p.y + (p.perm_products[s * len + idx] - p.perm_products[(s - 1) * len + r_last]) * l0;
+        fr_t delta = p.delta_start * p.omega_powers[idx];
+        const fr_t l_active = p.l_active[idx];
+        for (size_t s = 0; s < p.perm_sets; s++) {
+            const fr_t *prod = p.perm_products + s * len;
+            fr_t left = prod[r_next];
+            fr_t right = prod[idx];
+            const size_t base = s * p.chunk_len;
+            for (uint32_t j = 0; j < p.chunk_len && base + j < p.perm_columns_len; j++) {
+                const RawColumnRef ref = p.perm_columns[base + j];
+                const fr_t *col = column_base(p, ref.kind, ref.index);
+                if (!col) continue;
+                const fr_t v = col[idx];
+                left = left * (v + p.beta * p.perm_pk_cosets[(base + j) * len + idx] + p.gamma);
+                right = right * (v + delta + p.gamma);
+                delta = delta * p.delta_const;
+            }
+            value = value * p.y + (left - right) * l_active;
+        }
+    }
+
+    for (size_t n = 0; n < p.lookup_count; n++) {
+        // lookup argument (evaluation.rs:3408-3472)
+        const size_t len = p.len;
+        const size_t r_next = rot_index(idx, 1, p.rot_scale, len);
+        const size_t r_prev = rot_index(idx, -1, p.rot_scale, len);
+        const fr_t *prod = p.lk_product + n * len;
+        const fr_t *pin = p.lk_input + n * len;
+        const fr_t *ptab = p.lk_table + n * len;
+        const fr_t table_value = evaluate_graph<MAX>(p.lookup_graphs[n], p, idx, zero);
+        const fr_t a_minus_s = pin[idx] - ptab[idx];
+        const fr_t l0 = p.l0[idx], l_active = p.l_active[idx];
+        value = value * p.y + (one - prod[idx]) * l0;
+        value = value * p.y + (prod[idx].sqr() - prod[idx]) * p.l_last[idx];
+        value = value * p.y +
+                (prod[r_next] * (pin[idx] + p.beta) * (ptab[idx] + p.gamma) - prod[idx] * table_value) * l_active;
+        value = value * p.y + a_minus_s * l0;
+        value = value * p.y + a_minus_s * (pin[idx] - pin[r_prev]) * l_active;
+    }
+
+    for (size_t n = 0; n < p.trash_count; n++) {
+        // trash argument (evaluation.rs:3489-3521)
+        const uint32_t sel = p.trash_sel[n];
+        if (sel >= p.fixed_cols) continue;
+        const fr_t compressed = evaluate_graph<MAX>(p.trash_graphs[n], p, idx, zero);
+        const fr_t q = p.fixed[(size_t)sel * p.len + idx];
+        value = value * p.y + (compressed - (one - q) * p.trash_cosets[n * p.len + idx]);
+    }
+    p.out[idx] = value;
+}
+
+template <int MAX>
+__global__ void graph_batch_kernel(num_params p, fr_t *out)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= p.len) return;
+    out[idx] = evaluate_graph<MAX>(p.custom, p, idx, fr_t::zero());
+}
+
+// ---------------------------------------------------------------- host
+
+struct graph_upload {
+    dev_buf<fr_t> constants;
+    dev_buf<int32_t> rotations;
+    dev_buf<RawCalculation> calcs;
+    dev_buf<RawValueSource> parts;
+    dgraph g{};
+};
+
+static void upload_graph(graph_upload &u, const RawGraph &raw, cudaStream_t s)
+{
+    if ((raw.constants_len && !raw.constants) || (raw.rotations_len && !raw.rotations) ||
+        (raw.calculations_len && !raw.calculations) || (raw.horner_parts_len && !raw.horner_parts))
+        throw cuda_error((int)cudaErrorInvalidValue, "graph arrays missing");
+    u.constants = dev_buf<fr_t>(raw.constants_len, s);
+    u.rotations = dev_buf<int32_t>(raw.rotations_len, s);
+    u.calcs = dev_buf<RawCalculation>(raw.calculations_len, s);
+    u.parts = dev_buf<RawValueSource>(raw.horner_parts_len, s);
+    h2d(u.constants, raw.constants, raw.constants_len * sizeof(fr_t), s);
+    h2d(u.rotations, raw.rotations, raw.rotations_len * sizeof(int32_t), s);
+    h2d(u.calcs, raw.calculations, raw.calculations_len * sizeof(RawCalculation), s);
+    h2d(u.parts, raw.horner_parts, raw.horner_parts_len * sizeof(RawValueSource), s);
+    u.g.constants = u.constants;
+    u.g.nconst = (uint32_t)raw.constants_len;
+    u.g.rotations = u.rotations;
+    u.g.nrot = (uint32_t)raw.rotations_len;
+    u.g.calcs = u.calcs;
+    u.g.ncalc = (uint32_t)raw.calculations_len;
+    u.g.parts = u.parts;
+    u.g.nparts = (uint32_t)raw.horner_parts_len;
+    u.g.ninter = raw.num_intermediates;
+}
+
+static int capacity_for(uint32_t n)
+{
+    if (n <= 16) return 16;
+    if (n <= 64) return 64;
+    if (n <= 256) return 256;
+    return 0;
+}
+
+template <class F16, class F64, class F256>
+static void launch_by_capacity(int cap, F16 f16, F64 f64, F256 f256)
+{
+    if (cap == 16) f16();
+    else if (cap == 64) f64();
+    else if (cap == 256) f256();
+    else throw cuda_error((int)cudaErrorInvalidValue, "graph needs more than 256 intermediates");
+}
+
+static dev_buf<fr_t> upload_fr(const RawFr *h, size_t n, cudaStream_t s)
+{
+    dev_buf<fr_t> d(n, s);
+    h2d(d, h, n * sizeof(fr_t), s);
+    return d;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+RustError midnight_sppark_bls12_381_eval_numerator(
+    RawFr *out_raw, size_t len, const RawFr *initial_out, uint32_t run_custom, const RawFr *fixed, size_t fixed_cols,
+    const RawFr *advice, size_t advice_cols, const RawFr *instance, size_t instance_cols, const RawFr *challenges,
+    size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, RawFr omega,
+    RawFr delta_start, RawFr delta_const, int32_t rot_scale, int32_t last_rotation, uint32_t chunk_len,
+    const RawFr *l0, const RawFr *l_last, const RawFr *l_active, const RawFr *permutation_products,
+    size_t permutation_sets, const RawColumnRef *permutation_columns, size_t permutation_columns_len,
+    const RawFr *permutation_pk_cosets, size_t permutation_pk_cosets_len, const RawFr *lookup_product_cosets,
+    const RawFr *lookup_input_cosets, const RawFr *lookup_table_cosets, size_t lookup_count,
+    const RawFr *trash_cosets, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs)
+{
+    if (len == 0) return ok();
+    if (!out_raw) return make_error((int)cudaErrorInvalidValue, "null numerator output");
+    if (!run_custom && !initial_out)
+        return make_error((int)cudaErrorInvalidValue, "initial_out is required when custom evaluation is skipped");
+    if ((lookup_count && (!lookup_graphs || !lookup_product_cosets || !lookup_input_cosets || !lookup_table_cosets)) ||
+        (trash_count && (!trash_graphs || !trash_cosets || !trash_selector_fixed_indices)) ||
+        (permutation_sets && (!permutation_products || !l0 || !l_last || !l_active)) ||
+        (lookup_count && (!l0 || !l_last || !l_active)))
+        return make_error((int)cudaErrorInvalidValue, "invalid numerator arguments");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    num_params p{};
+    p.len = len;
+    p.rot_scale = rot_scale;
+    dev_buf<fr_t> d_out(len, s);
+    p.out = d_out;
+    auto d_fixed = upload_fr(fixed, fixed_cols * len, s);
+    auto d_advice = upload_fr(advice, advice_cols * len, s);
+    auto d_instance = upload_fr(instance, instance_cols * len, s);
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    p.fixed = d_fixed;
+    p.fixed_cols = fixed_cols;
+    p.advice = d_advice;
+    p.advice_cols = advice_cols;
+    p.instance = d_instance;
+    p.instance_cols = instance_cols;
+    p.challenges = d_chal;
+    p.challenge_len = challenge_len;
+    p.beta = from_raw(beta);
+    p.gamma = from_raw(gamma);
+    p.theta = from_raw(theta);
+    p.trash = from_raw(trash_challenge);
+    p.y = from_raw(y);
+    p.run_custom = run_custom ? 1 : 0;
+    dev_buf<fr_t> d_init;
+    if (!run_custom) {
+        d_init = upload_fr(initial_out, len, s);
+        p.initial = d_init;
+    }
+    uint32_t max_inter = run_custom ? custom_graph.num_intermediates : 0;
+    graph_upload custom;
+    if (run_custom) upload_graph(custom, custom_graph, s);
+    p.custom = custom.g;
+    const bool lagrange = permutation_sets || lookup_count;
+    auto d_l0 = upload_fr(l0, lagrange ? len : 0, s);
+    auto d_llast = upload_fr(l_last, lagrange ? len : 0, s);
+    auto d_lact = upload_fr(l_active, lagrange ? len : 0, s);
+    p.l0 = d_l0;
+    p.l_last = d_llast;
+    p.l_active = d_lact;
+    auto d_pprod = upload_fr(permutation_products, permutation_sets * len, s);
+    dev_buf<RawColumnRef> d_pcols(permutation_columns_len, s);
+    h2d(d_pcols, permutation_columns, permutation_columns_len * sizeof(RawColumnRef), s);
+    auto d_pk = upload_fr(permutation_pk_cosets, permutation_pk_cosets_len * len, s);
+    dev_buf<fr_t> d_omega(permutation_sets ? len : 0, s);
+    if (permutation_sets) omega_powers(d_omega, from_raw(omega), len, s);
+    p.perm_sets = permutation_sets;
+    p.perm_products = d_pprod;
+    p.perm_columns = d_pcols;
+    p.perm_columns_len = permutation_columns_len;
+    p.perm_pk_cosets = d_pk;
+    p.omega_powers = d_omega;
+    p.delta_start = from_raw(delta_start);
+    p.delta_const = from_raw(delta_const);
+    p.last_rotation = last_rotation;
+    p.chunk_len = chunk_len;
+    if (permutation_sets && permutation_pk_cosets_len < permutation_columns_len)
+        return make_error((int)cudaErrorInvalidValue, "fewer permutation cosets than permutation columns");
+    auto d_lprod = upload_fr(lookup_product_cosets, lookup_count * len, s);
+    auto d_lin = upload_fr(lookup_input_cosets, lookup_count * len, s);
+    auto d_ltab = upload_fr(lookup_table_cosets, lookup_count * len, s);
+    std::vector<graph_upload> lk(lookup_count), tr(trash_count);
+    std::vector<dgraph> lkg(lookup_count), trg(trash_count);
+    for (size_t i = 0; i < lookup_count; i++) {
+        upload_graph(lk[i], lookup_graphs[i], s);
+        lkg[i] = lk[i].g;
+        max_inter = std::max(max_inter, lookup_graphs[i].num_intermediates);
+    }
+    for (size_t i = 0; i < trash_count; i++) {
+        upload_graph(tr[i], trash_graphs[i], s);
+        trg[i] = tr[i].g;
+        max_inter = std::max(max_inter, trash_graphs[i].num_intermediates);
+    }
+    dev_buf<dgraph> d_lkg(lookup_count, s), d_trg(trash_count, s);
+    h2d(d_lkg, lkg.data(), lookup_count * sizeof(dgraph), s);
+    h2d(d_trg, trg.data(), trash_count * sizeof(dgraph), s);
+    p.lookup_count = lookup_count;
+    p.lk_product = d_lprod;
+    p.lk_input = d_lin;
+    p.lk_table = d_ltab;
+    p.lookup_graphs = d_lkg;
+    auto d_trash = upload_fr(trash_cosets, trash_count * len, s);
+    dev_buf<uint32_t> d_tsel(trash_count, s);
+    h2d(d_tsel, trash_selector_fixed_indices, trash_count * sizeof(uint32_t), s);
+    p.trash_count = trash_count;
+    p.trash_cosets = d_trash;
+    p.trash_sel = d_tsel;
+    p.trash_graphs = d_trg;
+    const unsigned grid = blocks_for(len, 128);
+    launch_by_capacity(
+        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
+        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
+    GB_CHECK_LAUNCH();
+    d2h(out_raw, d_out, len * sizeof(fr_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+RustError midnight_sppark_bls12_381_eval_graph_batch(RawFr *out_raw, size_t len, const RawFr *fixed, size_t fixed_cols,
+                                                      const RawFr *advice, size_t advice_cols, const RawFr *instance,
+                                                      size_t instance_cols, const RawFr *challenges,
+                                                      size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta,
+                                                      RawFr trash_challenge, RawFr y, int32_t rot_scale,
+                                                      const RawGraph *graphs, size_t graph_count)
+{
+    if (len == 0 || graph_count == 0) return ok();
+    if (!out_raw || !graphs || (fixed_cols && !fixed) || (advice_cols && !advice) || (instance_cols && !instance) ||
+        (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid graph batch arguments");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    num_params p{};
+    p.len = len;
+    p.rot_scale = rot_scale;
+    auto d_fixed = upload_fr(fixed, fixed_cols * len, s);
+    auto d_advice = upload_fr(advice, advice_cols * len, s);
+    auto d_instance = upload_fr(instance, instance_cols * len, s);
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    p.fixed = d_fixed;
+    p.fixed_cols = fixed_cols;
+    p.advice = d_advice;
+    p.advice_cols = advice_cols;
+    p.instance = d_instance;
+    p.instance_cols = instance_cols;
+    p.challenges = d_chal;
+    p.challenge_len = challenge_len;
+    p.beta = from_raw(beta);
+    p.gamma = from_raw(gamma);
+    p.theta = from_raw(theta);
+    p.trash = from_raw(trash_challenge);
+    p.y = from_raw(y);
+    dev_buf<fr_t> d_out(len * graph_count, s);
+    std::vector<graph_upload> up(graph_count);
+    const unsigned grid = blocks_for(len, 128);
+    for (size_t gi = 0; gi < graph_count; gi++) {
+        upload_graph(up[gi], graphs[gi], s);
+        p.custom = up[gi].g;
+        fr_t *o = d_out.get() + gi * len;
+        launch_by_capacity(
+            capacity_for(graphs[gi].num_intermediates), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
+        GB_CHECK_LAUNCH();
+    }
+    d2h(out_raw, d_out, len * graph_count * sizeof(fr_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+}  // extern "C"

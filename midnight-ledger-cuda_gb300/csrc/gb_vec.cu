@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gb_ntt.cuh"
+#include "gb_vec.cuh"
 
 namespace gb {
 
@@ -153,6 +154,20 @@ void batch_invert(fr_t *out, const fr_t *in, size_t n, const fr_t *mul, cudaStre
     size_t tiles = (n + kScanTile - 1) / kScanTile;
     batch_invert_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, mul, out);
     GB_CHECK_LAUNCH();
+}
+
+__global__ void power_factors_kernel(fr_t *d, fr_t w, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = i ? w : fr_t::one();
+}
+
+void omega_powers(fr_t *d, const fr_t &w, size_t n, cudaStream_t s)
+{
+    if (!n) return;
+    power_factors_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d, w, n);
+    GB_CHECK_LAUNCH();
+    prefix_product(d, d, n, s);
 }
 
 // ------------------------------------------------------------ products

@@ -63,7 +63,9 @@ def build(force=False, verbose=False):
 
 
 def _declare(L):
+    from .graph import RawGraph
     vp, sz, u32, b = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_bool
+    i32 = ctypes.c_int32
     fr = RawFr
     E = RustError
     sigs = {
@@ -119,6 +121,11 @@ def _declare(L):
         "gb_profile_read": (None, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
         "gb_profile_reset": (None, []),
         "gb_fr_shifted_prefix_product_noalloc": (E, [vp, fr, sz, vp]),
+        "midnight_sppark_bls12_381_eval_numerator": (E, [
+            vp, sz, vp, u32, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, fr, fr, fr, i32, i32, u32,
+            vp, vp, vp, vp, sz, vp, sz, vp, sz, vp, vp, vp, sz, vp, vp, sz, RawGraph, vp, vp]),
+        "midnight_sppark_bls12_381_eval_graph_batch": (E, [
+            vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, i32, vp, sz]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)

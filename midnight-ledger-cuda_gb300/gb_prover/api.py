@@ -21,7 +21,8 @@ __all__ = [
     "bls12_381_fr_lookup_products_device", "bls12_381_fr_device_quotient_pieces",
     "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "transfer_counters",
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
-    "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT",
+    "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
+    "bls12_381_eval_graph_batch",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -404,3 +405,71 @@ def profile_read(slot):
 
 def profile_reset():
     lib().gb_profile_reset()
+
+
+# ---------------------------------------------------------------- quotient numerator
+
+def _cols(a, length):
+    if a is None:
+        return None, 0
+    a = _fr_arr(a)
+    return a, len(a) // length if length else 0
+
+
+def bls12_381_eval_numerator(length, custom_graph, fixed=None, advice=None, instance=None, challenges=None,
+                             beta=None, gamma=None, theta=None, trash_challenge=None, y=None, omega=None,
+                             delta_start=None, delta_const=None, rot_scale=1, last_rotation=-1, chunk_len=1,
+                             l0=None, l_last=None, l_active=None, permutation_products=None, permutation_sets=0,
+                             permutation_columns=(), permutation_pk_cosets=None, lookups=(), trash=(),
+                             initial_out=None):
+    """midnight_sppark_bls12_381_eval_numerator (evaluation.rs:3114-3528).
+    lookups: list of (graph, product_coset, input_coset, table_coset);
+    trash: list of (graph, trash_coset, selector_fixed_index)."""
+    from .graph import column_refs, graph_array
+    z = np.zeros(4, dtype=np.uint64)
+    fx, nf = _cols(fixed, length)
+    ad, na = _cols(advice, length)
+    ins, ni = _cols(instance, length)
+    ch = _fr_arr(challenges) if challenges is not None else None
+    lag = [None if x is None else _fr_arr(x) for x in (l0, l_last, l_active)]
+    pp = None if permutation_products is None else _fr_arr(permutation_products)
+    pk = None if permutation_pk_cosets is None else _fr_arr(permutation_pk_cosets)
+    pcols = column_refs(list(permutation_columns))
+    lk_prod = np.concatenate([_fr_arr(l[1]) for l in lookups]) if lookups else None
+    lk_in = np.concatenate([_fr_arr(l[2]) for l in lookups]) if lookups else None
+    lk_tab = np.concatenate([_fr_arr(l[3]) for l in lookups]) if lookups else None
+    lk_g = graph_array([l[0] for l in lookups])
+    tr_c = np.concatenate([_fr_arr(t[1]) for t in trash]) if trash else None
+    tr_s = np.array([t[2] for t in trash] or [0], dtype=np.uint32)
+    tr_g = graph_array([t[0] for t in trash])
+    init = None if initial_out is None else _fr_arr(initial_out)
+    out = np.zeros((length, 4), dtype=np.uint64)
+    g = custom_graph.raw() if custom_graph is not None else graph_array([])[0]
+    f = lambda v: _fr(z if v is None else v)  # noqa: E731
+    check(lib().midnight_sppark_bls12_381_eval_numerator(
+        _ptr(out), length, _ptr(init), 1 if custom_graph is not None else 0, _ptr(fx), nf, _ptr(ad), na, _ptr(ins),
+        ni, _ptr(ch), 0 if ch is None else len(ch), f(beta), f(gamma), f(theta), f(trash_challenge), f(y), f(omega),
+        f(delta_start), f(delta_const), rot_scale, last_rotation, chunk_len, _ptr(lag[0]), _ptr(lag[1]),
+        _ptr(lag[2]), _ptr(pp), permutation_sets, ctypes.cast(pcols, ctypes.c_void_p), len(permutation_columns),
+        _ptr(pk), 0 if pk is None else len(pk) // length, _ptr(lk_prod), _ptr(lk_in), _ptr(lk_tab), len(lookups),
+        _ptr(tr_c), _ptr(tr_s), len(trash), g, ctypes.cast(lk_g, ctypes.c_void_p),
+        ctypes.cast(tr_g, ctypes.c_void_p)))
+    return out
+
+
+def bls12_381_eval_graph_batch(length, graphs, fixed=None, advice=None, instance=None, challenges=None,
+                               beta=None, gamma=None, theta=None, trash_challenge=None, y=None, rot_scale=1):
+    from .graph import graph_array
+    z = np.zeros(4, dtype=np.uint64)
+    fx, nf = _cols(fixed, length)
+    ad, na = _cols(advice, length)
+    ins, ni = _cols(instance, length)
+    ch = _fr_arr(challenges) if challenges is not None else None
+    ga = graph_array(list(graphs))
+    out = np.zeros((len(graphs), length, 4), dtype=np.uint64)
+    f = lambda v: _fr(z if v is None else v)  # noqa: E731
+    check(lib().midnight_sppark_bls12_381_eval_graph_batch(
+        _ptr(out), length, _ptr(fx), nf, _ptr(ad), na, _ptr(ins), ni, _ptr(ch), 0 if ch is None else len(ch),
+        f(beta), f(gamma), f(theta), f(trash_challenge), f(y), rot_scale, ctypes.cast(ga, ctypes.c_void_p),
+        len(graphs)))
+    return out

@@ -1234,3 +1234,302 @@ void orc_fr_sort_canonical(orc_fr *a, size_t len)
     INIT();
     qsort(a, len, sizeof(orc_fr), cmp_canon_qsort);
 }
+
+/* ======================================================================== */
+/* Quotient numerator                                                        */
+/* ======================================================================== */
+
+/* get_rotation_idx (evaluation.rs:40-45) */
+static size_t rot_idx(size_t idx, int32_t rot, int32_t scale, size_t len)
+{
+    long long v = (long long)idx + (long long)rot * (long long)scale;
+    long long m = (long long)len;
+    v %= m;
+    if (v < 0) v += m;
+    return (size_t)v;
+}
+
+typedef struct {
+    size_t len;
+    int32_t rot_scale;
+    const orc_fr *fixed, *advice, *instance, *challenges;
+    size_t fixed_cols, advice_cols, instance_cols, challenge_len;
+    const orc_fr *beta, *gamma, *theta, *trash, *y;
+} num_env;
+
+static const orc_fr *col_base(const num_env *e, uint32_t kind, uint32_t index)
+{
+    if (kind == 0 && index < e->fixed_cols) return e->fixed + (size_t)index * e->len;
+    if (kind == 1 && index < e->advice_cols) return e->advice + (size_t)index * e->len;
+    if (kind == 2 && index < e->instance_cols) return e->instance + (size_t)index * e->len;
+    return NULL;
+}
+
+/* ValueSource::get (evaluation.rs:83-129); unknown references read zero,
+ * as the reference's GPU interpreter does (.cu:447-516) */
+static void src_val(u64 *o, const orc_value_source *src, const orc_graph *g, const num_env *e, size_t idx,
+                    const u64 *inter, uint32_t ninter, const u64 *prev)
+{
+    memset(o, 0, 32);
+    switch (src->kind) {
+    case 0: if (src->a < g->constants_len) memcpy(o, g->constants[src->a].l, 32); break;
+    case 1: if (src->a < ninter) memcpy(o, inter + 4 * src->a, 32); break;
+    case 2: case 3: case 4: {
+        const orc_fr *b = col_base(e, src->kind - 2, src->a);
+        if (b && src->b < g->rotations_len) memcpy(o, b[rot_idx(idx, g->rotations[src->b], e->rot_scale, e->len)].l, 32);
+        break;
+    }
+    case 5: if (src->a < e->challenge_len) memcpy(o, e->challenges[src->a].l, 32); break;
+    case 6: memcpy(o, e->beta->l, 32); break;
+    case 7: memcpy(o, e->gamma->l, 32); break;
+    case 8: memcpy(o, e->theta->l, 32); break;
+    case 9: memcpy(o, e->trash->l, 32); break;
+    case 10: memcpy(o, e->y->l, 32); break;
+    case 11: memcpy(o, prev, 32); break;
+    default: break;
+    }
+}
+
+/* GraphEvaluator::evaluate (evaluation.rs:3797-3846) */
+static void eval_graph(u64 *out, const orc_graph *g, const num_env *e, size_t idx, const u64 *prev, u64 *inter)
+{
+    uint32_t ni = g->num_intermediates;
+    memset(inter, 0, 32 * (size_t)ni);
+    u64 last[4] = {0, 0, 0, 0};
+    for (size_t c = 0; c < g->calculations_len; c++) {
+        const orc_calculation *cl = &g->calculations[c];
+        u64 a[4], b[4], v[4] = {0, 0, 0, 0};
+        switch (cl->op) {
+        case 0: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); src_val(b, &cl->rhs, g, e, idx, inter, ni, prev); f_add(v, a, b, &FR); break;
+        case 1: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); src_val(b, &cl->rhs, g, e, idx, inter, ni, prev); f_sub(v, a, b, &FR); break;
+        case 2: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); src_val(b, &cl->rhs, g, e, idx, inter, ni, prev); f_mul(v, a, b, &FR); break;
+        case 3: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); f_mul(v, a, a, &FR); break;
+        case 4: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); f_add(v, a, a, &FR); break;
+        case 5: src_val(a, &cl->lhs, g, e, idx, inter, ni, prev); f_neg(v, a, &FR); break;
+        case 6: {
+            u64 factor[4];
+            src_val(factor, &cl->rhs, g, e, idx, inter, ni, prev);
+            src_val(v, &cl->lhs, g, e, idx, inter, ni, prev);
+            for (uint32_t k = 0; k < cl->parts_len; k++) {
+                u64 part[4] = {0, 0, 0, 0};
+                size_t pi = (size_t)cl->parts_offset + k;
+                if (pi < g->horner_parts_len) src_val(part, &g->horner_parts[pi], g, e, idx, inter, ni, prev);
+                f_mul(v, v, factor, &FR);
+                f_add(v, v, part, &FR);
+            }
+            break;
+        }
+        case 7: src_val(v, &cl->lhs, g, e, idx, inter, ni, prev); break;
+        default: break;
+        }
+        if (cl->target < ni) memcpy(inter + 4 * cl->target, v, 32);
+        memcpy(last, v, 32);
+    }
+    memcpy(out, last, 32);
+}
+
+typedef struct {
+    orc_fr *out;
+    const orc_fr *initial;
+    uint32_t run_custom;
+    num_env env;
+    const orc_fr *omega, *delta_start, *delta_const;
+    int32_t last_rotation;
+    uint32_t chunk_len;
+    const orc_fr *l0, *l_last, *l_active, *perm_products;
+    size_t perm_sets;
+    const orc_column_ref *perm_columns;
+    size_t perm_columns_len;
+    const orc_fr *perm_pk;
+    const orc_fr *lk_product, *lk_input, *lk_table;
+    size_t lookup_count;
+    const orc_fr *trash_cosets;
+    const uint32_t *trash_sel;
+    size_t trash_count;
+    const orc_graph *custom, *lookup_graphs, *trash_graphs;
+    uint32_t max_inter;
+} num_ctx;
+
+static void num_range(void *vctx, size_t b, size_t e_)
+{
+    num_ctx *c = (num_ctx *)vctx;
+    const num_env *e = &c->env;
+    const size_t len = e->len;
+    u64 *inter = (u64 *)calloc((size_t)(c->max_inter ? c->max_inter : 1) * 4, sizeof(u64));
+    const u64 *one = FR.one;
+    u64 zero[4] = {0, 0, 0, 0};
+    for (size_t idx = b; idx < e_; idx++) {
+        u64 value[4], t[4], t2[4];
+        if (c->run_custom) eval_graph(value, c->custom, e, idx, zero, inter);
+        else memcpy(value, c->initial[idx].l, 32);
+        if (c->perm_sets && c->chunk_len) {
+            /* evaluation.rs:3282-3352 */
+            size_t r_next = rot_idx(idx, 1, e->rot_scale, len);
+            size_t r_last = rot_idx(idx, c->last_rotation, e->rot_scale, len);
+            const orc_fr *first = c->perm_products, *last = c->perm_products + (c->perm_sets - 1) * len;
+            f_mul(value, value, e->y->l, &FR);
+            f_sub(t, one, first[idx].l, &FR);
+            f_mul(t, t, c->l0[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_mul(t, last[idx].l, last[idx].l, &FR);
+            f_sub(t, t, last[idx].l, &FR);
+            f_mul(t, t, c->l_last[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            for (size_t s = 1; s < c->perm_sets; s++) {
+                f_mul(value, value, e->y->l, &FR);
+                f_sub(t, c->perm_products[s * len + idx].l, c->perm_products[(s - 1) * len + r_last].l, &FR);
+                f_mul(t, t, c->l0[idx].l, &FR);
+                f_add(value, value, t, &FR);
+            }
+            u64 delta[4], wi[4];
+            u64 ie[1] = {idx};
+            f_pow(wi, c->omega->l, ie, 1, &FR);
+            f_mul(delta, c->delta_start->l, wi, &FR);
+            for (size_t s = 0; s < c->perm_sets; s++) {
+                const orc_fr *prod = c->perm_products + s * len;
+                u64 left[4], right[4];
+                memcpy(left, prod[r_next].l, 32);
+                memcpy(right, prod[idx].l, 32);
+                size_t base = s * c->chunk_len;
+                for (uint32_t j = 0; j < c->chunk_len && base + j < c->perm_columns_len; j++) {
+                    const orc_fr *col = col_base(e, c->perm_columns[base + j].kind, c->perm_columns[base + j].index);
+                    if (!col) continue;
+                    f_mul(t, e->beta->l, c->perm_pk[(base + j) * len + idx].l, &FR);
+                    f_add(t, t, col[idx].l, &FR);
+                    f_add(t, t, e->gamma->l, &FR);
+                    f_mul(left, left, t, &FR);
+                    f_add(t, col[idx].l, delta, &FR);
+                    f_add(t, t, e->gamma->l, &FR);
+                    f_mul(right, right, t, &FR);
+                    f_mul(delta, delta, c->delta_const->l, &FR);
+                }
+                f_mul(value, value, e->y->l, &FR);
+                f_sub(t, left, right, &FR);
+                f_mul(t, t, c->l_active[idx].l, &FR);
+                f_add(value, value, t, &FR);
+            }
+        }
+        for (size_t n = 0; n < c->lookup_count; n++) {
+            /* evaluation.rs:3408-3472 */
+            size_t r_next = rot_idx(idx, 1, e->rot_scale, len);
+            size_t r_prev = rot_idx(idx, -1, e->rot_scale, len);
+            const orc_fr *prod = c->lk_product + n * len, *pin = c->lk_input + n * len, *ptab = c->lk_table + n * len;
+            u64 table[4], ams[4];
+            eval_graph(table, &c->lookup_graphs[n], e, idx, zero, inter);
+            f_sub(ams, pin[idx].l, ptab[idx].l, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_sub(t, one, prod[idx].l, &FR);
+            f_mul(t, t, c->l0[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_mul(t, prod[idx].l, prod[idx].l, &FR);
+            f_sub(t, t, prod[idx].l, &FR);
+            f_mul(t, t, c->l_last[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_add(t, pin[idx].l, e->beta->l, &FR);
+            f_mul(t, prod[r_next].l, t, &FR);
+            f_add(t2, ptab[idx].l, e->gamma->l, &FR);
+            f_mul(t, t, t2, &FR);
+            f_mul(t2, prod[idx].l, table, &FR);
+            f_sub(t, t, t2, &FR);
+            f_mul(t, t, c->l_active[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_mul(t, ams, c->l0[idx].l, &FR);
+            f_add(value, value, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_sub(t, pin[idx].l, pin[r_prev].l, &FR);
+            f_mul(t, ams, t, &FR);
+            f_mul(t, t, c->l_active[idx].l, &FR);
+            f_add(value, value, t, &FR);
+        }
+        for (size_t n = 0; n < c->trash_count; n++) {
+            /* evaluation.rs:3489-3521 */
+            uint32_t sel = c->trash_sel[n];
+            if (sel >= e->fixed_cols) continue;
+            u64 comp[4];
+            eval_graph(comp, &c->trash_graphs[n], e, idx, zero, inter);
+            f_sub(t, one, e->fixed[(size_t)sel * len + idx].l, &FR);
+            f_mul(t, t, c->trash_cosets[n * len + idx].l, &FR);
+            f_sub(t, comp, t, &FR);
+            f_mul(value, value, e->y->l, &FR);
+            f_add(value, value, t, &FR);
+        }
+        memcpy(c->out[idx].l, value, 32);
+    }
+    free(inter);
+}
+
+int orc_eval_numerator(orc_fr *out, size_t len, const orc_fr *initial_out, uint32_t run_custom,
+                       const orc_fr *fixed, size_t fixed_cols, const orc_fr *advice, size_t advice_cols,
+                       const orc_fr *instance, size_t instance_cols, const orc_fr *challenges,
+                       size_t challenge_len, const orc_fr *beta, const orc_fr *gamma, const orc_fr *theta,
+                       const orc_fr *trash_challenge, const orc_fr *y, const orc_fr *omega,
+                       const orc_fr *delta_start, const orc_fr *delta_const, int32_t rot_scale,
+                       int32_t last_rotation, uint32_t chunk_len, const orc_fr *l0, const orc_fr *l_last,
+                       const orc_fr *l_active, const orc_fr *permutation_products, size_t permutation_sets,
+                       const orc_column_ref *permutation_columns, size_t permutation_columns_len,
+                       const orc_fr *permutation_pk_cosets, const orc_fr *lookup_product_cosets,
+                       const orc_fr *lookup_input_cosets, const orc_fr *lookup_table_cosets,
+                       size_t lookup_count, const orc_fr *trash_cosets,
+                       const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+                       const orc_graph *custom_graph, const orc_graph *lookup_graphs,
+                       const orc_graph *trash_graphs, int threads)
+{
+    INIT();
+    if (len == 0) return 0;
+    if (!run_custom && !initial_out) return -1;
+    num_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.out = out;
+    c.initial = initial_out;
+    c.run_custom = run_custom;
+    c.env.len = len;
+    c.env.rot_scale = rot_scale;
+    c.env.fixed = fixed;
+    c.env.fixed_cols = fixed_cols;
+    c.env.advice = advice;
+    c.env.advice_cols = advice_cols;
+    c.env.instance = instance;
+    c.env.instance_cols = instance_cols;
+    c.env.challenges = challenges;
+    c.env.challenge_len = challenge_len;
+    c.env.beta = beta;
+    c.env.gamma = gamma;
+    c.env.theta = theta;
+    c.env.trash = trash_challenge;
+    c.env.y = y;
+    c.omega = omega;
+    c.delta_start = delta_start;
+    c.delta_const = delta_const;
+    c.last_rotation = last_rotation;
+    c.chunk_len = chunk_len;
+    c.l0 = l0;
+    c.l_last = l_last;
+    c.l_active = l_active;
+    c.perm_products = permutation_products;
+    c.perm_sets = permutation_sets;
+    c.perm_columns = permutation_columns;
+    c.perm_columns_len = permutation_columns_len;
+    c.perm_pk = permutation_pk_cosets;
+    c.lk_product = lookup_product_cosets;
+    c.lk_input = lookup_input_cosets;
+    c.lk_table = lookup_table_cosets;
+    c.lookup_count = lookup_count;
+    c.trash_cosets = trash_cosets;
+    c.trash_sel = trash_selector_fixed_indices;
+    c.trash_count = trash_count;
+    c.custom = custom_graph;
+    c.lookup_graphs = lookup_graphs;
+    c.trash_graphs = trash_graphs;
+    uint32_t mx = run_custom ? custom_graph->num_intermediates : 0;
+    for (size_t i = 0; i < lookup_count; i++)
+        if (lookup_graphs[i].num_intermediates > mx) mx = lookup_graphs[i].num_intermediates;
+    for (size_t i = 0; i < trash_count; i++)
+        if (trash_graphs[i].num_intermediates > mx) mx = trash_graphs[i].num_intermediates;
+    c.max_inter = mx;
+    parallel_for(len, threads, num_range, &c);
+    return 0;
+}

@@ -132,6 +132,45 @@ int orc_fr_quotient_pieces(orc_fr *out, const orc_fr *quotient, size_t quotient_
                            size_t blind_count);
 void orc_fr_sort_canonical(orc_fr *a, size_t len);
 
+/* ---- quotient numerator ------------------------------------------------- */
+/* Same memory layout as the C ABI's RawValueSource / RawCalculation /
+ * RawGraph / RawColumnRef (midnight-sppark-msm/src/lib.rs:38-86). */
+typedef struct { uint32_t kind, a, b; } orc_value_source;
+typedef struct {
+    uint32_t op, target, parts_offset, parts_len;
+    orc_value_source lhs, rhs;
+} orc_calculation;
+typedef struct {
+    const orc_fr *constants;
+    size_t constants_len;
+    const int32_t *rotations;
+    size_t rotations_len;
+    const orc_calculation *calculations;
+    size_t calculations_len;
+    const orc_value_source *horner_parts;
+    size_t horner_parts_len;
+    uint32_t num_intermediates;
+} orc_graph;
+typedef struct { uint32_t kind, index; } orc_column_ref;
+
+/* Evaluator::evaluate_numerator (evaluation.rs:3114-3528) with the argument
+ * shapes of midnight_sppark_bls12_381_eval_numerator (.cu:5196). */
+int orc_eval_numerator(orc_fr *out, size_t len, const orc_fr *initial_out, uint32_t run_custom,
+                       const orc_fr *fixed, size_t fixed_cols, const orc_fr *advice, size_t advice_cols,
+                       const orc_fr *instance, size_t instance_cols, const orc_fr *challenges,
+                       size_t challenge_len, const orc_fr *beta, const orc_fr *gamma, const orc_fr *theta,
+                       const orc_fr *trash_challenge, const orc_fr *y, const orc_fr *omega,
+                       const orc_fr *delta_start, const orc_fr *delta_const, int32_t rot_scale,
+                       int32_t last_rotation, uint32_t chunk_len, const orc_fr *l0, const orc_fr *l_last,
+                       const orc_fr *l_active, const orc_fr *permutation_products, size_t permutation_sets,
+                       const orc_column_ref *permutation_columns, size_t permutation_columns_len,
+                       const orc_fr *permutation_pk_cosets, const orc_fr *lookup_product_cosets,
+                       const orc_fr *lookup_input_cosets, const orc_fr *lookup_table_cosets,
+                       size_t lookup_count, const orc_fr *trash_cosets,
+                       const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+                       const orc_graph *custom_graph, const orc_graph *lookup_graphs,
+                       const orc_graph *trash_graphs, int threads);
+
 #ifdef __cplusplus
 }
 #endif

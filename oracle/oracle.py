@@ -415,3 +415,98 @@ def fr_sort_canonical(a):
     a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
     lib().orc_fr_sort_canonical(_p(a), len(a))
     return a
+
+
+# ---------------------------------------------------------------- quotient numerator
+
+class _VS(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("a", ctypes.c_uint32), ("b", ctypes.c_uint32)]
+
+
+class _Calc(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_uint32), ("target", ctypes.c_uint32), ("parts_offset", ctypes.c_uint32),
+                ("parts_len", ctypes.c_uint32), ("lhs", _VS), ("rhs", _VS)]
+
+
+class _Graph(ctypes.Structure):
+    _fields_ = [("constants", ctypes.c_void_p), ("constants_len", ctypes.c_size_t),
+                ("rotations", ctypes.c_void_p), ("rotations_len", ctypes.c_size_t),
+                ("calculations", ctypes.c_void_p), ("calculations_len", ctypes.c_size_t),
+                ("horner_parts", ctypes.c_void_p), ("horner_parts_len", ctypes.c_size_t),
+                ("num_intermediates", ctypes.c_uint32)]
+
+
+class _ColRef(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("index", ctypes.c_uint32)]
+
+
+class OracleGraph:
+    """Same description as the product's Graph: (constants, rotations,
+    calcs, parts, num_intermediates)."""
+
+    def __init__(self, constants, rotations, calcs, parts, num_intermediates):
+        self.constants = np.ascontiguousarray(np.asarray(constants, dtype=np.uint64).reshape(-1, 4))
+        self.rotations = np.ascontiguousarray(np.asarray(rotations, dtype=np.int32))
+        self.calcs = (_Calc * max(len(calcs), 1))()
+        for i, (op, tgt, po, pl, lhs, rhs) in enumerate(calcs):
+            self.calcs[i] = _Calc(op, tgt, po, pl, _VS(*lhs), _VS(*rhs))
+        self.parts = (_VS * max(len(parts), 1))()
+        for i, pt in enumerate(parts):
+            self.parts[i] = _VS(*pt)
+        self.n = (len(calcs), len(parts))
+        self.ni = num_intermediates
+
+    def raw(self):
+        def ptr(a):
+            return a.ctypes.data_as(ctypes.c_void_p) if a.size else None
+        return _Graph(ptr(self.constants), len(self.constants), ptr(self.rotations), len(self.rotations),
+                      ctypes.cast(self.calcs, ctypes.c_void_p), self.n[0], ctypes.cast(self.parts, ctypes.c_void_p),
+                      self.n[1], self.ni)
+
+
+def eval_numerator(length, custom_graph, fixed=None, advice=None, instance=None, challenges=None, beta=None,
+                   gamma=None, theta=None, trash_challenge=None, y=None, omega=None, delta_start=None,
+                   delta_const=None, rot_scale=1, last_rotation=-1, chunk_len=1, l0=None, l_last=None,
+                   l_active=None, permutation_products=None, permutation_sets=0, permutation_columns=(),
+                   permutation_pk_cosets=None, lookups=(), trash=(), initial_out=None, threads=None):
+    """Evaluator::evaluate_numerator (evaluation.rs:3114-3528) restated in C."""
+    L = lib()
+    f = L.orc_eval_numerator
+    vp = ctypes.c_void_p
+    f.restype = ctypes.c_int
+    z = np.zeros(4, dtype=np.uint64)
+
+    def arr(a):
+        return None if a is None else np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4)
+
+    def p(a):
+        return None if a is None or not a.size else a.ctypes.data_as(vp)
+
+    def sc(v):
+        return np.ascontiguousarray(z if v is None else v, dtype=np.uint64).reshape(4)
+
+    fx, ad, ins, ch = arr(fixed), arr(advice), arr(instance), arr(challenges)
+    lag = [arr(x) for x in (l0, l_last, l_active)]
+    pp, pk = arr(permutation_products), arr(permutation_pk_cosets)
+    pcols = (_ColRef * max(len(permutation_columns), 1))(*[_ColRef(k, i) for k, i in permutation_columns])
+    lk = [np.concatenate([arr(l[i]) for l in lookups]) if lookups else None for i in (1, 2, 3)]
+    lkg = (_Graph * max(len(lookups), 1))(*[l[0].raw() for l in lookups])
+    trc = np.concatenate([arr(t[1]) for t in trash]) if trash else None
+    trs = np.array([t[2] for t in trash] or [0], dtype=np.uint32)
+    trg = (_Graph * max(len(trash), 1))(*[t[0].raw() for t in trash])
+    scal = [sc(v) for v in (beta, gamma, theta, trash_challenge, y, omega, delta_start, delta_const)]
+    init = arr(initial_out)
+    cg = custom_graph.raw() if custom_graph is not None else _Graph()
+    out = np.zeros((length, 4), dtype=np.uint64)
+    rc = f(p(out), ctypes.c_size_t(length), p(init), ctypes.c_uint32(1 if custom_graph is not None else 0),
+           p(fx), ctypes.c_size_t(0 if fx is None else len(fx) // length), p(ad),
+           ctypes.c_size_t(0 if ad is None else len(ad) // length), p(ins),
+           ctypes.c_size_t(0 if ins is None else len(ins) // length), p(ch), ctypes.c_size_t(0 if ch is None else len(ch)),
+           *[p(s) for s in scal], ctypes.c_int32(rot_scale), ctypes.c_int32(last_rotation), ctypes.c_uint32(chunk_len),
+           p(lag[0]), p(lag[1]), p(lag[2]), p(pp), ctypes.c_size_t(permutation_sets), ctypes.cast(pcols, vp),
+           ctypes.c_size_t(len(permutation_columns)), p(pk), p(lk[0]), p(lk[1]), p(lk[2]),
+           ctypes.c_size_t(len(lookups)), p(trc), trs.ctypes.data_as(vp), ctypes.c_size_t(len(trash)),
+           ctypes.byref(cg), ctypes.cast(lkg, vp), ctypes.cast(trg, vp), ctypes.c_int(threads or threads_default()))
+    if rc:
+        raise ValueError("invalid numerator arguments")
+    return out
