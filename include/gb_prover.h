@@ -274,6 +274,13 @@ GB_API size_t gb_fr_device_vec_len(const void *device_vec);
 GB_API RustError gb_g1_generator_mul(RawG1Affine *out, const RawFr *scalars, size_t n);
 /* same with device pointers; queued on the calling lane's stream */
 GB_API RustError gb_g1_generator_mul_device(RawG1Affine *d_out, const RawFr *d_scalars, size_t n);
+/* KZG SRS (no FFI counterpart; the reference does these in Rust on the CPU):
+ * g_lagrange = iFFT(g) * n^-1 over G1 for 2^k points (arithmetic.rs:34-50,
+ * params.rs:60-77 downsize), and the seeded-tau setup of params.rs:79-129
+ * (g[i] = [tau^i]G, g_lagrange[i] = [(tau^n-1)/n * w^i/(tau - w^i)]G; either
+ * output may be NULL).  Host buffers of 2^k affine points. */
+GB_API RustError gb_g1_to_lagrange(RawG1Affine *out, const RawG1Affine *g, uint32_t k);
+GB_API RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, RawFr tau, uint32_t k);
 /* measured device throughput of 32x32->64 multiply-adds per second */
 GB_API RustError gb_imad_peak(double *out_per_sec);
 /* cumulative host<->device bytes moved by this library */

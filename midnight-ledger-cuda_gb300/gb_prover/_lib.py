@@ -112,6 +112,8 @@ def _declare(L):
         "gb_g1_generator_mul": (E, [vp, vp, sz]),
         "gb_g1_generator_mul_device": (E, [vp, vp, sz]),
         "gb_imad_peak": (E, [ctypes.POINTER(ctypes.c_double)]),
+        "gb_g1_to_lagrange": (E, [vp, vp, u32]),
+        "gb_kzg_setup": (E, [vp, vp, fr, u32]),
         "gb_transfer_counters": (None, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
         "gb_transfer_counters_reset": (None, []),
         "gb_error_free": (None, [vp]),

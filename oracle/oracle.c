@@ -1533,3 +1533,138 @@ int orc_eval_numerator(orc_fr *out, size_t len, const orc_fr *initial_out, uint3
     parallel_for(len, threads, num_range, &c);
     return 0;
 }
+
+/* ======================================================================== */
+/* BLAKE2b (RFC 7693), for the transcript checks                            */
+/* ======================================================================== */
+
+typedef struct {
+    u64 h[8], t[2];
+    uint8_t b[128];
+    size_t c, outlen;
+} b2b_ctx;
+
+static const u64 B2B_IV[8] = {0x6a09e667f3bcc908ULL, 0xbb67ae8584caa73bULL, 0x3c6ef372fe94f82bULL,
+                              0xa54ff53a5f1d36f1ULL, 0x510e527fade682d1ULL, 0x9b05688c2b3e6c1fULL,
+                              0x1f83d9abfb41bd6bULL, 0x5be0cd19137e2179ULL};
+static const uint8_t B2B_SIGMA[12][16] = {
+    {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15}, {14, 10, 4, 8, 9, 15, 13, 6, 1, 12, 0, 2, 11, 7, 5, 3},
+    {11, 8, 12, 0, 5, 2, 15, 13, 10, 14, 3, 6, 7, 1, 9, 4}, {7, 9, 3, 1, 13, 12, 11, 14, 2, 6, 5, 10, 4, 0, 15, 8},
+    {9, 0, 5, 7, 2, 4, 10, 15, 14, 1, 11, 12, 6, 8, 3, 13}, {2, 12, 6, 10, 0, 11, 8, 3, 4, 13, 7, 5, 15, 14, 1, 9},
+    {12, 5, 1, 15, 14, 13, 4, 10, 0, 7, 6, 3, 9, 2, 8, 11}, {13, 11, 7, 14, 12, 1, 3, 9, 5, 0, 15, 4, 8, 6, 2, 10},
+    {6, 15, 14, 9, 11, 3, 0, 8, 12, 2, 13, 7, 1, 4, 10, 5}, {10, 2, 8, 4, 7, 6, 1, 5, 15, 11, 9, 14, 3, 12, 13, 0},
+    {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15}, {14, 10, 4, 8, 9, 15, 13, 6, 1, 12, 0, 2, 11, 7, 5, 3}};
+
+static u64 rotr64(u64 x, int n) { return (x >> n) | (x << (64 - n)); }
+
+static void b2b_compress(b2b_ctx *ctx, int last)
+{
+    u64 v[16], m[16];
+    for (int i = 0; i < 8; i++) {
+        v[i] = ctx->h[i];
+        v[i + 8] = B2B_IV[i];
+    }
+    v[12] ^= ctx->t[0];
+    v[13] ^= ctx->t[1];
+    if (last) v[14] = ~v[14];
+    for (int i = 0; i < 16; i++) {
+        m[i] = 0;
+        for (int k = 0; k < 8; k++) m[i] |= (u64)ctx->b[8 * i + k] << (8 * k);
+    }
+#define B2B_G(a, b, c, d, x, y)                \
+    do {                                       \
+        v[a] = v[a] + v[b] + (x);              \
+        v[d] = rotr64(v[d] ^ v[a], 32);        \
+        v[c] = v[c] + v[d];                    \
+        v[b] = rotr64(v[b] ^ v[c], 24);        \
+        v[a] = v[a] + v[b] + (y);              \
+        v[d] = rotr64(v[d] ^ v[a], 16);        \
+        v[c] = v[c] + v[d];                    \
+        v[b] = rotr64(v[b] ^ v[c], 63);        \
+    } while (0)
+    for (int r = 0; r < 12; r++) {
+        const uint8_t *s = B2B_SIGMA[r];
+        B2B_G(0, 4, 8, 12, m[s[0]], m[s[1]]);
+        B2B_G(1, 5, 9, 13, m[s[2]], m[s[3]]);
+        B2B_G(2, 6, 10, 14, m[s[4]], m[s[5]]);
+        B2B_G(3, 7, 11, 15, m[s[6]], m[s[7]]);
+        B2B_G(0, 5, 10, 15, m[s[8]], m[s[9]]);
+        B2B_G(1, 6, 11, 12, m[s[10]], m[s[11]]);
+        B2B_G(2, 7, 8, 13, m[s[12]], m[s[13]]);
+        B2B_G(3, 4, 9, 14, m[s[14]], m[s[15]]);
+    }
+#undef B2B_G
+    for (int i = 0; i < 8; i++) ctx->h[i] ^= v[i] ^ v[i + 8];
+}
+
+static void b2b_update(b2b_ctx *ctx, const uint8_t *in, size_t len)
+{
+    for (size_t i = 0; i < len; i++) {
+        if (ctx->c == 128) {
+            ctx->t[0] += ctx->c;
+            if (ctx->t[0] < ctx->c) ctx->t[1]++;
+            b2b_compress(ctx, 0);
+            ctx->c = 0;
+        }
+        ctx->b[ctx->c++] = in[i];
+    }
+}
+
+static void b2b_init(b2b_ctx *ctx, size_t outlen, const uint8_t *key, size_t keylen)
+{
+    for (int i = 0; i < 8; i++) ctx->h[i] = B2B_IV[i];
+    ctx->h[0] ^= 0x01010000ULL ^ ((u64)keylen << 8) ^ (u64)outlen;
+    ctx->t[0] = ctx->t[1] = 0;
+    ctx->c = 0;
+    ctx->outlen = outlen;
+    memset(ctx->b, 0, 128);
+    if (keylen) {
+        b2b_update(ctx, key, keylen);
+        ctx->c = 128;
+    }
+}
+
+/* digest of the state so far, leaving the state usable (like
+ * blake2b_simd::State::finalize, which works on a copy) */
+static void b2b_final_copy(const b2b_ctx *in, uint8_t *out)
+{
+    b2b_ctx ctx = *in;
+    ctx.t[0] += ctx.c;
+    if (ctx.t[0] < ctx.c) ctx.t[1]++;
+    while (ctx.c < 128) ctx.b[ctx.c++] = 0;
+    b2b_compress(&ctx, 1);
+    for (size_t i = 0; i < ctx.outlen; i++) out[i] = (uint8_t)(ctx.h[i >> 3] >> (8 * (i & 7)));
+}
+
+void orc_blake2b(uint8_t *out, size_t outlen, const uint8_t *key, size_t keylen, const uint8_t *in, size_t len)
+{
+    b2b_ctx ctx;
+    b2b_init(&ctx, outlen, key, keylen);
+    b2b_update(&ctx, in, len);
+    b2b_final_copy(&ctx, out);
+}
+
+/* Transcript replay (transcript/mod.rs:95-150, implementors.rs:13-33):
+ * ops[i] = 1 absorbs msgs[i] (prefix 0x01), ops[i] = 0 squeezes (prefix 0x00
+ * then digest -> from_uniform_bytes) into challenges[j++]. */
+void orc_transcript_replay(const uint8_t *ops, size_t nops, const uint8_t *const *msgs, const size_t *lens,
+                           orc_fr *challenges)
+{
+    INIT();
+    static const uint8_t key[] = "Domain separator for transcript";
+    b2b_ctx ctx;
+    b2b_init(&ctx, 64, key, sizeof(key) - 1);
+    size_t j = 0;
+    for (size_t i = 0; i < nops; i++) {
+        if (ops[i]) {
+            uint8_t one = 1;
+            b2b_update(&ctx, &one, 1);
+            b2b_update(&ctx, msgs[i], lens[i]);
+        } else {
+            uint8_t zero = 0, d[64];
+            b2b_update(&ctx, &zero, 1);
+            b2b_final_copy(&ctx, d);
+            orc_fr_from_uniform_bytes(&challenges[j++], d);
+        }
+    }
+}

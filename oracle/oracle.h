@@ -171,6 +171,11 @@ int orc_eval_numerator(orc_fr *out, size_t len, const orc_fr *initial_out, uint3
                        const orc_graph *custom_graph, const orc_graph *lookup_graphs,
                        const orc_graph *trash_graphs, int threads);
 
+/* ---- transcript ---------------------------------------------------------- */
+void orc_blake2b(uint8_t *out, size_t outlen, const uint8_t *key, size_t keylen, const uint8_t *in, size_t len);
+void orc_transcript_replay(const uint8_t *ops, size_t nops, const uint8_t *const *msgs, const size_t *lens,
+                           orc_fr *challenges);
+
 #ifdef __cplusplus
 }
 #endif

@@ -510,3 +510,29 @@ def eval_numerator(length, custom_graph, fixed=None, advice=None, instance=None,
     if rc:
         raise ValueError("invalid numerator arguments")
     return out
+
+
+# ---------------------------------------------------------------- transcript
+
+def blake2b(data, key=b"", outlen=64):
+    L = lib()
+    out = (ctypes.c_uint8 * outlen)()
+    kb = (ctypes.c_uint8 * max(len(key), 1)).from_buffer_copy(key or b"\0")
+    db = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data or b"\0")
+    L.orc_blake2b(out, ctypes.c_size_t(outlen), kb, ctypes.c_size_t(len(key)), db, ctypes.c_size_t(len(data)))
+    return bytes(out)
+
+
+def transcript_replay(ops):
+    """ops: list of ("absorb", bytes) or ("squeeze",); returns the challenges (n, 4)."""
+    L = lib()
+    n = len(ops)
+    kinds = (ctypes.c_uint8 * max(n, 1))(*[1 if o[0] == "absorb" else 0 for o in ops])
+    bufs = [(ctypes.c_uint8 * max(len(o[1]), 1)).from_buffer_copy(o[1] or b"\0") if o[0] == "absorb" else None
+            for o in ops]
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[ctypes.cast(b, ctypes.c_void_p) if b is not None else None for b in bufs])
+    lens = (ctypes.c_size_t * max(n, 1))(*[len(o[1]) if o[0] == "absorb" else 0 for o in ops])
+    nsq = sum(1 for o in ops if o[0] == "squeeze")
+    out = np.zeros((max(nsq, 1), 4), dtype=np.uint64)
+    L.orc_transcript_replay(kinds, ctypes.c_size_t(n), ptrs, lens, _p(out))
+    return out[:nsq]
