@@ -339,6 +339,72 @@ def main():
         dist.destroy_process_group()
 
 
+def mixed_scalars(n, rng):
+    """70% uniform Fr, 20% uniform below 2^64, 10% zero."""
+    s = fr_uniform(n, rng)
+    u = rng.random(n)
+    small = (u >= 0.7) & (u < 0.9)
+    k = int(small.sum())
+    s[small] = 0
+    # a uniform value below 2^64 in Montgomery form: v * R mod r, computed exactly
+    vals = rng.integers(0, 2**63, size=k, dtype=np.int64).astype(object) * 2 + rng.integers(0, 2, size=k)
+    R = pow(2, 256, R_MOD)
+    mont = [(int(v) * R) % R_MOD for v in vals]
+    s[small] = np.array([[(m >> (64 * i)) & 0xFFFFFFFFFFFFFFFF for i in range(4)] for m in mont],
+                        dtype=np.uint64).reshape(-1, 4)
+    s[u >= 0.9] = 0
+    return s
+
+
+def batched_config(gb, torch, rng):
+    """64 MSMs with sizes round(2^U), U ~ U[10, 18], the 70/20/10 scalar mix,
+    against a resident 2^18 SRS-like base set: one batched call versus one
+    call per MSM; and 64 NTTs of the matching power-of-two sizes, batched per
+    size versus one call per NTT."""
+    sizes = [int(round(2 ** u)) for u in rng.uniform(10, 18, size=64)]
+    N = 1 << 18
+    bases = gb.g1_generator_mul(fr_uniform(N, rng))
+    ctx = gb.Bls12_381G1MsmContext(bases)
+    scal = [mixed_scalars(n, rng) for n in sizes]
+    flat = np.concatenate(scal)
+    dv = gb.Bls12_381FrDeviceVec.upload(flat)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    slices = [(int(o), 0, n) for o, n in zip(offs, sizes)]
+    stream = torch.cuda.ExternalStream(gb.lane_stream())
+
+    def timed(fn, reps=3):
+        fn()
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    batched = timed(lambda: ctx.device_ragged(dv, slices))
+    single = timed(lambda: [ctx.device_ragged(dv, [sl]) for sl in slices])
+    out = {"msm64_total_points": int(sum(sizes)), "msm64_batched_ms": batched, "msm64_one_at_a_time_ms": single,
+           "msm64_batched_mpts_s": sum(sizes) / batched / 1e3}
+    # NTTs: next power of two of each size
+    logs = [max(1, (n - 1).bit_length()) for n in sizes]
+    polys = {lg: fr_uniform((1 << lg) * logs.count(lg), rng) for lg in set(logs)}
+    one = np.array([0x00000001FFFFFFFE, 0x5884B7FA00034802, 0x998C4FEFECBC4FF5, 0x1824B159ACC5056F], np.uint64)
+    vecs = {lg: gb.Bls12_381FrDeviceVec.upload(v) for lg, v in polys.items()}
+    singles = {lg: [gb.Bls12_381FrDeviceVec.upload(polys[lg][i << lg:(i + 1) << lg]) for i in range(logs.count(lg))]
+               for lg in set(logs)}
+    out["ntt64_batched_ms"] = timed(lambda: [vecs[lg].ntt_zeta_batch(lg, logs.count(lg), False, one, one, one)
+                                             for lg in vecs])
+    out["ntt64_one_at_a_time_ms"] = timed(lambda: [v.ntt_zeta(lg, False, one, one, one)
+                                                   for lg in singles for v in singles[lg]])
+    del ctx, dv
+    return out
+
+
 def extras(gb, torch, n, rng, bases, args):
     """Secondary numbers of the same configuration (not the headline)."""
     out = {}
@@ -372,6 +438,7 @@ def extras(gb, torch, n, rng, bases, args):
     lde.download(1)
     out["lde_2p20_to_2p22_x16_host_in_ms"] = (time.perf_counter() - t0) * 1e3
     del lde, src
+    out.update(batched_config(gb, torch, rng))
     return out
 
 

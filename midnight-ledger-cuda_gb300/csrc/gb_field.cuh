@@ -436,10 +436,16 @@ template <class Cfg>
 GB_D void mont_step(uint32_t *even, uint32_t *odd, const uint32_t *a, uint32_t bi)
 {
     constexpr int N = Cfg::N;
-#pragma unroll
-    for (int j = 0; j < N + 1; j++) odd[j] = 0;
     row_mac<N>(even, a, 0, bi);
-    row_mac<N>(odd, a, 1, bi);
+    // the odd row starts from zero each step: its limbs are plain products
+    // (no overlaps, so no carries) -- independent multiplies that can issue
+    // alongside the even row's carry chain
+#pragma unroll
+    for (int k = 0; k < N / 2; k++) {
+        odd[2 * k] = a[2 * k + 1] * bi;
+        odd[2 * k + 1] = __umulhi(a[2 * k + 1], bi);
+    }
+    odd[N] = 0;
     // value = even + odd * 2^32; the Montgomery step makes even[0] zero
     const uint32_t m = even[0] * Cfg::INV;
     row_mac_mod<Cfg>(even, 0, m);

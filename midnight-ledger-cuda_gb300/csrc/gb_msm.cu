@@ -1,25 +1,29 @@
 // BLS12-381 G1 multiexp (Pippenger) for sm_103a, and the MSM entry points
 // of the C ABI (midnight-sppark-msm/src/bls12_381_g1_msm.cu:6164-6486).
 //
-// Pipeline for one MSM of n (scalar, base) pairs with window c:
+// One engine serves every entry point: a BATCH of MSMs (one or many, of
+// uneven sizes) goes through each pipeline stage in a single launch.
 //   1. recode     : Montgomery -> canonical, signed c-bit digits per window
 //                   (digit in [-2^(c-1), 2^(c-1)], carry into the next window)
 //   2. histogram  : per-block shared-memory counts of bucket keys
-//   3. column scan: per-key prefix over blocks + per-key totals
+//   3. column scan: per-key prefix over the blocks of its segment + totals
 //   4. key scan   : exclusive scan of totals -> bucket start offsets
 //   5. scatter    : (bucket, point) pairs placed in bucket order
 //   6. accumulate : each thread sums L consecutive sorted entries into XYZZ
-//                   accumulators (fixed work per thread), writing finished
-//                   buckets directly and chunk-edge partials aside
+//                   accumulators (fixed work per thread whatever the bucket
+//                   sizes), writing finished buckets directly and chunk-edge
+//                   partials aside
 //   7. fix-up     : buckets spanning chunks add their partials
-//   8. reduce     : sum_k (k+1) * B_k per window by segmented running sums,
-//                   then a tree over segments, then the window combination.
+//   8. reduce     : sum_k (k+1) B_k per segment by segmented running sums and
+//                   a tree, then per MSM the window combination.
 //
-// Two modes share this pipeline.  "Plain" mode keys buckets by
-// (window, digit) and combines windows by Horner's rule.  "Precomputed" mode
-// (MSM contexts, whose bases are fixed) stores 2^(c*j) * P_i for every window
-// j at context creation, so all windows feed ONE set of 2^(c-1) buckets and
-// no window combination is needed.
+// A "segment" owns 2^(c-1) buckets.  Two modes:
+//   * precomputed (MSM contexts, whose bases are fixed): context creation
+//     stores 2^(c*j) P_i for every window j, so each MSM is ONE segment and
+//     needs no window combination;
+//   * plain (bases passed per call): each (MSM, window) is a segment and the
+//     windows are combined by Horner's rule.
+// Both decode a digit's point as point_base + (d / n) * stride + d % n.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -32,60 +36,7 @@ namespace gb {
 static constexpr uint32_t kZeroDigit = 0xffffffffu;
 static constexpr int kMaxWindowBits = 16;  // 2^15 u32 counters = 128 KB smem
 
-struct msm_plan {
-    int c;             // window bits
-    int nwin;          // windows: floor(255 / c) + 1 -> nwin * c >= 256
-    bool precomputed;  // bases hold 2^(c*j) P_i for every window j
-    size_t n;          // points
-    uint32_t K;        // buckets per segment = 2^(c-1)
-    uint32_t nseg;     // segments: nwin (plain) or 1 (precomputed)
-    uint32_t G;        // total buckets = nseg * K
-    size_t seglen;     // digits per segment
-    uint32_t bps;      // sort blocks per segment
-    size_t per_block;  // digits per sort block
-    uint32_t L;        // sorted entries per accumulate thread
-    uint32_t S;        // reduction sub-segments per segment
-    int acc_variant;   // accumulate kernel instantiation (0: 256x1, 1: 256x2, 2: 128x3);
-                       // GB_MSM_ACC_VARIANT overrides the default for tuning runs
-};
-
-static int default_acc_variant()
-{
-    const char *e = getenv("GB_MSM_ACC_VARIANT");
-    if (e && e[0] >= '0' && e[0] <= '2') return e[0] - '0';
-    return 1;  // 256 threads, 2 blocks per SM: the fastest on GB300 at n = 2^20
-}
-
 static int windows_for(int c) { return 255 / c + 1; }
-
-static msm_plan make_plan(size_t n, int c, bool precomputed)
-{
-    msm_plan p;
-    p.c = c;
-    p.nwin = windows_for(c);
-    p.precomputed = precomputed;
-    p.n = n;
-    p.K = 1u << (c - 1);
-    p.nseg = precomputed ? 1 : (uint32_t)p.nwin;
-    p.G = p.nseg * p.K;
-    p.seglen = precomputed ? n * (size_t)p.nwin : n;
-    size_t total = n * (size_t)p.nwin;
-    // aim for ~4 sort blocks per SM-pair over all segments, >= 4096 digits each
-    size_t target_blocks = 608;
-    size_t per = (total + target_blocks - 1) / target_blocks;
-    per = std::max<size_t>(per, 4096);
-    per = std::min<size_t>(per, (size_t)1 << 16);
-    p.bps = (uint32_t)((p.seglen + per - 1) / per);
-    p.per_block = (p.seglen + p.bps - 1) / p.bps;
-    // accumulate chunk: about 2 expected entries per bucket, 8..64
-    double avg = (double)total / (double)p.G;
-    uint32_t L = (uint32_t)std::max(8.0, std::min(64.0, avg * 0.5));
-    p.L = L;
-    uint32_t S = std::min<uint32_t>(p.K, precomputed ? 8192u : 256u);
-    p.S = S;
-    p.acc_variant = default_acc_variant();
-    return p;
-}
 
 // Window size: minimise mixed additions plus bucket-reduction additions.
 static int choose_window(size_t n, bool precomputed)
@@ -106,6 +57,39 @@ static int choose_window(size_t n, bool precomputed)
     return best;
 }
 
+static int default_acc_variant()
+{
+    const char *e = getenv("GB_MSM_ACC_VARIANT");
+    if (e && e[0] >= '0' && e[0] <= '2') return e[0] - '0';
+    return 1;  // 256 threads, 2 blocks per SM: the fastest on GB300 at n = 2^20
+}
+
+// one MSM of a batch (host view)
+struct msm_item {
+    const fr_t *scalars;  // device pointer, n values
+    size_t n;
+    size_t point_base;    // first base of this MSM in table row 0
+};
+
+// per-segment and per-sort-block descriptors (device view)
+struct seg_desc {
+    uint64_t digit_off;   // first digit of the segment
+    uint32_t len;         // digits in the segment
+    uint32_t n;           // points of the segment's MSM (digit d -> window d / n, point d % n)
+    uint64_t point_base;  // base index of the MSM's first point in table row 0
+    uint32_t blk0, nblk;  // sort blocks of the segment
+};
+struct blk_desc {
+    uint32_t seg;
+    uint32_t lo, hi;      // digit range within the segment
+};
+struct item_desc {
+    const fr_t *scalars;
+    uint64_t point_prefix;  // sum of n over earlier items (thread -> item map)
+    uint64_t digit_base;    // digits of the item start here: [window][n]
+    uint32_t n;
+};
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
@@ -120,74 +104,81 @@ __device__ __forceinline__ affine_t load_affine(const affine_t *pts, uint32_t id
     return r;
 }
 
-// 1. recode: digits[j * n + i] = key | sign << 31, or kZeroDigit
-__global__ void msm_recode_kernel(const fr_t *__restrict__ scalars, size_t n, int c, int nwin,
-                                  uint32_t key_stride, uint32_t *__restrict__ digits)
+// 1. recode: for item m, point i, window j: digits[base_m + j * n_m + i] =
+//    (|digit| - 1) | sign << 31, or kZeroDigit
+__global__ void msm_recode_kernel(const item_desc *__restrict__ items, uint32_t nitems, uint64_t total, int c,
+                                  int nwin, uint32_t *__restrict__ digits)
 {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    fr_t s = scalars[i];
-    s = s.from_mont();
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    uint32_t lo = 0, hi = nitems;  // last item with point_prefix <= t
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (items[mid].point_prefix <= t) lo = mid;
+        else hi = mid;
+    }
+    const item_desc it = items[lo];
+    const uint64_t i = t - it.point_prefix;
+    fr_t s = it.scalars[i].from_mont();
     const uint32_t half = 1u << (c - 1);
     const uint32_t mask = (1u << c) - 1;
     uint32_t carry = 0;
+    uint32_t *out = digits + it.digit_base + i;
     for (int j = 0; j < nwin; j++) {
         int bit = j * c;
         int limb = bit >> 5, off = bit & 31;
-        uint32_t lo = limb < 8 ? s.v[limb] : 0;
-        uint32_t hi = limb + 1 < 8 ? s.v[limb + 1] : 0;
-        uint32_t raw = (uint32_t)((((uint64_t)hi << 32) | lo) >> off) & mask;
+        uint32_t l0 = limb < 8 ? s.v[limb] : 0;
+        uint32_t l1 = limb + 1 < 8 ? s.v[limb + 1] : 0;
+        uint32_t raw = (uint32_t)((((uint64_t)l1 << 32) | l0) >> off) & mask;
         raw += carry;
-        uint32_t out;
+        uint32_t d;
         if (raw == 0) {
             carry = 0;
-            out = kZeroDigit;
+            d = kZeroDigit;
         } else if (raw <= half) {
             carry = 0;
-            out = (raw - 1) + (uint32_t)j * key_stride;
+            d = raw - 1;
         } else {
             carry = 1;
             uint32_t mag = (1u << c) - raw;  // digit = raw - 2^c < 0
-            out = mag == 0 ? kZeroDigit : (((mag - 1) + (uint32_t)j * key_stride) | 0x80000000u);
+            d = mag == 0 ? kZeroDigit : ((mag - 1) | 0x80000000u);
         }
-        digits[(size_t)j * n + i] = out;
+        out[(uint64_t)j * it.n] = d;
     }
 }
 
-// 2. per-block histograms: hist[b][k] for block b of segment (b / bps)
-__global__ void msm_hist_kernel(const uint32_t *__restrict__ digits, size_t seglen, uint32_t bps,
-                                size_t per_block, uint32_t K, uint32_t *__restrict__ hist)
+// 2. per-block histograms: hist[b][k]
+__global__ void msm_hist_kernel(const uint32_t *__restrict__ digits, const seg_desc *__restrict__ segs,
+                                const blk_desc *__restrict__ blks, uint32_t K, uint32_t *__restrict__ hist)
 {
     extern __shared__ uint32_t sh[];
-    const uint32_t b = blockIdx.x;
-    const uint32_t seg = b / bps, within = b % bps;
+    const blk_desc bd = blks[blockIdx.x];
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) sh[k] = 0;
     __syncthreads();
-    size_t lo = (size_t)within * per_block;
-    size_t hi = std::min(lo + per_block, seglen);
-    const uint32_t *d = digits + (size_t)seg * seglen;
-    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const uint32_t *d = digits + segs[bd.seg].digit_off;
+    for (uint32_t i = bd.lo + threadIdx.x; i < bd.hi; i += blockDim.x) {
         uint32_t v = d[i];
-        if (v != kZeroDigit) atomicAdd(&sh[(v & 0x7fffffffu) & (K - 1)], 1u);
+        if (v != kZeroDigit) atomicAdd(&sh[v & (K - 1)], 1u);
     }
     __syncthreads();
-    uint32_t *out = hist + (size_t)b * K;
+    uint32_t *out = hist + (size_t)blockIdx.x * K;
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) out[k] = sh[k];
 }
 
-// 3. per global key g = seg*K + k: exclusive prefix over the segment's
+// 3. per global key g = seg * K + k: exclusive prefix over the segment's
 //    blocks (in place in hist) and the total into counts[g]
-__global__ void msm_colscan_kernel(uint32_t *__restrict__ hist, uint32_t bps, uint32_t K,
+__global__ void msm_colscan_kernel(uint32_t *__restrict__ hist, const seg_desc *__restrict__ segs, uint32_t K,
                                    uint32_t G, uint32_t *__restrict__ counts)
 {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    uint32_t seg = g / K, k = g % K;
+    const seg_desc sd = segs[g / K];
+    const uint32_t k = g % K;
     uint32_t run = 0;
-    uint32_t *col = hist + (size_t)seg * bps * K + k;
+    uint32_t *col = hist + (size_t)sd.blk0 * K + k;
     uint32_t w = 0;
     // batches of 16 independent loads keep the column walk off the latency path
-    for (; w + 16 <= bps; w += 16) {
+    for (; w + 16 <= sd.nblk; w += 16) {
         uint32_t v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = col[(size_t)(w + u) * K];
@@ -197,7 +188,7 @@ __global__ void msm_colscan_kernel(uint32_t *__restrict__ hist, uint32_t bps, ui
             run += v[u];
         }
     }
-    for (; w < bps; w++) {
+    for (; w < sd.nblk; w++) {
         uint32_t v = col[(size_t)w * K];
         col[(size_t)w * K] = run;
         run += v;
@@ -205,61 +196,95 @@ __global__ void msm_colscan_kernel(uint32_t *__restrict__ hist, uint32_t bps, ui
     counts[g] = run;
 }
 
-// 4. exclusive scan of counts[0..G) into starts[0..G], starts[G] = total.
-//    One block; each thread scans a contiguous run.
-__global__ void msm_keyscan_kernel(const uint32_t *__restrict__ counts, uint32_t G,
-                                   uint32_t *__restrict__ starts)
+// 4. exclusive scan of counts[0..G) into starts[0..G], starts[G] = total:
+//    tile sums, a one-block scan of the tile sums, then the tiles themselves
+static constexpr uint32_t kScanTileU32 = 4096;
+
+__global__ void u32_tile_sum_kernel(const uint32_t *__restrict__ in, uint32_t n, uint32_t *__restrict__ sums)
+{
+    __shared__ uint32_t sh[256];
+    uint32_t base = blockIdx.x * kScanTileU32;
+    uint32_t s = 0;
+    for (uint32_t i = base + threadIdx.x; i < min(base + kScanTileU32, n); i += 256) s += in[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 128; off; off >>= 1) {
+        if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[blockIdx.x] = sh[0];
+}
+
+// exclusive scan in place of up to 1024 * 64 values with one block
+__global__ void u32_small_scan_kernel(uint32_t *__restrict__ v, uint32_t n)
 {
     __shared__ uint32_t part[1024];
     const uint32_t T = blockDim.x;
-    const uint32_t per = (G + T - 1) / T;
-    const uint32_t lo = threadIdx.x * per;
-    const uint32_t hi = min(lo + per, G);
-    uint32_t sum = 0;
-    for (uint32_t i = lo; i < hi; i++) sum += counts[i];
-    part[threadIdx.x] = sum;
+    const uint32_t per = (n + T - 1) / T;
+    const uint32_t lo = threadIdx.x * per, hi = min(lo + per, n);
+    uint32_t s = 0;
+    for (uint32_t i = lo; i < hi; i++) s += v[i];
+    part[threadIdx.x] = s;
     __syncthreads();
-    // Hillis-Steele inclusive scan over the per-thread sums
     for (uint32_t off = 1; off < T; off <<= 1) {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        uint32_t x = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
         __syncthreads();
-        part[threadIdx.x] += v;
+        part[threadIdx.x] += x;
         __syncthreads();
     }
     uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
     for (uint32_t i = lo; i < hi; i++) {
-        starts[i] = run;
-        run += counts[i];
+        uint32_t x = v[i];
+        v[i] = run;
+        run += x;
     }
-    if (threadIdx.x == T - 1) starts[G] = part[T - 1];
+}
+
+// out[i] = tile prefix + exclusive prefix within the tile
+__global__ void u32_tile_scan_kernel(const uint32_t *__restrict__ in, uint32_t n, const uint32_t *__restrict__ tile_pre,
+                                     uint32_t *__restrict__ out)
+{
+    __shared__ uint32_t part[256];
+    const uint32_t base = blockIdx.x * kScanTileU32;
+    const uint32_t per = kScanTileU32 / 256;
+    const uint32_t lo = base + threadIdx.x * per;
+    uint32_t s = 0;
+    for (uint32_t i = lo; i < min(lo + per, n); i++) s += in[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < 256; off <<= 1) {
+        uint32_t x = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    uint32_t run = tile_pre[blockIdx.x] + (threadIdx.x ? part[threadIdx.x - 1] : 0);
+    for (uint32_t i = lo; i < min(lo + per, n); i++) {
+        out[i] = run;
+        run += in[i];
+    }
 }
 
 // 5. scatter into bucket order: sorted[pos] = point_ref | sign << 31
-__global__ void msm_scatter_kernel(const uint32_t *__restrict__ digits, size_t n, size_t seglen,
-                                   uint32_t bps, size_t per_block, uint32_t K, int precomputed,
+__global__ void msm_scatter_kernel(const uint32_t *__restrict__ digits, const seg_desc *__restrict__ segs,
+                                   const blk_desc *__restrict__ blks, uint32_t K, uint64_t stride,
                                    const uint32_t *__restrict__ hist, const uint32_t *__restrict__ starts,
                                    uint32_t *__restrict__ sorted)
 {
     extern __shared__ uint32_t cursor[];
-    const uint32_t b = blockIdx.x;
-    const uint32_t seg = b / bps, within = b % bps;
-    const uint32_t *h = hist + (size_t)b * K;
-    const uint32_t *st = starts + (size_t)seg * K;
+    const blk_desc bd = blks[blockIdx.x];
+    const seg_desc sd = segs[bd.seg];
+    const uint32_t *h = hist + (size_t)blockIdx.x * K;
+    const uint32_t *st = starts + (size_t)bd.seg * K;
     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) cursor[k] = st[k] + h[k];
     __syncthreads();
-    size_t lo = (size_t)within * per_block;
-    size_t hi = std::min(lo + per_block, seglen);
-    const uint32_t *d = digits + (size_t)seg * seglen;
-    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const uint32_t *d = digits + sd.digit_off;
+    for (uint32_t i = bd.lo + threadIdx.x; i < bd.hi; i += blockDim.x) {
         uint32_t v = d[i];
         if (v == kZeroDigit) continue;
-        uint32_t k = (v & 0x7fffffffu) & (K - 1);
-        uint32_t pos = atomicAdd(&cursor[k], 1u);
-        // point reference: precomputed mode indexes the (window, point) table,
-        // which is laid out exactly like the digit array; plain mode uses the
-        // point index within the window.
-        uint32_t ref = precomputed ? (uint32_t)i : (uint32_t)(i % n);
-        sorted[pos] = ref | (v & 0x80000000u);
+        uint32_t pos = atomicAdd(&cursor[v & (K - 1)], 1u);
+        uint64_t ref = sd.point_base + (uint64_t)(i / sd.n) * stride + (i % sd.n);
+        sorted[pos] = (uint32_t)ref | (v & 0x80000000u);
     }
 }
 
@@ -372,18 +397,20 @@ __global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__rest
     if (threadIdx.x == 0) out[(size_t)seg * gridDim.x + blockIdx.x] = sh[0];
 }
 
-// 8c. combine windows (Horner) and emit a Jacobian point
-__global__ void msm_combine_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t nseg, int c,
-                                   jacobian_t *__restrict__ out)
+// 8c. per MSM: combine its window segments (Horner) and emit a Jacobian point
+__global__ void msm_combine_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t nitems, uint32_t segs_per_item,
+                                   int c, jacobian_t *__restrict__ out)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nitems) return;
+    const xyzz_t *ss = seg_sum + (size_t)m * segs_per_item;
     xyzz_t acc = xyzz_t::inf();
-    for (int w = (int)nseg - 1; w >= 0; w--) {
-        if (w != (int)nseg - 1)
+    for (int w = (int)segs_per_item - 1; w >= 0; w--) {
+        if (w != (int)segs_per_item - 1)
             for (int k = 0; k < c; k++) acc = acc.dbl();
-        acc.add(seg_sum[w]);
+        acc.add(ss[w]);
     }
-    *out = acc.to_jacobian();
+    out[m] = acc.to_jacobian();
 }
 
 // precompute: table[j * n + i] = 2^(c*j) P_i
@@ -411,11 +438,6 @@ __global__ void add_mask_kernel(fr_t *__restrict__ out, const fr_t *__restrict__
 // host engine
 // ---------------------------------------------------------------------------
 
-struct msm_workspace {
-    dev_buf<uint32_t> digits, hist, counts, starts, sorted;
-    dev_buf<xyzz_t> buckets, head, tail, partial, segsum;
-};
-
 static void set_smem_attrs()
 {
     static std::once_flag once;
@@ -426,84 +448,147 @@ static void set_smem_attrs()
     });
 }
 
-// Run one MSM over device-resident scalars; result written to d_out (device).
-static void msm_run(const msm_plan &p, const affine_t *d_points, const fr_t *d_scalars,
-                    jacobian_t *d_out, cudaStream_t s)
+// Exclusive scan of n u32 counts into out[0..n], out[n] = total (device).
+static void u32_exclusive_scan(const uint32_t *in, uint32_t n, uint32_t *out, cudaStream_t s)
+{
+    uint32_t tiles = (n + kScanTileU32 - 1) / kScanTileU32;
+    if (tiles > 1024 * 64) throw cuda_error((int)cudaErrorInvalidValue, "MSM bucket count too large");
+    dev_buf<uint32_t> sums(tiles + 1, s);
+    u32_tile_sum_kernel<<<tiles, 256, 0, s>>>(in, n, sums);
+    GB_CHECK_LAUNCH();
+    // total = sum of tile sums: scan tiles+1 values whose last is 0
+    GB_CUDA_OK(cudaMemsetAsync(sums.get() + tiles, 0, sizeof(uint32_t), s));
+    u32_small_scan_kernel<<<1, 1024, 0, s>>>(sums, tiles + 1);
+    GB_CHECK_LAUNCH();
+    // sums[tiles] now holds the grand total; pass it through device memory
+    u32_tile_scan_kernel<<<tiles, 256, 0, s>>>(in, n, sums, out);
+    GB_CHECK_LAUNCH();
+    GB_CUDA_OK(cudaMemcpyAsync(out + n, sums.get() + tiles, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+}
+
+// Run a batch of MSMs.  precomputed: `points` is a table of nwin rows of
+// `stride` bases (row j = 2^(c*j) P); plain: `points` holds the bases.
+// Results (one Jacobian point per item) are written to d_out (device).
+static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precomputed, const affine_t *points,
+                          size_t stride, jacobian_t *d_out, cudaStream_t s)
 {
     set_smem_attrs();
-    if (p.n == 0) {
-        xyzz_t inf = xyzz_t::inf();
-        jacobian_t j = inf.to_jacobian();
-        GB_CUDA_OK(cudaMemcpyAsync(d_out, &j, sizeof(j), cudaMemcpyHostToDevice, s));
-        GB_CUDA_OK(cudaStreamSynchronize(s));
-        return;
+    const uint32_t nitems = (uint32_t)items.size();
+    if (!nitems) return;
+    const int nwin = windows_for(c);
+    const uint32_t K = 1u << (c - 1);
+    const uint32_t segs_per_item = precomputed ? 1u : (uint32_t)nwin;
+    const uint32_t nseg = nitems * segs_per_item;
+    const uint64_t G64 = (uint64_t)nseg * K;
+    if (G64 >= 0x7fffffffull) throw cuda_error((int)cudaErrorInvalidValue, "MSM batch too large");
+    const uint32_t G = (uint32_t)G64;
+
+    // items, segments, sort blocks
+    std::vector<item_desc> idesc(nitems);
+    std::vector<seg_desc> sdesc(nseg);
+    uint64_t points_total = 0, digits_total = 0;
+    for (uint32_t m = 0; m < nitems; m++) {
+        const msm_item &it = items[m];
+        if (it.n >= 0x7fffffffull / (uint64_t)nwin) throw cuda_error((int)cudaErrorInvalidValue, "MSM too large");
+        idesc[m] = item_desc{it.scalars, points_total, digits_total, (uint32_t)it.n};
+        for (uint32_t j = 0; j < segs_per_item; j++) {
+            seg_desc &sd = sdesc[m * segs_per_item + j];
+            sd.digit_off = digits_total + (precomputed ? 0 : (uint64_t)j * it.n);
+            sd.len = (uint32_t)(precomputed ? it.n * nwin : it.n);
+            sd.n = (uint32_t)std::max<size_t>(it.n, 1);
+            sd.point_base = it.point_base;
+        }
+        points_total += it.n;
+        digits_total += (uint64_t)it.n * nwin;
     }
-    const size_t total = p.n * (size_t)p.nwin;
-    const uint32_t nblocks = p.nseg * p.bps;
-    const size_t nchunks = (total + p.L - 1) / p.L;
-    msm_workspace w;
-    w.digits = dev_buf<uint32_t>(total, s);
-    w.hist = dev_buf<uint32_t>((size_t)nblocks * p.K, s);
-    w.counts = dev_buf<uint32_t>(p.G, s);
-    w.starts = dev_buf<uint32_t>(p.G + 1, s);
-    w.sorted = dev_buf<uint32_t>(total, s);
-    w.buckets = dev_buf<xyzz_t>(p.G, s);
-    w.head = dev_buf<xyzz_t>(nchunks, s);
-    w.tail = dev_buf<xyzz_t>(nchunks, s);
-    w.partial = dev_buf<xyzz_t>((size_t)p.nseg * p.S, s);
-    w.segsum = dev_buf<xyzz_t>(p.nseg, s);
+    if (points_total + stride * (uint64_t)nwin >= 0x80000000ull && precomputed)
+        throw cuda_error((int)cudaErrorInvalidValue, "MSM table too large for 31-bit point references");
+    // ~4 sort blocks per SM pair over the whole batch, 4096..65536 digits each
+    uint64_t per = std::max<uint64_t>(4096, std::min<uint64_t>(65536, (digits_total + 607) / 608));
+    std::vector<blk_desc> bdesc;
+    for (uint32_t sidx = 0; sidx < nseg; sidx++) {
+        seg_desc &sd = sdesc[sidx];
+        sd.blk0 = (uint32_t)bdesc.size();
+        uint32_t nb = (uint32_t)std::max<uint64_t>(1, (sd.len + per - 1) / per);
+        uint32_t chunk = (sd.len + nb - 1) / std::max<uint32_t>(nb, 1);
+        for (uint32_t b = 0; b < nb; b++) {
+            uint32_t lo = b * chunk, hi = std::min(sd.len, lo + chunk);
+            bdesc.push_back(blk_desc{sidx, lo, std::max(lo, hi)});
+        }
+        sd.nblk = nb;
+    }
+    const uint32_t nblocks = (uint32_t)bdesc.size();
+    const double avg = (double)digits_total / (double)G;
+    const uint32_t L = (uint32_t)std::max(8.0, std::min(64.0, avg * 0.5));
+    // reduction sub-segments: ~64K threads over the batch, 32..8192 per segment
+    uint32_t S = 32;
+    while (S < 8192 && (uint64_t)S * 2 * nseg <= 65536) S *= 2;
+    S = std::min<uint32_t>(K, S);
+    const uint64_t nchunks = std::max<uint64_t>(1, (digits_total + L - 1) / L);
+    const int variant = default_acc_variant();
+
+    dev_buf<item_desc> d_items(nitems, s);
+    dev_buf<seg_desc> d_segs(nseg, s);
+    dev_buf<blk_desc> d_blks(nblocks, s);
+    h2d(d_items, idesc.data(), nitems * sizeof(item_desc), s);
+    h2d(d_segs, sdesc.data(), nseg * sizeof(seg_desc), s);
+    h2d(d_blks, bdesc.data(), nblocks * sizeof(blk_desc), s);
+    dev_buf<uint32_t> digits(std::max<uint64_t>(digits_total, 1), s), sorted(std::max<uint64_t>(digits_total, 1), s);
+    dev_buf<uint32_t> hist((size_t)nblocks * K, s), counts(G, s), starts((size_t)G + 1, s);
+    dev_buf<xyzz_t> buckets(G, s), head(nchunks, s), tail(nchunks, s);
+    dev_buf<xyzz_t> partial((size_t)nseg * S, s), segsum(nseg, s);
 
     int tok_all = timed_begin(s);
-    msm_recode_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(d_scalars, p.n, p.c, p.nwin,
-                                                           p.precomputed ? 0u : p.K, w.digits);
+    if (points_total) {
+        msm_recode_kernel<<<(unsigned)((points_total + 255) / 256), 256, 0, s>>>(d_items, nitems, points_total, c,
+                                                                                 nwin, digits);
+        GB_CHECK_LAUNCH();
+    }
+    const size_t smem = (size_t)K * 4;
+    msm_hist_kernel<<<nblocks, 1024, smem, s>>>(digits, d_segs, d_blks, K, hist);
     GB_CHECK_LAUNCH();
-    size_t smem = (size_t)p.K * 4;
-    msm_hist_kernel<<<nblocks, 1024, smem, s>>>(w.digits, p.seglen, p.bps, p.per_block, p.K, w.hist);
+    msm_colscan_kernel<<<blocks_for(G, 256), 256, 0, s>>>(hist, d_segs, K, G, counts);
     GB_CHECK_LAUNCH();
-    msm_colscan_kernel<<<blocks_for(p.G, 256), 256, 0, s>>>(w.hist, p.bps, p.K, p.G, w.counts);
-    GB_CHECK_LAUNCH();
-    msm_keyscan_kernel<<<1, 1024, 0, s>>>(w.counts, p.G, w.starts);
-    GB_CHECK_LAUNCH();
-    msm_scatter_kernel<<<nblocks, 1024, smem, s>>>(w.digits, p.n, p.seglen, p.bps, p.per_block, p.K,
-                                                   p.precomputed ? 1 : 0, w.hist, w.starts, w.sorted);
+    u32_exclusive_scan(counts, G, starts, s);
+    msm_scatter_kernel<<<nblocks, 1024, smem, s>>>(digits, d_segs, d_blks, K, precomputed ? stride : 0, hist,
+                                                   starts, sorted);
     GB_CHECK_LAUNCH();
     int tok = timed_begin(s);
-    if (p.acc_variant == 1) {
-        msm_accumulate_kernel<256, 2><<<blocks_for(nchunks, 256), 256, 0, s>>>(
-            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
-    } else if (p.acc_variant == 2) {
-        msm_accumulate_kernel<128, 3><<<blocks_for(nchunks, 128), 128, 0, s>>>(
-            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+    if (variant == 1) {
+        msm_accumulate_kernel<256, 2><<<(unsigned)((nchunks + 255) / 256), 256, 0, s>>>(
+            sorted, starts, G, L, nchunks, points, buckets, head, tail);
+    } else if (variant == 2) {
+        msm_accumulate_kernel<128, 3><<<(unsigned)((nchunks + 127) / 128), 128, 0, s>>>(
+            sorted, starts, G, L, nchunks, points, buckets, head, tail);
     } else {
-        msm_accumulate_kernel<256, 1><<<blocks_for(nchunks, 256), 256, 0, s>>>(
-            w.sorted, w.starts, p.G, p.L, nchunks, d_points, w.buckets, w.head, w.tail);
+        msm_accumulate_kernel<256, 1><<<(unsigned)((nchunks + 255) / 256), 256, 0, s>>>(
+            sorted, starts, G, L, nchunks, points, buckets, head, tail);
     }
     GB_CHECK_LAUNCH();
     timed_end(tok, s, GB_SLOT_MSM_ACCUMULATE);
-    msm_fixup_kernel<<<blocks_for(p.G, 128), 128, 0, s>>>(w.starts, p.G, p.L, w.head, w.tail, w.buckets);
+    msm_fixup_kernel<<<blocks_for(G, 128), 128, 0, s>>>(starts, G, L, head, tail, buckets);
     GB_CHECK_LAUNCH();
-    msm_reduce_partial_kernel<<<blocks_for((size_t)p.nseg * p.S, 128), 128, 0, s>>>(
-        w.buckets, p.K, p.S, p.nseg, w.partial);
+    msm_reduce_partial_kernel<<<blocks_for((size_t)nseg * S, 128), 128, 0, s>>>(buckets, K, S, nseg, partial);
     GB_CHECK_LAUNCH();
-    // tree-sum each segment's S partials down to one point
     {
-        const xyzz_t *src = w.partial;
-        uint32_t len = p.S;
+        // tree-sum each segment's S partials down to one point
+        const xyzz_t *src = partial;
+        uint32_t len = S;
         dev_buf<xyzz_t> tmp_a, tmp_b;
         bool use_a = true;
         while (len > 1) {
             uint32_t blocks = (len + 511) / 512;
             dev_buf<xyzz_t> &dst = use_a ? tmp_a : tmp_b;
-            dst = dev_buf<xyzz_t>((size_t)p.nseg * blocks, s);
-            xyzz_tree_sum_kernel<<<dim3(blocks, p.nseg), 256, 0, s>>>(src, len, dst);
+            dst = dev_buf<xyzz_t>((size_t)nseg * blocks, s);
+            xyzz_tree_sum_kernel<<<dim3(blocks, nseg), 256, 0, s>>>(src, len, dst);
             GB_CHECK_LAUNCH();
             src = dst;
             len = blocks;
             use_a = !use_a;
         }
-        GB_CUDA_OK(cudaMemcpyAsync(w.segsum, src, (size_t)p.nseg * sizeof(xyzz_t), cudaMemcpyDeviceToDevice, s));
+        GB_CUDA_OK(cudaMemcpyAsync(segsum, src, (size_t)nseg * sizeof(xyzz_t), cudaMemcpyDeviceToDevice, s));
     }
-    msm_combine_kernel<<<1, 32, 0, s>>>(w.segsum, p.nseg, p.c, d_out);
+    msm_combine_kernel<<<blocks_for(nitems, 32), 32, 0, s>>>(segsum, nitems, segs_per_item, c, d_out);
     GB_CHECK_LAUNCH();
     timed_end(tok_all, s, GB_SLOT_MSM_TOTAL);
 }
@@ -555,43 +640,67 @@ static int plan_window(size_t n, bool precomputed, uint32_t requested)
     return choose_window(n, precomputed);
 }
 
-// Plain MSM of host bases + host scalars (one call, nothing resident).
-static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *scalars, size_t n,
-                           size_t nmsms)
+// Plain MSMs of host bases + host scalars [nmsms][n] (nothing resident):
+// one batch through the engine.
+static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *scalars, size_t n, size_t nmsms)
 {
     cudaStream_t s = lane_stream();
     dev_buf<affine_t> d_points(n, s);
-    dev_buf<fr_t> d_scalars(n, s);
+    dev_buf<fr_t> d_scalars(n * nmsms, s);
     dev_buf<jacobian_t> d_out(std::max<size_t>(nmsms, 1), s);
     h2d(d_points, points, n * sizeof(affine_t), s);
-    msm_plan p = make_plan(n, plan_window(n, false, 0), false);
-    for (size_t m = 0; m < nmsms; m++) {
-        h2d(d_scalars, scalars + m * n, n * sizeof(fr_t), s);
-        msm_run(p, d_points, d_scalars, d_out.get() + m, s);
-    }
+    h2d(d_scalars, scalars, n * nmsms * sizeof(fr_t), s);
+    std::vector<msm_item> items;
+    for (size_t m = 0; m < nmsms; m++) items.push_back(msm_item{d_scalars.get() + m * n, n, 0});
+    msm_run_batch(items, choose_window(n, false), false, d_points, 0, d_out, s);
     d2h(out, d_out, nmsms * sizeof(jacobian_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    timed_collect();
 }
 
-static void context_run_device(msm_context_t *ctx, jacobian_t *out_host, const fr_t *d_scalars,
-                               size_t npoints, size_t nmsms, cudaStream_t s)
+// MSMs below this size skip the context's precomputed windows: a
+// precomputed MSM always pays for 2^(c-1) buckets (c = 16 at full size),
+// while a small plain MSM with its own small window pays far less.
+static constexpr size_t kPrecomputedMin = (size_t)1 << 13;
+
+// A batch against the context; results to the host.  Large items use the
+// precomputed table; small ones run as one plain batch over table row 0 (the
+// bases themselves) with a window sized for them.
+static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const std::vector<msm_item> &items,
+                              cudaStream_t s)
 {
-    dev_buf<jacobian_t> d_out(std::max<size_t>(nmsms, 1), s);
-    msm_plan p = make_plan(npoints, ctx->c, true);
-    // the table is laid out [window][ctx->npoints]; a shorter MSM over the
-    // first npoints bases needs the same per-window stride, so index through
-    // a plan whose point count is the context's and whose scalars beyond
-    // npoints are absent: run with n = npoints over a strided view.
-    if (npoints != ctx->npoints) {
-        // Use the plain (non-precomputed) engine over window 0 of the table.
-        msm_plan q = make_plan(npoints, plan_window(npoints, false, 0), false);
-        for (size_t m = 0; m < nmsms; m++) msm_run(q, ctx->table, d_scalars + m * npoints, d_out.get() + m, s);
-    } else {
-        for (size_t m = 0; m < nmsms; m++) msm_run(p, ctx->table, d_scalars + m * npoints, d_out.get() + m, s);
+    dev_buf<jacobian_t> d_out(std::max<size_t>(items.size(), 1), s);
+    std::vector<msm_item> big, small;
+    std::vector<size_t> big_idx, small_idx;
+    size_t small_max = 0;
+    for (size_t i = 0; i < items.size(); i++) {
+        if (items[i].n >= kPrecomputedMin || items.size() == 1) {
+            big.push_back(items[i]);
+            big_idx.push_back(i);
+        } else {
+            small.push_back(items[i]);
+            small_idx.push_back(i);
+            small_max = std::max(small_max, items[i].n);
+        }
     }
-    d2h(out_host, d_out, nmsms * sizeof(jacobian_t), s);
+    dev_buf<jacobian_t> d_big(std::max<size_t>(big.size(), 1), s), d_small(std::max<size_t>(small.size(), 1), s);
+    if (!big.empty()) msm_run_batch(big, ctx->c, true, ctx->table, ctx->npoints, d_big, s);
+    if (!small.empty()) msm_run_batch(small, choose_window(small_max, false), false, ctx->table, 0, d_small, s);
+    std::vector<jacobian_t> hb(big.size()), hs(small.size());
+    d2h(hb.data(), d_big, big.size() * sizeof(jacobian_t), s);
+    d2h(hs.data(), d_small, small.size() * sizeof(jacobian_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < big.size(); i++) out_host[big_idx[i]] = hb[i];
+    for (size_t i = 0; i < small.size(); i++) out_host[small_idx[i]] = hs[i];
     timed_collect();
+}
+
+static void context_run_device(msm_context_t *ctx, jacobian_t *out_host, const fr_t *d_scalars, size_t npoints,
+                               size_t nmsms, cudaStream_t s)
+{
+    std::vector<msm_item> items;
+    for (size_t m = 0; m < nmsms; m++) items.push_back(msm_item{d_scalars + m * npoints, npoints, 0});
+    context_run_items(ctx, out_host, items, s);
 }
 
 }  // namespace gb
@@ -745,19 +854,10 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_ragged(RawG1Projective
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaStream_t s = lane_stream();
     device_vec_wait(dv, s);
-    dev_buf<jacobian_t> d_out(count, s);
-    for (size_t i = 0; i < count; i++) {
-        const RawMsmSlice &sl = slices[i];
-        if (sl.point_offset == 0 && sl.len == ctx->npoints) {
-            msm_plan p = make_plan(sl.len, ctx->c, true);
-            msm_run(p, ctx->table, dv->values + sl.scalar_offset, d_out.get() + i, s);
-        } else {
-            msm_plan q = make_plan(sl.len, plan_window(sl.len, false, 0), false);
-            msm_run(q, ctx->table + sl.point_offset, dv->values + sl.scalar_offset, d_out.get() + i, s);
-        }
-    }
-    d2h(out, d_out, count * sizeof(jacobian_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    std::vector<msm_item> items;
+    for (size_t i = 0; i < count; i++)
+        items.push_back(msm_item{dv->values + slices[i].scalar_offset, slices[i].len, slices[i].point_offset});
+    context_run_items(ctx, out, items, s);
     return ok();
     GB_ENTRY_END
 }

@@ -171,3 +171,47 @@ def test_msm_2p20_linearity(gb, orc):
     plain = gb.bls12_381_g1_msm(b, t)
     assert (affine_of(orc, plain) == affine_of(orc, res[1])).all()
     ctx.close()
+
+
+def _mixed_scalars(orc, n, rng):
+    """70% uniform Fr, 20% uniform below 2^64, 10% zero (the batched configuration's mix)."""
+    s = orc.fr_random(n, rng)
+    u = rng.random(n)
+    small = (u >= 0.7) & (u < 0.9)
+    s[small] = orc.fr_from_ints([int(x) for x in rng.integers(0, 2**63, size=int(small.sum()), dtype=np.int64)])
+    s[u >= 0.9] = 0
+    return s
+
+
+def test_ragged_batch_uneven_sizes(gb, orc):
+    """One batched call over MSMs of uneven sizes, offsets and an empty slice,
+    each equal to its own oracle MSM."""
+    rng = np.random.default_rng(44)
+    N = 1 << 14
+    b = gb.g1_generator_mul(orc.fr_random(N, rng))
+    sizes = [1 << 10, 3000, 0, 1, 1 << 13, 777, N]
+    offs = [0, 100, 5, 9, 0, 2000, 0]
+    scal = [_mixed_scalars(orc, n, rng) for n in sizes]
+    flat = np.concatenate([x for x in scal if len(x)] + [np.zeros((1, 4), np.uint64)])
+    so, slices = 0, []
+    for n, po in zip(sizes, offs):
+        slices.append((so, po, n))
+        so += n
+    ctx = gb.Bls12_381G1MsmContext(b)
+    dv = gb.Bls12_381FrDeviceVec.upload(flat)
+    got = ctx.device_ragged(dv, slices)
+    for i, (n, po) in enumerate(zip(sizes, offs)):
+        want = affine_of(orc, orc.g1_msm(b[po:po + n], scal[i])) if n else np.zeros((1, 12), np.uint64)
+        assert (affine_of(orc, got[i]) == want).all(), i
+    ctx.close()
+
+
+def test_batch_plain_matches_single_calls(gb, orc):
+    rng = np.random.default_rng(45)
+    n = 2500
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    sb = np.stack([_mixed_scalars(orc, n, rng) for _ in range(5)])
+    got = gb.bls12_381_g1_msm_batch(b, sb)
+    for i in range(5):
+        assert (affine_of(orc, got[i]) == affine_of(orc, gb.bls12_381_g1_msm(b, sb[i]))).all()
+        assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all()
