@@ -248,6 +248,12 @@ GB_API RustError midnight_sppark_bls12_381_eval_graph_batch(
     RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, int32_t rot_scale, const RawGraph *graphs,
     size_t graph_count);
 
+/* ---- KZG opening helpers ---------------------------------------------------- */
+/* bls12_381_g1_msm.cu:3985-4031: out[p] = sum_i polys[p][i] * point^i for the
+ * poly_count resident polynomials of poly_len coefficients */
+GB_API RustError midnight_sppark_bls12_381_fr_device_eval_polys(RawFr *out, const void *device_vec, size_t poly_len,
+                                                                size_t poly_count, RawFr point);
+
 /* ---- device vectors --------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:2741-3442 */
 GB_API RustError midnight_sppark_bls12_381_fr_device_vec_upload(void **out, const RawFr *values, size_t len);
@@ -281,6 +287,11 @@ GB_API RustError gb_g1_generator_mul_device(RawG1Affine *d_out, const RawFr *d_s
  * output may be NULL).  Host buffers of 2^k affine points. */
 GB_API RustError gb_g1_to_lagrange(RawG1Affine *out, const RawG1Affine *g, uint32_t k);
 GB_API RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, RawFr tau, uint32_t k);
+/* Kate quotients (f(X) - f(point)) / (X - point) of poly_count resident
+ * polynomials (the division of the reference's multi-open kate scan,
+ * bls12_381_g1_msm.cu:1923-1959), into a new device vector */
+GB_API RustError gb_fr_device_kate_divide(void **out, const void *device_vec, size_t poly_len, size_t poly_count,
+                                          RawFr point);
 /* measured device throughput of 32x32->64 multiply-adds per second */
 GB_API RustError gb_imad_peak(double *out_per_sec);
 /* cumulative host<->device bytes moved by this library */

@@ -103,6 +103,95 @@ void prefix_product(fr_t *out, const fr_t *in, size_t n, cudaStream_t s)
     GB_CHECK_LAUNCH();
 }
 
+// ------------------------------------------------------------ additive suffix scan
+
+// out[i] = sum_{j >= i} in[j], by tiles of 2048 counted from the top end
+__global__ void __launch_bounds__(kScanThreads) sfx_tile_sum_kernel(const fr_t *__restrict__ in, size_t n,
+                                                                    fr_t *__restrict__ aux)
+{
+    __shared__ fr_t sh[kScanThreads];
+    // tile t covers reversed positions [t*2048, (t+1)*2048), element n-1-r
+    size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPer;
+    fr_t acc = fr_t::zero();
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++)
+        if (base + e < n) acc = acc + in[n - 1 - (base + e)];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (unsigned off = blockDim.x / 2; off; off >>= 1) {
+        if (threadIdx.x < off) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) aux[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kScanThreads) sfx_tile_apply_kernel(const fr_t *in, size_t n,
+                                                                      const fr_t *__restrict__ aux_incl, fr_t *out)
+{
+    __shared__ fr_t sh[kScanThreads];
+    size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPer;
+    fr_t v[kScanPer];
+    fr_t acc = fr_t::zero();
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++) {
+        v[e] = base + e < n ? in[n - 1 - (base + e)] : fr_t::zero();
+        acc = acc + v[e];
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (unsigned off = 1; off < blockDim.x; off <<= 1) {
+        fr_t other = threadIdx.x >= off ? sh[threadIdx.x - off] : fr_t::zero();
+        __syncthreads();
+        if (threadIdx.x >= off) sh[threadIdx.x] = sh[threadIdx.x] + other;
+        __syncthreads();
+    }
+    fr_t run = threadIdx.x ? sh[threadIdx.x - 1] : fr_t::zero();
+    if (blockIdx.x) run = run + aux_incl[blockIdx.x - 1];
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++) {
+        run = run + v[e];
+        if (base + e < n) out[n - 1 - (base + e)] = run;
+    }
+}
+
+// inclusive prefix sum of tile totals, in place (reuses the suffix machinery
+// on the reversed view of a reversed array: a plain forward scan)
+__global__ void __launch_bounds__(kScanThreads) fwd_sum_scan_small_kernel(fr_t *a, size_t n)
+{
+    // single block, n <= kScanTile * kScanTile handled by recursion on the host
+    __shared__ fr_t sh[kScanThreads];
+    const size_t per = (n + blockDim.x - 1) / blockDim.x;
+    const size_t lo = threadIdx.x * per, hi = min(lo + per, n);
+    fr_t acc = fr_t::zero();
+    for (size_t i = lo; i < hi; i++) acc = acc + a[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (unsigned off = 1; off < blockDim.x; off <<= 1) {
+        fr_t other = threadIdx.x >= off ? sh[threadIdx.x - off] : fr_t::zero();
+        __syncthreads();
+        if (threadIdx.x >= off) sh[threadIdx.x] = sh[threadIdx.x] + other;
+        __syncthreads();
+    }
+    fr_t run = threadIdx.x ? sh[threadIdx.x - 1] : fr_t::zero();
+    for (size_t i = lo; i < hi; i++) {
+        run = run + a[i];
+        a[i] = run;
+    }
+}
+
+void suffix_sum(fr_t *out, const fr_t *in, size_t n, cudaStream_t s)
+{
+    if (!n) return;
+    size_t tiles = (n + kScanTile - 1) / kScanTile;
+    dev_buf<fr_t> aux(tiles, s);
+    sfx_tile_sum_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, aux);
+    GB_CHECK_LAUNCH();
+    fwd_sum_scan_small_kernel<<<1, kScanThreads, 0, s>>>(aux, tiles);
+    GB_CHECK_LAUNCH();
+    sfx_tile_apply_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, aux, out);
+    GB_CHECK_LAUNCH();
+}
+
 // ------------------------------------------------------------ batch inversion
 
 // Montgomery's trick per tile: one Fermat inversion per tile of 2048

@@ -9,6 +9,8 @@ namespace gb {
 void prefix_product(fr_t *out, const fr_t *in, size_t n, cudaStream_t s);
 // out[i] = (mul ? mul[i] : 1) / in[i], zeros stay zero; out may alias in or mul
 void batch_invert(fr_t *out, const fr_t *in, size_t n, const fr_t *mul, cudaStream_t s);
+// out[i] = sum_{j >= i} in[j]; out may alias in
+void suffix_sum(fr_t *out, const fr_t *in, size_t n, cudaStream_t s);
 // d[i] = w^i for i < n
 void omega_powers(fr_t *d, const fr_t &w, size_t n, cudaStream_t s);
 

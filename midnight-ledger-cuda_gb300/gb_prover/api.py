@@ -22,7 +22,7 @@ __all__ = [
     "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "transfer_counters",
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
-    "bls12_381_eval_graph_batch",
+    "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -473,3 +473,18 @@ def bls12_381_eval_graph_batch(length, graphs, fixed=None, advice=None, instance
         f(beta), f(gamma), f(theta), f(trash_challenge), f(y), rot_scale, ctypes.cast(ga, ctypes.c_void_p),
         len(graphs)))
     return out
+
+
+# ---------------------------------------------------------------- opening helpers
+
+def bls12_381_fr_device_eval_polys(devvec, poly_len, poly_count, point):
+    out = np.zeros((poly_count, 4), dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_fr_device_eval_polys(_ptr(out), devvec.raw, poly_len, poly_count,
+                                                                _fr(point)))
+    return out
+
+
+def fr_device_kate_divide(devvec, poly_len, poly_count, point):
+    h = ctypes.c_void_p()
+    check(lib().gb_fr_device_kate_divide(ctypes.byref(h), devvec.raw, poly_len, poly_count, _fr(point)))
+    return Bls12_381FrDeviceVec(h)

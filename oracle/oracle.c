@@ -1239,6 +1239,33 @@ void orc_fr_sort_canonical(orc_fr *a, size_t len)
 /* Quotient numerator                                                        */
 /* ======================================================================== */
 
+
+/* eval_polynomial (vendor/midnight-proofs-0.8.1/src/utils/arithmetic.rs:53-77):
+ * Horner from the top coefficient */
+void orc_fr_eval_poly(orc_fr *out, const orc_fr *poly, size_t len, const orc_fr *point)
+{
+    INIT();
+    u64 acc[4] = {0, 0, 0, 0};
+    for (size_t i = len; i-- > 0;) {
+        f_mul(acc, acc, point->l, &FR);
+        f_add(acc, acc, poly[i].l, &FR);
+    }
+    memcpy(out->l, acc, sizeof acc);
+}
+
+/* kate_division (arithmetic.rs:97-116): q = (a - a(b)) / (X - b), len - 1
+ * coefficients: q[len-2] = a[len-1], q[i-1] = a[i] + b * q[i] */
+void orc_fr_kate_division(orc_fr *q, const orc_fr *a, size_t len, const orc_fr *b)
+{
+    INIT();
+    if (len < 2) return;
+    u64 tmp[4] = {0, 0, 0, 0};
+    for (size_t i = len - 1; i >= 1; i--) {
+        f_add(q[i - 1].l, a[i].l, tmp, &FR);
+        f_mul(tmp, q[i - 1].l, b->l, &FR);
+    }
+}
+
 /* get_rotation_idx (evaluation.rs:40-45) */
 static size_t rot_idx(size_t idx, int32_t rot, int32_t scale, size_t len)
 {

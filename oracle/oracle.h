@@ -131,6 +131,10 @@ int orc_fr_quotient_pieces(orc_fr *out, const orc_fr *quotient, size_t quotient_
                            size_t poly_len, size_t piece_count, const orc_fr *blinds,
                            size_t blind_count);
 void orc_fr_sort_canonical(orc_fr *a, size_t len);
+/* eval_polynomial (arithmetic.rs:53-77): sum_i poly[i] * point^i */
+void orc_fr_eval_poly(orc_fr *out, const orc_fr *poly, size_t len, const orc_fr *point);
+/* kate_division (arithmetic.rs:97-116): len - 1 quotient coefficients */
+void orc_fr_kate_division(orc_fr *q, const orc_fr *a, size_t len, const orc_fr *b);
 
 /* ---- quotient numerator ------------------------------------------------- */
 /* Same memory layout as the C ABI's RawValueSource / RawCalculation /

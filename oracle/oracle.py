@@ -86,6 +86,8 @@ def _declare(L):
         "orc_fr_poly_lincomb": (None, [vp, vp, sz, sz, vp]),
         "orc_fr_quotient_pieces": (i32, [vp, vp, sz, sz, sz, vp, sz]),
         "orc_fr_sort_canonical": (None, [vp, sz]),
+        "orc_fr_eval_poly": (None, [vp, vp, sz, vp]),
+        "orc_fr_kate_division": (None, [vp, vp, sz, vp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -415,6 +417,21 @@ def fr_sort_canonical(a):
     a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
     lib().orc_fr_sort_canonical(_p(a), len(a))
     return a
+
+
+def fr_eval_poly(poly, point):
+    a = np.ascontiguousarray(poly, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros(4, dtype=np.uint64)
+    lib().orc_fr_eval_poly(_p(o), _p(a), len(a), _p(np.ascontiguousarray(point, dtype=np.uint64)))
+    return o
+
+
+def fr_kate_division(poly, point):
+    """(a - a(point)) / (X - point): len(a) - 1 coefficients."""
+    a = np.ascontiguousarray(poly, dtype=np.uint64).reshape(-1, 4)
+    q = np.zeros((max(len(a) - 1, 0), 4), dtype=np.uint64)
+    lib().orc_fr_kate_division(_p(q), _p(a), len(a), _p(np.ascontiguousarray(point, dtype=np.uint64)))
+    return q
 
 
 # ---------------------------------------------------------------- quotient numerator

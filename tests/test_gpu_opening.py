@@ -1,0 +1,45 @@
+"""KZG opening helpers on the GPU through the C ABI, bit-exact against the
+oracle's eval_polynomial and kate_division (arithmetic.rs:53-116)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("ln,count", [(1, 1), (7, 3), (2048, 2), (8193, 1), (1 << 16, 4)])
+def test_eval_polys(gb, orc, ln, count):
+    rng = np.random.default_rng(ln + count)
+    polys = orc.fr_random(ln * count, rng)
+    z = orc.fr_random(1, rng)[0]
+    dv = gb.Bls12_381FrDeviceVec.upload(polys)
+    got = gb.bls12_381_fr_device_eval_polys(dv, ln, count, z)
+    for p in range(count):
+        assert (got[p] == orc.fr_eval_poly(polys[p * ln:(p + 1) * ln], z)).all()
+    dv.free()
+
+
+def test_eval_polys_shape_errors(gb, orc):
+    dv = gb.Bls12_381FrDeviceVec.upload(orc.fr_random(10, np.random.default_rng(0)))
+    z = orc.fr_from_ints([3])[0]
+    with pytest.raises(gb.MsmError):
+        gb.bls12_381_fr_device_eval_polys(dv, 3, 3, z)
+    with pytest.raises(gb.MsmError):
+        gb.bls12_381_fr_device_eval_polys(dv, 0, 1, z)
+    dv.free()
+
+
+@pytest.mark.parametrize("ln,count,zero", [(2, 1, False), (100, 3, False), (4097, 2, False),
+                                           (1 << 17, 1, False), (300, 2, True)])
+def test_kate_divide(gb, orc, ln, count, zero):
+    rng = np.random.default_rng(ln * 3 + count)
+    polys = orc.fr_random(ln * count, rng)
+    z = orc.fr_from_ints([0])[0] if zero else orc.fr_random(1, rng)[0]
+    dv = gb.Bls12_381FrDeviceVec.upload(polys)
+    q = gb.fr_device_kate_divide(dv, ln, count, z)
+    got = q.download().reshape(count, ln, 4)
+    for p in range(count):
+        want = orc.fr_kate_division(polys[p * ln:(p + 1) * ln], z)
+        assert (got[p, :ln - 1] == want).all()
+        assert (got[p, ln - 1] == 0).all()
+    q.free()
+    dv.free()

@@ -244,3 +244,23 @@ def test_batch_invert_and_sort(orc):
     rng = np.random.default_rng(4)
     a = orc.fr_random(300, rng)
     assert orc.fr_to_ints(orc.fr_sort_canonical(a)) == sorted(orc.fr_to_ints(a))
+
+
+def test_eval_and_kate_division(orc):
+    """eval_polynomial and kate_division (arithmetic.rs:53-116) against
+    integer arithmetic: q (X - z) + a(z) == a, including z = 0 and len 1."""
+    rng = np.random.default_rng(11)
+    for ln, zv in ((50, None), (33, 0), (1, None), (2, 5)):
+        a = orc.fr_random(ln, rng)
+        z = orc.fr_random(1, rng)[0] if zv is None else orc.fr_from_ints([zv])[0]
+        ai, zi = orc.fr_to_ints(a), orc.fr_to_ints(z[None])[0]
+        ev = sum(c * pow(zi, i, R) for i, c in enumerate(ai)) % R
+        assert orc.fr_to_ints(orc.fr_eval_poly(a, z)[None])[0] == ev
+        q = orc.fr_to_ints(orc.fr_kate_division(a, z))
+        assert len(q) == ln - 1
+        back = [0] * ln
+        for i, c in enumerate(q):
+            back[i + 1] = (back[i + 1] + c) % R
+            back[i] = (back[i] - c * zi) % R
+        back[0] = (back[0] + ev) % R
+        assert back == ai
