@@ -1,0 +1,171 @@
+"""Seeded randomness for the prover's blinding values and synthetic circuits.
+
+`ChaCha20Rng` restates rand_chacha's ChaCha20Rng (rand_chacha 0.3.1, the
+`ChaCha20Rng` of vendor/midnight-proofs-0.8.1/src/plonk/vanishing/prover.rs:41-75
+and the `StdRng` family): the 20-round ChaCha block function of RFC 8439
+with a 64-bit block counter in words 12-13 and a 64-bit stream id (0) in
+words 14-15, output words consumed in order, `next_u64` = low word | high
+word << 32.  `seed_from_u64` is rand_core 0.6's PCG32 seed expansion.
+
+`fr_random` is `Fq::random` (vendor/midnight-curves-0.3.1/src/bls12_381/fq.rs:373-387):
+four u64 draws, the top bit masked, rejected when >= r, stored in
+Montgomery form.
+"""
+import hashlib
+
+import numpy as np
+
+R_MOD = 0x73eda753299d7d483339d80809a1d80553bda402fffe5bfeffffffff00000001
+_MASK64 = (1 << 64) - 1
+_SIGMA = np.array([0x61707865, 0x3320646E, 0x79622D32, 0x6B206574], dtype=np.uint32)
+
+
+def _rotl(x, n):
+    return (x << np.uint32(n)) | (x >> np.uint32(32 - n))
+
+
+def _chacha_blocks(key_words, counter0, nblocks, stream=0):
+    """nblocks consecutive 64-byte ChaCha20 blocks as an (nblocks, 16) u32 array."""
+    ctr = np.arange(counter0, counter0 + nblocks, dtype=np.uint64)
+    st = np.empty((16, nblocks), dtype=np.uint32)
+    st[0:4] = _SIGMA[:, None]
+    st[4:12] = np.asarray(key_words, dtype=np.uint32)[:, None]
+    st[12] = (ctr & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    st[13] = (ctr >> np.uint64(32)).astype(np.uint32)
+    st[14] = np.uint32(stream & 0xFFFFFFFF)
+    st[15] = np.uint32(stream >> 32)
+    x = [st[i].copy() for i in range(16)]
+
+    def qr(a, b, c, d):
+        x[a] += x[b]; x[d] ^= x[a]; x[d] = _rotl(x[d], 16)
+        x[c] += x[d]; x[b] ^= x[c]; x[b] = _rotl(x[b], 12)
+        x[a] += x[b]; x[d] ^= x[a]; x[d] = _rotl(x[d], 8)
+        x[c] += x[d]; x[b] ^= x[c]; x[b] = _rotl(x[b], 7)
+
+    with np.errstate(over="ignore"):
+        for _ in range(10):
+            qr(0, 4, 8, 12); qr(1, 5, 9, 13); qr(2, 6, 10, 14); qr(3, 7, 11, 15)
+            qr(0, 5, 10, 15); qr(1, 6, 11, 12); qr(2, 7, 8, 13); qr(3, 4, 9, 14)
+        out = np.stack([x[i] + st[i] for i in range(16)], axis=1)
+    return out
+
+
+class ChaCha20Rng:
+    def __init__(self, seed: bytes):
+        if len(seed) != 32:
+            raise ValueError("ChaCha20Rng seed must be 32 bytes")
+        self._key = np.frombuffer(seed, dtype="<u4").astype(np.uint32)
+        self._block = 0
+        self._buf = np.zeros(0, dtype=np.uint32)
+        self._pos = 0
+
+    @classmethod
+    def seed_from_u64(cls, state: int):
+        """rand_core SeedableRng::seed_from_u64: PCG32 fills the 32-byte seed."""
+        mul, inc = 6364136223846793005, 11634580027462260723
+        out = bytearray()
+        state &= _MASK64
+        for _ in range(8):
+            state = (state * mul + inc) & _MASK64
+            xorshifted = (((state >> 18) ^ state) >> 27) & 0xFFFFFFFF
+            rot = state >> 59
+            v = ((xorshifted >> rot) | (xorshifted << ((32 - rot) & 31))) & 0xFFFFFFFF
+            out += v.to_bytes(4, "little")
+        return cls(bytes(out))
+
+    @classmethod
+    def from_label(cls, label: str):
+        """Seed = SHA-256 of a workload label."""
+        return cls(hashlib.sha256(label.encode()).digest())
+
+    def _words(self, count):
+        """The next `count` keystream words, in order."""
+        have = len(self._buf) - self._pos
+        if have < count:
+            need = count - have
+            nblocks = (need + 15) // 16
+            fresh = _chacha_blocks(self._key, self._block, nblocks).reshape(-1)
+            self._block += nblocks
+            self._buf = np.concatenate([self._buf[self._pos:], fresh])
+            self._pos = 0
+        w = self._buf[self._pos:self._pos + count]
+        self._pos += count
+        return w
+
+    def next_u32(self):
+        return int(self._words(1)[0])
+
+    def next_u64_array(self, count):
+        w = self._words(2 * count).astype(np.uint64).reshape(-1, 2)
+        return w[:, 0] | (w[:, 1] << np.uint64(32))
+
+    def next_u64(self):
+        return int(self.next_u64_array(1)[0])
+
+    def fill_bytes(self, n):
+        nw = (n + 3) // 4
+        return self._words(nw).astype("<u4").tobytes()[:n]
+
+
+_R_LIMBS = np.array([(R_MOD >> (64 * i)) & _MASK64 for i in range(4)], dtype=np.uint64)
+_R2 = pow(2, 512, R_MOD)
+
+
+def _below_r(raw):
+    """rows of 4 little-endian u64 limbs that are < r"""
+    lt = np.zeros(len(raw), dtype=bool)
+    eq = np.ones(len(raw), dtype=bool)
+    for i in (3, 2, 1, 0):
+        lt |= eq & (raw[:, i] < _R_LIMBS[i])
+        eq &= raw[:, i] == _R_LIMBS[i]
+    return lt
+
+
+def ints_to_mont(vals):
+    """canonical integers -> (n, 4) u64 Montgomery limbs (R = 2^256)"""
+    out = np.empty((len(vals), 4), dtype=np.uint64)
+    for i, v in enumerate(vals):
+        m = (int(v) << 256) % R_MOD
+        out[i] = (m & _MASK64, (m >> 64) & _MASK64, (m >> 128) & _MASK64, m >> 192)
+    return out
+
+
+def mont_to_ints(arr):
+    """(n, 4) u64 Montgomery limbs -> canonical integers"""
+    arr = np.asarray(arr, dtype=np.uint64).reshape(-1, 4)
+    rinv = pow(1 << 256, -1, R_MOD)
+    out = []
+    for row in arr:
+        v = int(row[0]) | int(row[1]) << 64 | int(row[2]) << 128 | int(row[3]) << 192
+        out.append(v * rinv % R_MOD)
+    return out
+
+
+def raw_to_mont(raw):
+    """canonical limb rows (< r) -> Montgomery rows"""
+    vals = [int(r[0]) | int(r[1]) << 64 | int(r[2]) << 128 | int(r[3]) << 192 for r in raw]
+    return ints_to_mont(vals)
+
+
+def fr_random(rng: ChaCha20Rng, n):
+    """n field elements by Fq::random's rejection rule, Montgomery form (n, 4)."""
+    got = []
+    total = 0
+    while total < n:
+        want = n - total
+        draw = want + want // 8 + 8
+        raw = rng.next_u64_array(4 * draw).reshape(-1, 4)
+        raw[:, 3] &= np.uint64(0x7FFFFFFFFFFFFFFF)
+        ok = _below_r(raw)
+        # accept in draw order; once `want` are accepted, give the unused
+        # draws back so the stream matches one-at-a-time sampling
+        idx = np.flatnonzero(ok)
+        if len(idx) >= want:
+            last = idx[want - 1]
+            unused = draw - (last + 1)
+            rng._pos -= int(unused) * 8
+            idx = idx[:want]
+        got.append(raw[idx])
+        total += len(idx)
+    raw = np.concatenate(got) if got else np.zeros((0, 4), np.uint64)
+    return raw_to_mont(raw)
