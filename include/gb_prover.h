@@ -248,6 +248,37 @@ GB_API RustError midnight_sppark_bls12_381_eval_graph_batch(
     RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, int32_t rot_scale, const RawGraph *graphs,
     size_t graph_count);
 
+/* ---- resident forms of the argument and quotient entry points ---------------- */
+/* midnight_sppark_bls12_381_fr_permutation_products over device vectors
+ * (the resident trace path of .cu:4342-4449, prover.rs:216-262) */
+GB_API RustError gb_fr_permutation_products_device(void **out, const void *columns_vec,
+                                                   const void *permutations_vec, size_t len, size_t column_count,
+                                                   size_t chunk_len, RawFr beta, RawFr gamma, RawFr omega,
+                                                   const RawFr *delta_powers, const RawFr *blind_values,
+                                                   size_t blinding_factors);
+/* midnight_sppark_bls12_381_eval_graph_batch over device vectors, into a new
+ * device vector [graph_count][len] (the resident lookup compression of
+ * lookup/prover.rs:556-590) */
+GB_API RustError gb_eval_graph_batch_device(void **out, size_t len, const void *fixed_vec, size_t fixed_cols,
+                                            const void *advice_vec, size_t advice_cols, const void *instance_vec,
+                                            size_t instance_cols, const RawFr *challenges, size_t challenge_len,
+                                            RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y,
+                                            int32_t rot_scale, const RawGraph *graphs, size_t graph_count);
+/* midnight_sppark_bls12_381_eval_numerator over device vectors (the numerator
+ * context of .cu:5968-6162): lagrange_vec = l0 | l_last | l_active (3 x len),
+ * lookup_permuted_vec = per lookup its permuted input then permuted table
+ * coset; out = a new device vector of len rows */
+GB_API RustError gb_eval_numerator_device(
+    void **out, size_t len, const void *initial_vec, uint32_t run_custom, const void *fixed_vec, size_t fixed_cols,
+    const void *advice_vec, size_t advice_cols, const void *instance_vec, size_t instance_cols,
+    const RawFr *challenges, size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge,
+    RawFr y, RawFr omega, RawFr delta_start, RawFr delta_const, int32_t rot_scale, int32_t last_rotation,
+    uint32_t chunk_len, const void *lagrange_vec, const void *permutation_products_vec, size_t permutation_sets,
+    const RawColumnRef *permutation_columns, size_t permutation_columns_len, const void *permutation_pk_vec,
+    size_t permutation_pk_cosets_len, const void *lookup_products_vec, const void *lookup_permuted_vec,
+    size_t lookup_count, const void *trash_vec, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs);
+
 /* ---- KZG opening helpers ---------------------------------------------------- */
 /* bls12_381_g1_msm.cu:3985-4031: out[p] = sum_i polys[p][i] * point^i for the
  * poly_count resident polynomials of poly_len coefficients */

@@ -55,6 +55,7 @@ struct num_params {
     const fr_t *l0, *l_last, *l_active;
     size_t lookup_count;
     const fr_t *lk_product, *lk_input, *lk_table;
+    size_t lk_stride;  // distance between consecutive lookups' input (and table) columns
     const dgraph *lookup_graphs;
     size_t trash_count;
     const fr_t *trash_cosets;
@@ -217,8 +218,8 @@ __global__ void numerator_kernel(num_params p)
         const size_t r_next = rot_index(idx, 1, p.rot_scale, len);
         const size_t r_prev = rot_index(idx, -1, p.rot_scale, len);
         const fr_t *prod = p.lk_product + n * len;
-        const fr_t *pin = p.lk_input + n * len;
-        const fr_t *ptab = p.lk_table + n * len;
+        const fr_t *pin = p.lk_input + n * p.lk_stride;
+        const fr_t *ptab = p.lk_table + n * p.lk_stride;
         const fr_t table_value = evaluate_graph<MAX>(p.lookup_graphs[n], p, idx, zero);
         const fr_t a_minus_s = pin[idx] - ptab[idx];
         const fr_t l0 = p.l0[idx], l_active = p.l_active[idx];
@@ -307,6 +308,154 @@ static dev_buf<fr_t> upload_fr(const RawFr *h, size_t n, cudaStream_t s)
     return d;
 }
 
+
+// graph_count graphs over device columns into d_out [graph_count][len];
+// challenges are a host array
+static void graph_batch_core(fr_t *d_out, size_t len, const fr_t *fixed, size_t fixed_cols, const fr_t *advice,
+                             size_t advice_cols, const fr_t *instance, size_t instance_cols, const RawFr *challenges,
+                             size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge,
+                             RawFr y, int32_t rot_scale, const RawGraph *graphs, size_t graph_count, cudaStream_t s)
+{
+    num_params p{};
+    p.len = len;
+    p.rot_scale = rot_scale;
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    p.fixed = fixed;
+    p.fixed_cols = fixed_cols;
+    p.advice = advice;
+    p.advice_cols = advice_cols;
+    p.instance = instance;
+    p.instance_cols = instance_cols;
+    p.challenges = d_chal;
+    p.challenge_len = challenge_len;
+    p.beta = from_raw(beta);
+    p.gamma = from_raw(gamma);
+    p.theta = from_raw(theta);
+    p.trash = from_raw(trash_challenge);
+    p.y = from_raw(y);
+    std::vector<graph_upload> up(graph_count);
+    const unsigned grid = blocks_for(len, 128);
+    for (size_t gi = 0; gi < graph_count; gi++) {
+        upload_graph(up[gi], graphs[gi], s);
+        p.custom = up[gi].g;
+        fr_t *o = d_out + gi * len;
+        launch_by_capacity(
+            capacity_for(graphs[gi].num_intermediates), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
+        GB_CHECK_LAUNCH();
+    }
+}
+
+// Device pointers of one numerator evaluation; graphs still in host memory.
+struct numerator_inputs {
+    size_t len;
+    const fr_t *fixed, *advice, *instance, *challenges, *initial;
+    size_t fixed_cols, advice_cols, instance_cols, challenge_len;
+    const fr_t *l0, *l_last, *l_active;
+    const fr_t *perm_products, *perm_pk;
+    size_t perm_sets;
+    const RawColumnRef *perm_columns;  // host
+    size_t perm_columns_len, perm_pk_len;
+    const fr_t *lk_product, *lk_input, *lk_table;
+    size_t lk_stride, lookup_count;
+    const fr_t *trash_cosets;
+    const uint32_t *trash_sel;  // host
+    size_t trash_count;
+    uint32_t run_custom;
+    const RawGraph *custom_graph, *lookup_graphs, *trash_graphs;  // host
+};
+
+static void numerator_core(fr_t *d_out, const numerator_inputs &in, RawFr beta, RawFr gamma, RawFr theta,
+                           RawFr trash_challenge, RawFr y, RawFr omega, RawFr delta_start, RawFr delta_const,
+                           int32_t rot_scale, int32_t last_rotation, uint32_t chunk_len, cudaStream_t s)
+{
+    const size_t len = in.len;
+    num_params p{};
+    p.out = d_out;
+    p.len = len;
+    p.rot_scale = rot_scale;
+    p.fixed = in.fixed;
+    p.fixed_cols = in.fixed_cols;
+    p.advice = in.advice;
+    p.advice_cols = in.advice_cols;
+    p.instance = in.instance;
+    p.instance_cols = in.instance_cols;
+    p.challenges = in.challenges;
+    p.challenge_len = in.challenge_len;
+    p.beta = from_raw(beta);
+    p.gamma = from_raw(gamma);
+    p.theta = from_raw(theta);
+    p.trash = from_raw(trash_challenge);
+    p.y = from_raw(y);
+    p.run_custom = in.run_custom ? 1 : 0;
+    p.initial = in.initial;
+    uint32_t max_inter = in.run_custom ? in.custom_graph->num_intermediates : 0;
+    graph_upload custom;
+    if (in.run_custom) upload_graph(custom, *in.custom_graph, s);
+    p.custom = custom.g;
+    p.l0 = in.l0;
+    p.l_last = in.l_last;
+    p.l_active = in.l_active;
+    dev_buf<RawColumnRef> d_pcols(in.perm_columns_len, s);
+    h2d(d_pcols, in.perm_columns, in.perm_columns_len * sizeof(RawColumnRef), s);
+    dev_buf<fr_t> d_omega(in.perm_sets ? len : 0, s);
+    if (in.perm_sets) omega_powers(d_omega, from_raw(omega), len, s);
+    p.perm_sets = in.perm_sets;
+    p.perm_products = in.perm_products;
+    p.perm_columns = d_pcols;
+    p.perm_columns_len = in.perm_columns_len;
+    p.perm_pk_cosets = in.perm_pk;
+    p.omega_powers = d_omega;
+    p.delta_start = from_raw(delta_start);
+    p.delta_const = from_raw(delta_const);
+    p.last_rotation = last_rotation;
+    p.chunk_len = chunk_len;
+    std::vector<graph_upload> lk(in.lookup_count), tr(in.trash_count);
+    std::vector<dgraph> lkg(in.lookup_count), trg(in.trash_count);
+    for (size_t i = 0; i < in.lookup_count; i++) {
+        upload_graph(lk[i], in.lookup_graphs[i], s);
+        lkg[i] = lk[i].g;
+        max_inter = std::max(max_inter, in.lookup_graphs[i].num_intermediates);
+    }
+    for (size_t i = 0; i < in.trash_count; i++) {
+        upload_graph(tr[i], in.trash_graphs[i], s);
+        trg[i] = tr[i].g;
+        max_inter = std::max(max_inter, in.trash_graphs[i].num_intermediates);
+    }
+    dev_buf<dgraph> d_lkg(in.lookup_count, s), d_trg(in.trash_count, s);
+    h2d(d_lkg, lkg.data(), in.lookup_count * sizeof(dgraph), s);
+    h2d(d_trg, trg.data(), in.trash_count * sizeof(dgraph), s);
+    p.lookup_count = in.lookup_count;
+    p.lk_product = in.lk_product;
+    p.lk_input = in.lk_input;
+    p.lk_table = in.lk_table;
+    p.lk_stride = in.lk_stride;
+    p.lookup_graphs = d_lkg;
+    dev_buf<uint32_t> d_tsel(in.trash_count, s);
+    h2d(d_tsel, in.trash_sel, in.trash_count * sizeof(uint32_t), s);
+    p.trash_count = in.trash_count;
+    p.trash_cosets = in.trash_cosets;
+    p.trash_sel = d_tsel;
+    p.trash_graphs = d_trg;
+    const unsigned grid = blocks_for(len, 128);
+    launch_by_capacity(
+        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
+        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
+    GB_CHECK_LAUNCH();
+    // the graph and column-reference buffers are released in stream order
+    // after the launch; the caller's stream keeps the kernel ahead of them
+}
+
+static const fr_t *vec_values(const void *v, size_t need, const char *what)
+{
+    if (!need) return nullptr;
+    if (!v) throw cuda_error((int)cudaErrorInvalidValue, what);
+    auto *dv = reinterpret_cast<const fr_device_vec *>(v);
+    if (dv->len < need) throw cuda_error((int)cudaErrorInvalidValue, what);
+    return dv->values;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -334,102 +483,138 @@ RustError midnight_sppark_bls12_381_eval_numerator(
         (permutation_sets && (!permutation_products || !l0 || !l_last || !l_active)) ||
         (lookup_count && (!l0 || !l_last || !l_active)))
         return make_error((int)cudaErrorInvalidValue, "invalid numerator arguments");
+    if (permutation_sets && permutation_pk_cosets_len < permutation_columns_len)
+        return make_error((int)cudaErrorInvalidValue, "fewer permutation cosets than permutation columns");
     GB_ENTRY_BEGIN
     cudaStream_t s = lane_stream();
-    num_params p{};
-    p.len = len;
-    p.rot_scale = rot_scale;
     dev_buf<fr_t> d_out(len, s);
-    p.out = d_out;
     auto d_fixed = upload_fr(fixed, fixed_cols * len, s);
     auto d_advice = upload_fr(advice, advice_cols * len, s);
     auto d_instance = upload_fr(instance, instance_cols * len, s);
     auto d_chal = upload_fr(challenges, challenge_len, s);
-    p.fixed = d_fixed;
-    p.fixed_cols = fixed_cols;
-    p.advice = d_advice;
-    p.advice_cols = advice_cols;
-    p.instance = d_instance;
-    p.instance_cols = instance_cols;
-    p.challenges = d_chal;
-    p.challenge_len = challenge_len;
-    p.beta = from_raw(beta);
-    p.gamma = from_raw(gamma);
-    p.theta = from_raw(theta);
-    p.trash = from_raw(trash_challenge);
-    p.y = from_raw(y);
-    p.run_custom = run_custom ? 1 : 0;
     dev_buf<fr_t> d_init;
-    if (!run_custom) {
-        d_init = upload_fr(initial_out, len, s);
-        p.initial = d_init;
-    }
-    uint32_t max_inter = run_custom ? custom_graph.num_intermediates : 0;
-    graph_upload custom;
-    if (run_custom) upload_graph(custom, custom_graph, s);
-    p.custom = custom.g;
+    if (!run_custom) d_init = upload_fr(initial_out, len, s);
     const bool lagrange = permutation_sets || lookup_count;
     auto d_l0 = upload_fr(l0, lagrange ? len : 0, s);
     auto d_llast = upload_fr(l_last, lagrange ? len : 0, s);
     auto d_lact = upload_fr(l_active, lagrange ? len : 0, s);
-    p.l0 = d_l0;
-    p.l_last = d_llast;
-    p.l_active = d_lact;
     auto d_pprod = upload_fr(permutation_products, permutation_sets * len, s);
-    dev_buf<RawColumnRef> d_pcols(permutation_columns_len, s);
-    h2d(d_pcols, permutation_columns, permutation_columns_len * sizeof(RawColumnRef), s);
     auto d_pk = upload_fr(permutation_pk_cosets, permutation_pk_cosets_len * len, s);
-    dev_buf<fr_t> d_omega(permutation_sets ? len : 0, s);
-    if (permutation_sets) omega_powers(d_omega, from_raw(omega), len, s);
-    p.perm_sets = permutation_sets;
-    p.perm_products = d_pprod;
-    p.perm_columns = d_pcols;
-    p.perm_columns_len = permutation_columns_len;
-    p.perm_pk_cosets = d_pk;
-    p.omega_powers = d_omega;
-    p.delta_start = from_raw(delta_start);
-    p.delta_const = from_raw(delta_const);
-    p.last_rotation = last_rotation;
-    p.chunk_len = chunk_len;
-    if (permutation_sets && permutation_pk_cosets_len < permutation_columns_len)
-        return make_error((int)cudaErrorInvalidValue, "fewer permutation cosets than permutation columns");
     auto d_lprod = upload_fr(lookup_product_cosets, lookup_count * len, s);
     auto d_lin = upload_fr(lookup_input_cosets, lookup_count * len, s);
     auto d_ltab = upload_fr(lookup_table_cosets, lookup_count * len, s);
-    std::vector<graph_upload> lk(lookup_count), tr(trash_count);
-    std::vector<dgraph> lkg(lookup_count), trg(trash_count);
-    for (size_t i = 0; i < lookup_count; i++) {
-        upload_graph(lk[i], lookup_graphs[i], s);
-        lkg[i] = lk[i].g;
-        max_inter = std::max(max_inter, lookup_graphs[i].num_intermediates);
-    }
-    for (size_t i = 0; i < trash_count; i++) {
-        upload_graph(tr[i], trash_graphs[i], s);
-        trg[i] = tr[i].g;
-        max_inter = std::max(max_inter, trash_graphs[i].num_intermediates);
-    }
-    dev_buf<dgraph> d_lkg(lookup_count, s), d_trg(trash_count, s);
-    h2d(d_lkg, lkg.data(), lookup_count * sizeof(dgraph), s);
-    h2d(d_trg, trg.data(), trash_count * sizeof(dgraph), s);
-    p.lookup_count = lookup_count;
-    p.lk_product = d_lprod;
-    p.lk_input = d_lin;
-    p.lk_table = d_ltab;
-    p.lookup_graphs = d_lkg;
     auto d_trash = upload_fr(trash_cosets, trash_count * len, s);
-    dev_buf<uint32_t> d_tsel(trash_count, s);
-    h2d(d_tsel, trash_selector_fixed_indices, trash_count * sizeof(uint32_t), s);
-    p.trash_count = trash_count;
-    p.trash_cosets = d_trash;
-    p.trash_sel = d_tsel;
-    p.trash_graphs = d_trg;
-    const unsigned grid = blocks_for(len, 128);
-    launch_by_capacity(
-        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
-        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
-    GB_CHECK_LAUNCH();
+    numerator_inputs in{};
+    in.len = len;
+    in.fixed = d_fixed;
+    in.fixed_cols = fixed_cols;
+    in.advice = d_advice;
+    in.advice_cols = advice_cols;
+    in.instance = d_instance;
+    in.instance_cols = instance_cols;
+    in.challenges = d_chal;
+    in.challenge_len = challenge_len;
+    in.initial = d_init;
+    in.run_custom = run_custom;
+    in.l0 = d_l0;
+    in.l_last = d_llast;
+    in.l_active = d_lact;
+    in.perm_products = d_pprod;
+    in.perm_sets = permutation_sets;
+    in.perm_columns = permutation_columns;
+    in.perm_columns_len = permutation_columns_len;
+    in.perm_pk = d_pk;
+    in.perm_pk_len = permutation_pk_cosets_len;
+    in.lk_product = d_lprod;
+    in.lk_input = d_lin;
+    in.lk_table = d_ltab;
+    in.lk_stride = len;
+    in.lookup_count = lookup_count;
+    in.trash_cosets = d_trash;
+    in.trash_sel = trash_selector_fixed_indices;
+    in.trash_count = trash_count;
+    in.custom_graph = &custom_graph;
+    in.lookup_graphs = lookup_graphs;
+    in.trash_graphs = trash_graphs;
+    numerator_core(d_out, in, beta, gamma, theta, trash_challenge, y, omega, delta_start, delta_const, rot_scale,
+                   last_rotation, chunk_len, s);
     d2h(out_raw, d_out, len * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+// The numerator over resident columns, into a new device vector of len rows.
+RustError gb_eval_numerator_device(
+    void **out, size_t len, const void *initial_vec, uint32_t run_custom, const void *fixed_vec, size_t fixed_cols,
+    const void *advice_vec, size_t advice_cols, const void *instance_vec, size_t instance_cols,
+    const RawFr *challenges, size_t challenge_len, RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge,
+    RawFr y, RawFr omega, RawFr delta_start, RawFr delta_const, int32_t rot_scale, int32_t last_rotation,
+    uint32_t chunk_len, const void *lagrange_vec, const void *permutation_products_vec, size_t permutation_sets,
+    const RawColumnRef *permutation_columns, size_t permutation_columns_len, const void *permutation_pk_vec,
+    size_t permutation_pk_cosets_len, const void *lookup_products_vec, const void *lookup_permuted_vec,
+    size_t lookup_count, const void *trash_vec, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs)
+{
+    if (!out) return make_error((int)cudaErrorInvalidValue, "null numerator output");
+    *out = nullptr;
+    if (len == 0) return make_error((int)cudaErrorInvalidValue, "empty numerator domain");
+    if ((lookup_count && !lookup_graphs) || (trash_count && (!trash_graphs || !trash_selector_fixed_indices)) ||
+        (permutation_columns_len && !permutation_columns) || (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid resident numerator arguments");
+    if (permutation_sets && permutation_pk_cosets_len < permutation_columns_len)
+        return make_error((int)cudaErrorInvalidValue, "fewer permutation cosets than permutation columns");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    for (const void *v : {initial_vec, fixed_vec, advice_vec, instance_vec, lagrange_vec, permutation_products_vec,
+                          permutation_pk_vec, lookup_products_vec, lookup_permuted_vec, trash_vec})
+        if (v) device_vec_wait(reinterpret_cast<const fr_device_vec *>(v), s);
+    const bool lagrange = permutation_sets || lookup_count;
+    numerator_inputs in{};
+    in.len = len;
+    in.run_custom = run_custom;
+    in.initial = run_custom ? nullptr : vec_values(initial_vec, len, "initial values missing");
+    in.fixed = vec_values(fixed_vec, fixed_cols * len, "fixed cosets too short");
+    in.fixed_cols = fixed_cols;
+    in.advice = vec_values(advice_vec, advice_cols * len, "advice cosets too short");
+    in.advice_cols = advice_cols;
+    in.instance = vec_values(instance_vec, instance_cols * len, "instance cosets too short");
+    in.instance_cols = instance_cols;
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    in.challenges = d_chal;
+    in.challenge_len = challenge_len;
+    const fr_t *lag = vec_values(lagrange_vec, lagrange ? 3 * len : 0, "l0 | l_last | l_active cosets too short");
+    in.l0 = lag;
+    in.l_last = lag ? lag + len : nullptr;
+    in.l_active = lag ? lag + 2 * len : nullptr;
+    in.perm_products = vec_values(permutation_products_vec, permutation_sets * len, "permutation products too short");
+    in.perm_sets = permutation_sets;
+    in.perm_columns = permutation_columns;
+    in.perm_columns_len = permutation_columns_len;
+    in.perm_pk = vec_values(permutation_pk_vec, permutation_pk_cosets_len * len, "permutation cosets too short");
+    in.perm_pk_len = permutation_pk_cosets_len;
+    in.lk_product = vec_values(lookup_products_vec, lookup_count * len, "lookup products too short");
+    const fr_t *perm = vec_values(lookup_permuted_vec, 2 * lookup_count * len, "permuted lookup columns too short");
+    in.lk_input = perm;
+    in.lk_table = perm ? perm + len : nullptr;
+    in.lk_stride = 2 * len;
+    in.lookup_count = lookup_count;
+    in.trash_cosets = vec_values(trash_vec, trash_count * len, "trash cosets too short");
+    in.trash_sel = trash_selector_fixed_indices;
+    in.trash_count = trash_count;
+    in.custom_graph = &custom_graph;
+    in.lookup_graphs = lookup_graphs;
+    in.trash_graphs = trash_graphs;
+    fr_device_vec *v = device_vec_new(len, s);
+    try {
+        numerator_core(v->values, in, beta, gamma, theta, trash_challenge, y, omega, delta_start, delta_const,
+                       rot_scale, last_rotation, chunk_len, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
     return ok();
     GB_ENTRY_END
 }
@@ -447,41 +632,47 @@ RustError midnight_sppark_bls12_381_eval_graph_batch(RawFr *out_raw, size_t len,
         return make_error((int)cudaErrorInvalidValue, "invalid graph batch arguments");
     GB_ENTRY_BEGIN
     cudaStream_t s = lane_stream();
-    num_params p{};
-    p.len = len;
-    p.rot_scale = rot_scale;
     auto d_fixed = upload_fr(fixed, fixed_cols * len, s);
     auto d_advice = upload_fr(advice, advice_cols * len, s);
     auto d_instance = upload_fr(instance, instance_cols * len, s);
-    auto d_chal = upload_fr(challenges, challenge_len, s);
-    p.fixed = d_fixed;
-    p.fixed_cols = fixed_cols;
-    p.advice = d_advice;
-    p.advice_cols = advice_cols;
-    p.instance = d_instance;
-    p.instance_cols = instance_cols;
-    p.challenges = d_chal;
-    p.challenge_len = challenge_len;
-    p.beta = from_raw(beta);
-    p.gamma = from_raw(gamma);
-    p.theta = from_raw(theta);
-    p.trash = from_raw(trash_challenge);
-    p.y = from_raw(y);
     dev_buf<fr_t> d_out(len * graph_count, s);
-    std::vector<graph_upload> up(graph_count);
-    const unsigned grid = blocks_for(len, 128);
-    for (size_t gi = 0; gi < graph_count; gi++) {
-        upload_graph(up[gi], graphs[gi], s);
-        p.custom = up[gi].g;
-        fr_t *o = d_out.get() + gi * len;
-        launch_by_capacity(
-            capacity_for(graphs[gi].num_intermediates), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
-        GB_CHECK_LAUNCH();
-    }
+    graph_batch_core(d_out, len, d_fixed, fixed_cols, d_advice, advice_cols, d_instance, instance_cols, challenges,
+                     challenge_len, beta, gamma, theta, trash_challenge, y, rot_scale, graphs, graph_count, s);
     d2h(out_raw, d_out, len * graph_count * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+// graph_count graphs over resident columns (len rows each), into a new
+// device vector [graph_count][len]
+RustError gb_eval_graph_batch_device(void **out, size_t len, const void *fixed_vec, size_t fixed_cols,
+                                     const void *advice_vec, size_t advice_cols, const void *instance_vec,
+                                     size_t instance_cols, const RawFr *challenges, size_t challenge_len, RawFr beta,
+                                     RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, int32_t rot_scale,
+                                     const RawGraph *graphs, size_t graph_count)
+{
+    if (!out) return make_error((int)cudaErrorInvalidValue, "null graph batch output");
+    *out = nullptr;
+    if (len == 0 || graph_count == 0 || !graphs || (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid resident graph batch arguments");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    for (const void *v : {fixed_vec, advice_vec, instance_vec})
+        if (v) device_vec_wait(reinterpret_cast<const fr_device_vec *>(v), s);
+    const fr_t *fx = vec_values(fixed_vec, fixed_cols * len, "fixed columns too short");
+    const fr_t *ad = vec_values(advice_vec, advice_cols * len, "advice columns too short");
+    const fr_t *in = vec_values(instance_vec, instance_cols * len, "instance columns too short");
+    fr_device_vec *v = device_vec_new(len * graph_count, s);
+    try {
+        graph_batch_core(v->values, len, fx, fixed_cols, ad, advice_cols, in, instance_cols, challenges,
+                         challenge_len, beta, gamma, theta, trash_challenge, y, rot_scale, graphs, graph_count, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
     return ok();
     GB_ENTRY_END
 }

@@ -630,6 +630,46 @@ RustError midnight_sppark_bls12_381_fr_permutation_products(void **out, const Ra
     GB_ENTRY_END
 }
 
+// The permutation products over resident columns and permutation values
+// (column_count x len each); delta powers and blinds are host arrays.
+RustError gb_fr_permutation_products_device(void **out, const void *columns_vec, const void *permutations_vec,
+                                            size_t len, size_t column_count, size_t chunk_len, RawFr beta_raw,
+                                            RawFr gamma_raw, RawFr omega_raw, const RawFr *delta_powers_raw,
+                                            const RawFr *blind_values_raw, size_t blinding_factors)
+{
+    const fr_t *delta_powers = reinterpret_cast<const fr_t *>(delta_powers_raw);
+    const fr_t *blind_values = reinterpret_cast<const fr_t *>(blind_values_raw);
+    if (!out || len == 0 || column_count == 0 || chunk_len == 0 || !columns_vec || !permutations_vec ||
+        !delta_powers || blinding_factors >= len || (blinding_factors != 0 && !blind_values))
+        return make_error((int)cudaErrorInvalidValue, "invalid resident permutation product arguments");
+    *out = nullptr;
+    const size_t sets = (column_count + chunk_len - 1) / chunk_len;
+    if (column_count > SIZE_MAX / len || sets > SIZE_MAX / len)
+        return make_error((int)cudaErrorInvalidValue, "permutation product size overflow");
+    GB_ENTRY_BEGIN
+    auto *cv = reinterpret_cast<const fr_device_vec *>(columns_vec);
+    auto *pv = reinterpret_cast<const fr_device_vec *>(permutations_vec);
+    if (cv->len < column_count * len || pv->len < column_count * len)
+        return make_error((int)cudaErrorInvalidValue, "resident permutation columns too short");
+    cudaStream_t s = lane_stream();
+    device_vec_wait(cv, s);
+    device_vec_wait(pv, s);
+    auto dd = upload(delta_powers, column_count, s);
+    auto db = upload(blind_values, sets * blinding_factors, s);
+    fr_device_vec *v = device_vec_new(sets * len, s);
+    try {
+        permutation_products(v->values, cv->values, pv->values, len, column_count, chunk_len, gb::from_raw(beta_raw),
+                             gb::from_raw(gamma_raw), gb::from_raw(omega_raw), dd, db, blinding_factors, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
 // bls12_381_g1_msm.cu:4451-4548
 RustError midnight_sppark_bls12_381_fr_lookup_products(void **out, const RawFr *compressed_inputs_raw, const RawFr *compressed_tables_raw, const RawFr *permuted_inputs_raw, const RawFr *permuted_tables_raw, size_t len, size_t lookup_count, RawFr beta_raw, RawFr gamma_raw, const RawFr *blind_values_raw, size_t blinding_factors)
 {

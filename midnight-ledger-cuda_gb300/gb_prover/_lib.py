@@ -130,6 +130,12 @@ def _declare(L):
             vp, vp, vp, vp, sz, vp, sz, vp, sz, vp, vp, vp, sz, vp, vp, sz, RawGraph, vp, vp]),
         "midnight_sppark_bls12_381_eval_graph_batch": (E, [
             vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, i32, vp, sz]),
+        "gb_eval_graph_batch_device": (E, [
+            vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, i32, vp, sz]),
+        "gb_eval_numerator_device": (E, [
+            vp, sz, vp, u32, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, fr, fr, fr, i32, i32, u32,
+            vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, vp, sz, RawGraph, vp, vp]),
+        "gb_fr_permutation_products_device": (E, [vp, vp, vp, sz, sz, sz, fr, fr, fr, vp, vp, sz]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)

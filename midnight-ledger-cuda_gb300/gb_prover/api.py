@@ -23,6 +23,7 @@ __all__ = [
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
+    "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -487,4 +488,68 @@ def bls12_381_fr_device_eval_polys(devvec, poly_len, poly_count, point):
 def fr_device_kate_divide(devvec, poly_len, poly_count, point):
     h = ctypes.c_void_p()
     check(lib().gb_fr_device_kate_divide(ctypes.byref(h), devvec.raw, poly_len, poly_count, _fr(point)))
+    return Bls12_381FrDeviceVec(h)
+
+
+# ---------------------------------------------------------------- resident argument / quotient forms
+
+def _raw(v):
+    return None if v is None else v.raw
+
+
+def fr_permutation_products_device(columns, permutations, length, column_count, chunk_len, beta, gamma, omega,
+                                   delta_powers, blind_values, blinding_factors):
+    d = _fr_arr(delta_powers)
+    b = _fr_arr(blind_values) if blind_values is not None and len(blind_values) else None
+    h = ctypes.c_void_p()
+    check(lib().gb_fr_permutation_products_device(ctypes.byref(h), columns.raw, permutations.raw, length,
+                                                  column_count, chunk_len, _fr(beta), _fr(gamma), _fr(omega),
+                                                  _ptr(d), _ptr(b), blinding_factors))
+    return Bls12_381FrDeviceVec(h)
+
+
+def eval_graph_batch_device(length, graphs, fixed=None, fixed_cols=0, advice=None, advice_cols=0, instance=None,
+                            instance_cols=0, challenges=None, beta=None, gamma=None, theta=None,
+                            trash_challenge=None, y=None, rot_scale=1):
+    from .graph import graph_array
+    z = np.zeros(4, dtype=np.uint64)
+    ch = _fr_arr(challenges) if challenges is not None else None
+    ga = graph_array(list(graphs))
+    f = lambda v: _fr(z if v is None else v)  # noqa: E731
+    h = ctypes.c_void_p()
+    check(lib().gb_eval_graph_batch_device(
+        ctypes.byref(h), length, _raw(fixed), fixed_cols, _raw(advice), advice_cols, _raw(instance), instance_cols,
+        _ptr(ch), 0 if ch is None else len(ch), f(beta), f(gamma), f(theta), f(trash_challenge), f(y), rot_scale,
+        ctypes.cast(ga, ctypes.c_void_p), len(graphs)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def eval_numerator_device(length, custom_graph, fixed=None, fixed_cols=0, advice=None, advice_cols=0,
+                          instance=None, instance_cols=0, challenges=None, beta=None, gamma=None, theta=None,
+                          trash_challenge=None, y=None, omega=None, delta_start=None, delta_const=None, rot_scale=1,
+                          last_rotation=-1, chunk_len=1, lagrange=None, permutation_products=None,
+                          permutation_sets=0, permutation_columns=(), permutation_pk_cosets=None,
+                          permutation_pk_count=0, lookup_products=None, lookup_permuted=None, lookup_graphs=(),
+                          trash=None, trash_selectors=(), trash_graphs=(), initial=None):
+    """gb_eval_numerator_device: every column argument a Bls12_381FrDeviceVec;
+    lagrange = l0 | l_last | l_active; lookup_permuted = per lookup its
+    permuted input then permuted table coset."""
+    from .graph import column_refs, graph_array
+    z = np.zeros(4, dtype=np.uint64)
+    ch = _fr_arr(challenges) if challenges is not None else None
+    pcols = column_refs(list(permutation_columns))
+    lk_g = graph_array(list(lookup_graphs))
+    tr_g = graph_array(list(trash_graphs))
+    tr_s = np.array(list(trash_selectors) or [0], dtype=np.uint32)
+    g = custom_graph.raw() if custom_graph is not None else graph_array([])[0]
+    f = lambda v: _fr(z if v is None else v)  # noqa: E731
+    h = ctypes.c_void_p()
+    check(lib().gb_eval_numerator_device(
+        ctypes.byref(h), length, _raw(initial), 1 if custom_graph is not None else 0, _raw(fixed), fixed_cols,
+        _raw(advice), advice_cols, _raw(instance), instance_cols, _ptr(ch), 0 if ch is None else len(ch), f(beta),
+        f(gamma), f(theta), f(trash_challenge), f(y), f(omega), f(delta_start), f(delta_const), rot_scale,
+        last_rotation, chunk_len, _raw(lagrange), _raw(permutation_products), permutation_sets,
+        ctypes.cast(pcols, ctypes.c_void_p), len(permutation_columns), _raw(permutation_pk_cosets),
+        permutation_pk_count, _raw(lookup_products), _raw(lookup_permuted), len(lookup_graphs), _raw(trash),
+        _ptr(tr_s), len(trash_graphs), g, ctypes.cast(lk_g, ctypes.c_void_p), ctypes.cast(tr_g, ctypes.c_void_p)))
     return Bls12_381FrDeviceVec(h)

@@ -46,7 +46,7 @@ from . import api
 from .graph import (ADD, BETA, CONSTANT, DOUBLE, FIXED, ADVICE, INSTANCE, GAMMA, HORNER, INTERMEDIATE, MUL,
                     NEGATE, PREVIOUS, SQUARE, STORE, SUB, THETA, Y, Graph)
 from .kzg import CircuitTranscript, ParamsKZG, affine_from_projective, compress, fr_to_repr
-from .rng import ChaCha20Rng, fr_random, ints_to_mont, mont_to_ints
+from .rng import R2_LIMBS, ChaCha20Rng, fr_random, fr_random_raw, ints_to_mont, mont_to_ints
 
 R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
 S_TWO_ADICITY = 32
@@ -625,21 +625,18 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
 
     # ---- lookups: compress, permute, commit A' and S' (lookup/prover.rs:688-733)
     L = c.lookups
-    lk = []
     if L:
         comp = backend.eval_graphs_lagrange([g for pair in zip(pk.lookup_input_graphs, pk.lookup_table_graphs)
                                              for g in pair], pk.fixed_lagrange, c.num_fixed, adv_l, m, n,
                                             theta=w(theta))
-    for li in range(L):
-        ci, ct = comp[2 * li], comp[2 * li + 1]
-        ib = fr_random(rng, bf + 1)
-        tb = fr_random(rng, bf + 1)
-        a_p, s_p = _permute_expression_pair(backend, ci, ct, u, ib, tb)
-        lk.append({"ci": ci, "ct": ct, "a": a_p, "s": s_p})
-    if L:
-        perm_l = backend.put(np.concatenate([np.concatenate([x["a"], x["s"]]) for x in lk]))
-        cms = backend.commit_lagrange(perm_l, n, 2 * L)
-        for cm in cms:
+        permuted = []
+        for li in range(L):
+            ib = fr_random(rng, bf + 1)
+            tb = fr_random(rng, bf + 1)
+            ci, ct = backend.to_host(comp, n, 2 * li), backend.to_host(comp, n, 2 * li + 1)
+            permuted += list(_permute_expression_pair(backend, ci, ct, u, ib, tb))
+        perm_l = backend.put(np.concatenate(permuted))
+        for cm in backend.commit_lagrange(perm_l, n, 2 * L):
             transcript.write_point(cm)
     beta = fr_int(transcript.squeeze_challenge())
     gamma = fr_int(transcript.squeeze_challenge())
@@ -652,9 +649,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     z_perm = backend.permutation_products(adv_l, pk.sigma_lagrange, n, m, c.chunk_len, w(beta), w(gamma),
                                           w(dom.omega), deltas, perm_blinds, bf)
     if L:
-        z_lk = backend.lookup_products(np.concatenate([x["ci"] for x in lk]), np.concatenate([x["ct"] for x in lk]),
-                                       np.concatenate([x["a"] for x in lk]), np.concatenate([x["s"] for x in lk]),
-                                       n, L, w(beta), w(gamma), lk_blinds, bf)
+        z_lk = backend.lookup_products(comp, perm_l, n, L, w(beta), w(gamma), lk_blinds, bf)
     for cm in backend.commit_lagrange(z_perm, n, sets):
         transcript.write_point(cm)
     if L:
@@ -663,7 +658,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     transcript.squeeze_challenge()  # trash challenge (no trash arguments)
 
     # ---- vanishing argument: random polynomial (vanishing/prover.rs:41-97)
-    random_poly = backend.put(fr_random(rng, n))
+    random_poly = backend.to_mont(fr_random_raw(rng, n))
     transcript.write_point(backend.commit(random_poly, n, 1)[0])
     y = fr_int(transcript.squeeze_challenge())
 
@@ -893,36 +888,43 @@ class GpuBackend:
         return self._commit(h, n, count, False)
 
     # arguments
+    def to_mont(self, raw):
+        """canonical limb rows -> resident Montgomery values (a product with R^2)"""
+        return api.bls12_381_fr_device_poly_lincomb(self.put(raw), len(raw), 1, R2_LIMBS.reshape(1, 4))
+
+    def to_host(self, h, n, i):
+        return h.gather_polys(n, [i]).download()
+
     def sort_canonical(self, arr):
         return api.bls12_381_fr_sort_canonical(arr)
 
     def eval_graphs_lagrange(self, builders, fixed_h, nfixed, adv_h, m, n, theta):
         graphs = [b.compile(Graph) for b in builders]
-        out = api.bls12_381_eval_graph_batch(n, graphs, fixed=fixed_h.download(), advice=adv_h.download(),
-                                             theta=theta, rot_scale=1)
-        return [out[i] for i in range(len(graphs))]
+        return api.eval_graph_batch_device(n, graphs, fixed=fixed_h, fixed_cols=nfixed, advice=adv_h, advice_cols=m,
+                                           theta=theta, rot_scale=1)
 
     def permutation_products(self, adv_h, sigma_h, n, m, chunk, beta, gamma, omega, deltas, blinds, bf):
-        return api.bls12_381_fr_permutation_products(adv_h.download(), sigma_h.download(), n, m, chunk, beta, gamma,
-                                                     omega, deltas, blinds, bf)
+        return api.fr_permutation_products_device(adv_h, sigma_h, n, m, chunk, beta, gamma, omega, deltas, blinds, bf)
 
-    def lookup_products(self, ci, ct, a, s, n, L, beta, gamma, blinds, bf):
-        return api.bls12_381_fr_lookup_products(ci, ct, a, s, n, L, beta, gamma, blinds, bf)
+    def lookup_products(self, comp_h, perm_h, n, L, beta, gamma, blinds, bf):
+        # trace [compressed inputs | compressed tables | permuted inputs | permuted tables]
+        both = self.cat([comp_h, perm_h])
+        idx = [2 * i for i in range(L)] + [2 * i + 1 for i in range(L)] + \
+              [2 * L + 2 * i for i in range(L)] + [2 * L + 2 * i + 1 for i in range(L)]
+        trace = both.gather_polys(n, idx)
+        return api.bls12_381_fr_lookup_products_device(trace, n, L, beta, gamma, blinds, bf)
 
     def numerator(self, pk, ek, adv_e, m, beta, gamma, theta, y, omega, delta_start, delta_const, rot_scale,
                   last_rotation, chunk_len, zp_e, sets, lookups):
         N = 1 << ek
-        lks = []
-        for g, zl_e, perm_e, li in lookups:
-            pe = perm_e.download()
-            lks.append((g.compile(Graph), zl_e.download()[li * N:(li + 1) * N], pe[2 * li * N:(2 * li + 1) * N],
-                        pe[(2 * li + 1) * N:(2 * li + 2) * N]))
-        lc = pk.l_cosets.download()
-        out = api.bls12_381_eval_numerator(
-            N, pk.custom_graph.compile(Graph), fixed=pk.fixed_cosets.download(), advice=adv_e.download(),
-            beta=beta, gamma=gamma, theta=theta, y=y, omega=omega, delta_start=delta_start,
+        c = pk.circuit
+        zl_e = lookups[0][1] if lookups else None
+        perm_e = lookups[0][2] if lookups else None
+        return api.eval_numerator_device(
+            N, pk.custom_graph.compile(Graph), fixed=pk.fixed_cosets, fixed_cols=c.num_fixed, advice=adv_e,
+            advice_cols=m, beta=beta, gamma=gamma, theta=theta, y=y, omega=omega, delta_start=delta_start,
             delta_const=delta_const, rot_scale=rot_scale, last_rotation=last_rotation, chunk_len=chunk_len,
-            l0=lc[:N], l_last=lc[N:2 * N], l_active=lc[2 * N:], permutation_products=zp_e.download(),
-            permutation_sets=sets, permutation_columns=[(1, i) for i in range(m)],
-            permutation_pk_cosets=pk.sigma_cosets.download(), lookups=lks)
-        return self.put(out)
+            lagrange=pk.l_cosets, permutation_products=zp_e, permutation_sets=sets,
+            permutation_columns=[(1, i) for i in range(m)], permutation_pk_cosets=pk.sigma_cosets,
+            permutation_pk_count=m, lookup_products=zl_e, lookup_permuted=perm_e,
+            lookup_graphs=[g.compile(Graph) for g, _, _, _ in lookups])

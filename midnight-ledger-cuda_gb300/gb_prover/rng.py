@@ -149,6 +149,17 @@ def raw_to_mont(raw):
 
 def fr_random(rng: ChaCha20Rng, n):
     """n field elements by Fq::random's rejection rule, Montgomery form (n, 4)."""
+    return raw_to_mont(fr_random_raw(rng, n))
+
+
+# R^2 mod r as limbs: a Montgomery product with it maps a canonical value
+# to its Montgomery form
+R2_LIMBS = np.array([(_R2 >> (64 * i)) & _MASK64 for i in range(4)], dtype=np.uint64)
+
+
+def fr_random_raw(rng: ChaCha20Rng, n):
+    """The draws of fr_random as canonical limb rows (n, 4), before the
+    Montgomery conversion."""
     got = []
     total = 0
     while total < n:
@@ -167,5 +178,4 @@ def fr_random(rng: ChaCha20Rng, n):
             idx = idx[:want]
         got.append(raw[idx])
         total += len(idx)
-    raw = np.concatenate(got) if got else np.zeros((0, 4), np.uint64)
-    return raw_to_mont(raw)
+    return np.concatenate(got) if got else np.zeros((0, 4), np.uint64)

@@ -143,19 +143,30 @@ class OracleBackend:
         return self._commit(h, n, count, self.params.g)
 
     # arguments
+    def to_mont(self, raw):
+        from gb_prover.rng import R2_LIMBS
+        return HostPoly(orc.fr_mul_assign(raw, R2_LIMBS))
+
+    def to_host(self, h, n, i):
+        return h.a[i * n:(i + 1) * n].copy()
+
     def sort_canonical(self, arr):
         return orc.fr_sort_canonical(arr)
 
     def eval_graphs_lagrange(self, builders, fixed_h, nfixed, adv_h, m, n, theta):
-        return [orc.eval_numerator(n, b.compile(orc.OracleGraph), fixed=fixed_h.a, advice=adv_h.a, theta=theta,
-                                   rot_scale=1, threads=self.threads) for b in builders]
+        return HostPoly(np.concatenate([orc.eval_numerator(n, b.compile(orc.OracleGraph), fixed=fixed_h.a,
+                                                           advice=adv_h.a, theta=theta, rot_scale=1,
+                                                           threads=self.threads) for b in builders]))
 
     def permutation_products(self, adv_h, sigma_h, n, m, chunk, beta, gamma, omega, deltas, blinds, bf):
         return HostPoly(orc.fr_permutation_products(adv_h.a, sigma_h.a, n, m, chunk, beta, gamma, omega, deltas,
                                                      blinds, bf))
 
-    def lookup_products(self, ci, ct, a, s, n, L, beta, gamma, blinds, bf):
-        return HostPoly(orc.fr_lookup_products(ci, ct, a, s, n, L, beta, gamma, blinds, bf))
+    def lookup_products(self, comp_h, perm_h, n, L, beta, gamma, blinds, bf):
+        cols = lambda h, j: h.a[j * n:(j + 1) * n]  # noqa: E731
+        stack = lambda h, off: np.concatenate([cols(h, 2 * i + off) for i in range(L)])  # noqa: E731
+        return HostPoly(orc.fr_lookup_products(stack(comp_h, 0), stack(comp_h, 1), stack(perm_h, 0), stack(perm_h, 1),
+                                               n, L, beta, gamma, blinds, bf))
 
     def numerator(self, pk, ek, adv_e, m, beta, gamma, theta, y, omega, delta_start, delta_const, rot_scale,
                   last_rotation, chunk_len, zp_e, sets, lookups):

@@ -86,8 +86,9 @@ def test_permute_expression_pair_properties():
     pk = plonk.keygen(p, c, be, fixed, copies)
     adv = be.put(plonk.ints_to_mont([v for col in advice for v in col]))
     theta = plonk.fr_mont(11)
-    ci, ct = be.eval_graphs_lagrange([pk.lookup_input_graphs[0], pk.lookup_table_graphs[0]], pk.fixed_lagrange,
-                                     c.num_fixed, adv, c.m, c.n, theta)
+    comp = be.eval_graphs_lagrange([pk.lookup_input_graphs[0], pk.lookup_table_graphs[0]], pk.fixed_lagrange,
+                                   c.num_fixed, adv, c.m, c.n, theta)
+    ci, ct = be.to_host(comp, c.n, 0), be.to_host(comp, c.n, 1)
     u = c.usable_rows
     blinds = np.zeros((c.n - u, 4), np.uint64)
     a_p, s_p = plonk._permute_expression_pair(be, ci, ct, u, blinds, blinds)
