@@ -316,6 +316,8 @@ def main():
         cpu = {"value": v, "unit": "Mpts/s", "cores": threads, "kind": "port",
                "sample": "one n=2^%d MSM (same scalar/base distribution), oracle C Pippenger on all host "
                          "threads (%.1f s)" % (args.n_ref.bit_length() - 1, dt)}
+        if not args.no_extras:
+            cpu["proof_k16_s"] = cpu_baseline_proof()
 
     del ctx, dv
     if rank == 0:
@@ -410,6 +412,113 @@ def batched_config(gb, torch, rng):
     return out
 
 
+def proof_config(gb, steps=10):
+    """The full synthetic PLONK/KZG proof at k = 16 (3 advice columns,
+    standard gate, 2^14 copy constraints, one 2-column lookup into a 2^12-row
+    table, SRS of 2^16 points from a seeded tau): proofs one at a time
+    through the GPU prover, the witness already in Montgomery form on the
+    host, each proof ending with its bytes on the host."""
+    from gb_prover import plonk
+    from gb_prover.kzg import CircuitTranscript, ParamsKZG
+    from gb_prover.rng import ChaCha20Rng, ints_to_mont
+    c = plonk.SyntheticCircuit(16, advice=3, degree=3, lookups=1, copies=1 << 14, table_log=12,
+                               label="full synthetic PLONK/KZG proof, k=16")
+    fixed, advice, copies = c.synthesize()
+    params = ParamsKZG.unsafe_setup(16, plonk.fr_mont(0x5EED0F7A0))
+    be = plonk.GpuBackend(params)
+    t0 = time.perf_counter()
+    pk = plonk.keygen(params, c, be, fixed, copies)
+    keygen_s = time.perf_counter() - t0
+    adv = ints_to_mont([v for col in advice for v in col])
+    for i in range(2):
+        plonk.create_proof(params, pk, adv, be, CircuitTranscript(), ChaCha20Rng.from_label("warm%d" % i))
+    lat = []
+    for i in range(steps):
+        t0 = time.perf_counter()
+        proof = plonk.create_proof(params, pk, adv, be, CircuitTranscript(), ChaCha20Rng.from_label("p%d" % i))
+        lat.append(time.perf_counter() - t0)
+    lat.sort()
+    return {"proof_k16_proofs_per_s": steps / sum(lat), "proof_k16_p50_ms": lat[len(lat) // 2] * 1e3,
+            "proof_k16_p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] * 1e3,
+            "proof_k16_bytes": len(proof), "proof_k16_keygen_s": keygen_s, "proof_k16_count": steps}
+
+
+SERVE_CIRCUITS = [  # (k, advice, gate degree, lookups, share of requests)
+    (12, 3, 3, 0, 0.40), (13, 4, 4, 1, 0.25), (14, 8, 5, 2, 0.15),
+    (15, 5, 3, 1, 0.10), (16, 3, 3, 1, 0.05), (18, 4, 4, 0, 0.05)]
+
+
+def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, load=0.85):
+    """Proof serving: a Poisson stream of proof requests over 6 synthetic
+    circuits (k = 12..18, 3-8 advice columns, gate degree 3-5, 0-2 lookups,
+    request shares 40/25/15/10/5/5 %), the 2^18-point SRS (downsized per k)
+    and every proving key resident. The arrival rate loads the sequential
+    prover to `load` of its capacity; the same stream then runs through the
+    one-at-a-time prover (1 slot) and the continuous-batching server
+    (`slots` lanes, HBM budget for proofs in flight)."""
+    from gb_prover import plonk, serve
+    from gb_prover.kzg import CircuitTranscript, ParamsKZG
+    from gb_prover.rng import ChaCha20Rng, ints_to_mont
+    t0 = time.perf_counter()
+    srs = ParamsKZG.unsafe_setup(18, plonk.fr_mont(0x5EED0F7A0))
+    entries, wits, shares, per_k = {}, {}, [], {18: srs}
+    for cid, (k, m, d, L, share) in enumerate(SERVE_CIRCUITS):
+        c = plonk.SyntheticCircuit(k, advice=m, degree=d, lookups=L, copies=1 << (k - 2),
+                                   table_log=min(12, k - 3), label="serve circuit %d" % cid)
+        fixed, advice, copies = c.synthesize()
+        params = per_k.setdefault(k, srs.downsize(k))
+        entries[cid] = (params, plonk.keygen(params, c, plonk.GpuBackend(params), fixed, copies))
+        wits[cid] = ints_to_mont([v for col in advice for v in col])
+        shares.append(share)
+    setup_s = time.perf_counter() - t0
+    # sequential service time per circuit (after a warm-up proof each)
+    service = []
+    for cid, (params, pk) in entries.items():
+        be = plonk.GpuBackend(params)
+        plonk.create_proof(params, pk, wits[cid], be, CircuitTranscript(), ChaCha20Rng.from_label("warm"))
+        t1 = time.perf_counter()
+        for i in range(3):
+            plonk.create_proof(params, pk, wits[cid], be, CircuitTranscript(), ChaCha20Rng.from_label("w%d" % i))
+        service.append((time.perf_counter() - t1) / 3)
+    mean_s = sum(sh * t for sh, t in zip(shares, service))
+    rate = load / mean_s
+    rng = np.random.default_rng(2024)
+    cids = rng.choice(len(shares), size=requests, p=np.array(shares) / sum(shares))
+    arrivals = serve.poisson_arrivals(rng, rate, requests)
+    reqs = [(int(c), wits[int(c)], "request-%d" % i) for i, c in enumerate(cids)]
+    out = {"serve_setup_s": setup_s, "serve_rate_per_s": rate, "serve_requests": requests,
+           "serve_service_ms": [t * 1e3 for t in service], "serve_slots": slots, "serve_hbm_budget_gb": hbm_budget / 2 ** 30}
+    proofs = {}
+    for name, nslots in (("sequential", 1), ("batched", slots)):
+        srv = serve.ProofServer(entries, slots=nslots, hbm_budget=hbm_budget)
+        done, ts = serve.run_stream(srv, reqs, arrivals)
+        srv.close()
+        summ = serve.latency_summary(done, ts)
+        for key in ("proofs_per_s", "p50_ms", "p99_ms", "mean_ms"):
+            out["serve_%s_%s" % (name, key)] = summ[key]
+        proofs[name] = [r.future.result() for r in done]
+    out["serve_batched_equals_sequential"] = proofs["batched"] == proofs["sequential"]
+    return out
+
+
+def cpu_baseline_proof():
+    """One k = 16 proof of the same circuit through the prover driver on the
+    oracle's C restatements (all host threads)."""
+    from gb_prover import plonk
+    from gb_prover.kzg import CircuitTranscript
+    from gb_prover.rng import ChaCha20Rng
+    from oracle import plonk_cpu
+    c = plonk.SyntheticCircuit(16, advice=3, degree=3, lookups=1, copies=1 << 14, table_log=12,
+                               label="full synthetic PLONK/KZG proof, k=16")
+    fixed, advice, copies = c.synthesize()
+    params = plonk_cpu.setup_params(16, 0x5EED0F7A0)
+    be = plonk_cpu.OracleBackend(params)
+    pk = plonk.keygen(params, c, be, fixed, copies)
+    t0 = time.perf_counter()
+    plonk.create_proof(params, pk, advice, be, CircuitTranscript(), ChaCha20Rng.from_label("cpu"))
+    return time.perf_counter() - t0
+
+
 def extras(gb, torch, n, rng, bases, args):
     """Secondary numbers of the same configuration (not the headline)."""
     out = {}
@@ -444,6 +553,8 @@ def extras(gb, torch, n, rng, bases, args):
     out["lde_2p20_to_2p22_x16_host_in_ms"] = (time.perf_counter() - t0) * 1e3
     del lde, src
     out.update(batched_config(gb, torch, rng))
+    out.update(proof_config(gb))
+    out.update(serve_config(gb))
     return out
 
 

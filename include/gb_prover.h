@@ -279,6 +279,25 @@ GB_API RustError gb_eval_numerator_device(
     size_t lookup_count, const void *trash_vec, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
     RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs);
 
+/* permute_expression_pair (lookup/prover.rs:1573-1690) for lookup_count
+ * lookups on the device: compressed_vec = per lookup its compressed input
+ * then compressed table column (len rows each); out = a new device vector,
+ * per lookup A' then S' (len rows each), rows usable_rows.. taken from
+ * input_blinds / table_blinds ([lookup_count][len - usable_rows] each).
+ * An input value missing from the table is an error. */
+GB_API RustError gb_fr_lookup_permute_device(void **out, const void *compressed_vec, size_t len, size_t usable_rows,
+                                             size_t lookup_count, const RawFr *input_blinds,
+                                             const RawFr *table_blinds);
+
+/* ---- blinding draws ---------------------------------------------------------- */
+/* n values by Fq::random's rejection rule (fq.rs:373-387) from the
+ * ChaCha20Rng stream with this 32-byte seed, starting at keystream word
+ * word_offset, into a new device vector in Montgomery form;
+ * *words_consumed = the keystream words the n draws used (the large draw of
+ * vanishing/prover.rs:41-75 made on the device) */
+GB_API RustError gb_fr_random_chacha20(void **out, const uint8_t *key32, uint64_t word_offset, size_t n,
+                                       uint64_t *words_consumed);
+
 /* ---- KZG opening helpers ---------------------------------------------------- */
 /* bls12_381_g1_msm.cu:3985-4031: out[p] = sum_i polys[p][i] * point^i for the
  * poly_count resident polynomials of poly_len coefficients */

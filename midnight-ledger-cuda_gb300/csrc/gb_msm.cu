@@ -609,7 +609,8 @@ struct msm_context_t {
     int nwin = 0;
     affine_t *table = nullptr;  // [nwin][npoints]: 2^(c*j) P_i
     cudaStream_t owner = nullptr;
-    std::mutex mu;
+    // read-only once created: calls from different lanes run concurrently,
+    // each with its own stream-ordered scratch
 };
 
 static RawMsmConfig default_config(size_t npoints)
@@ -802,7 +803,6 @@ RustError midnight_sppark_bls12_381_g1_msm_context_batch(RawG1Projective *out_ra
     if (nmsms == 0) return ok();
     if (!out || (npoints && !scalars)) return make_error((int)cudaErrorInvalidValue, "invalid MSM batch arguments");
     if (npoints > ctx->npoints) return make_error((int)cudaErrorInvalidValue, "more scalars than context bases");
-    std::lock_guard<std::mutex> lk(ctx->mu);
     cudaStream_t s = lane_stream();
     dev_buf<fr_t> d_scalars(npoints * nmsms, s);
     h2d(d_scalars, scalars, npoints * nmsms * sizeof(fr_t), s);
@@ -826,7 +826,6 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_batch(RawG1Projective 
         return make_error((int)cudaErrorInvalidValue, "resident MSM range exceeds device vector");
     if (npoints > ctx->npoints) return make_error((int)cudaErrorInvalidValue, "more scalars than context bases");
     if (nmsms == 0) return ok();
-    std::lock_guard<std::mutex> lk(ctx->mu);
     cudaStream_t s = lane_stream();
     device_vec_wait(dv, s);
     context_run_device(ctx, out, dv->values + scalar_offset, npoints, nmsms, s);
@@ -851,7 +850,6 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_ragged(RawG1Projective
         if (sl.point_offset > ctx->npoints || sl.len > ctx->npoints - sl.point_offset)
             return make_error((int)cudaErrorInvalidValue, "ragged MSM slice exceeds context bases");
     }
-    std::lock_guard<std::mutex> lk(ctx->mu);
     cudaStream_t s = lane_stream();
     device_vec_wait(dv, s);
     std::vector<msm_item> items;
@@ -885,7 +883,6 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch(RawG1P
         return make_error((int)cudaErrorInvalidValue, "scrambled resident MSM range exceeds device vector");
     if (npoints > ctx->npoints) return make_error((int)cudaErrorInvalidValue, "more scalars than context bases");
     if (count == 0) return ok();
-    std::lock_guard<std::mutex> lk(ctx->mu);
     cudaStream_t s = lane_stream();
     device_vec_wait(dv, s);
     device_vec_wait(mv, s);

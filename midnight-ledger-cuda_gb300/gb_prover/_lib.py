@@ -136,6 +136,8 @@ def _declare(L):
             vp, sz, vp, u32, vp, sz, vp, sz, vp, sz, vp, sz, fr, fr, fr, fr, fr, fr, fr, fr, i32, i32, u32,
             vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, vp, sz, RawGraph, vp, vp]),
         "gb_fr_permutation_products_device": (E, [vp, vp, vp, sz, sz, sz, fr, fr, fr, vp, vp, sz]),
+        "gb_fr_random_chacha20": (E, [vp, vp, ctypes.c_uint64, sz, vp]),
+        "gb_fr_lookup_permute_device": (E, [vp, vp, sz, sz, sz, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)

@@ -23,7 +23,8 @@ __all__ = [
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
-    "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device",
+    "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
+    "fr_lookup_permute_device",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -552,4 +553,22 @@ def eval_numerator_device(length, custom_graph, fixed=None, fixed_cols=0, advice
         ctypes.cast(pcols, ctypes.c_void_p), len(permutation_columns), _raw(permutation_pk_cosets),
         permutation_pk_count, _raw(lookup_products), _raw(lookup_permuted), len(lookup_graphs), _raw(trash),
         _ptr(tr_s), len(trash_graphs), g, ctypes.cast(lk_g, ctypes.c_void_p), ctypes.cast(tr_g, ctypes.c_void_p)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def fr_random_chacha20(key32, word_offset, n):
+    """(device vector of n Montgomery values, keystream words consumed)"""
+    key = (ctypes.c_uint8 * 32).from_buffer_copy(bytes(key32))
+    used = ctypes.c_uint64()
+    h = ctypes.c_void_p()
+    check(lib().gb_fr_random_chacha20(ctypes.byref(h), key, word_offset, n, ctypes.byref(used)))
+    return Bls12_381FrDeviceVec(h), used.value
+
+
+def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, input_blinds, table_blinds):
+    ib = _fr_arr(input_blinds) if len(input_blinds) else None
+    tb = _fr_arr(table_blinds) if len(table_blinds) else None
+    h = ctypes.c_void_p()
+    check(lib().gb_fr_lookup_permute_device(ctypes.byref(h), compressed.raw, length, usable_rows, lookup_count,
+                                            _ptr(ib), _ptr(tb)))
     return Bls12_381FrDeviceVec(h)

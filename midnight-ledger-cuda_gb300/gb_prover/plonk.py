@@ -629,13 +629,8 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
         comp = backend.eval_graphs_lagrange([g for pair in zip(pk.lookup_input_graphs, pk.lookup_table_graphs)
                                              for g in pair], pk.fixed_lagrange, c.num_fixed, adv_l, m, n,
                                             theta=w(theta))
-        permuted = []
-        for li in range(L):
-            ib = fr_random(rng, bf + 1)
-            tb = fr_random(rng, bf + 1)
-            ci, ct = backend.to_host(comp, n, 2 * li), backend.to_host(comp, n, 2 * li + 1)
-            permuted += list(_permute_expression_pair(backend, ci, ct, u, ib, tb))
-        perm_l = backend.put(np.concatenate(permuted))
+        blinds = [fr_random(rng, bf + 1) for _ in range(2 * L)]  # per lookup: input, then table
+        perm_l = backend.permute_lookups(comp, n, u, L, np.concatenate(blinds[0::2]), np.concatenate(blinds[1::2]))
         for cm in backend.commit_lagrange(perm_l, n, 2 * L):
             transcript.write_point(cm)
     beta = fr_int(transcript.squeeze_challenge())
@@ -658,7 +653,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     transcript.squeeze_challenge()  # trash challenge (no trash arguments)
 
     # ---- vanishing argument: random polynomial (vanishing/prover.rs:41-97)
-    random_poly = backend.to_mont(fr_random_raw(rng, n))
+    random_poly = backend.random_mont(rng, n)
     transcript.write_point(backend.commit(random_poly, n, 1)[0])
     y = fr_int(transcript.squeeze_challenge())
 
@@ -892,8 +887,21 @@ class GpuBackend:
         """canonical limb rows -> resident Montgomery values (a product with R^2)"""
         return api.bls12_381_fr_device_poly_lincomb(self.put(raw), len(raw), 1, R2_LIMBS.reshape(1, 4))
 
+    def random_mont(self, rng, n):
+        """fr_random(rng, n), resident: large draws run the ChaCha20 stream and
+        the rejection sampling on the device, then the host rng skips the
+        words they used"""
+        if n < 4096:
+            return self.put(fr_random(rng, n))
+        vec, used = api.fr_random_chacha20(rng.seed, rng.word_position(), n)
+        rng.skip_words(used)
+        return vec
+
     def to_host(self, h, n, i):
         return h.gather_polys(n, [i]).download()
+
+    def permute_lookups(self, comp_h, n, u, L, input_blinds, table_blinds):
+        return api.fr_lookup_permute_device(comp_h, n, u, L, input_blinds, table_blinds)
 
     def sort_canonical(self, arr):
         return api.bls12_381_fr_sort_canonical(arr)

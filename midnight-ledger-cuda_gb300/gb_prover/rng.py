@@ -83,7 +83,7 @@ class ChaCha20Rng:
         have = len(self._buf) - self._pos
         if have < count:
             need = count - have
-            nblocks = (need + 15) // 16
+            nblocks = max((need + 15) // 16, 256)
             fresh = _chacha_blocks(self._key, self._block, nblocks).reshape(-1)
             self._block += nblocks
             self._buf = np.concatenate([self._buf[self._pos:], fresh])
@@ -91,6 +91,28 @@ class ChaCha20Rng:
         w = self._buf[self._pos:self._pos + count]
         self._pos += count
         return w
+
+    @property
+    def seed(self):
+        return self._key.astype("<u4").tobytes()
+
+    def word_position(self):
+        """absolute index of the next keystream word"""
+        return self._block * 16 - (len(self._buf) - self._pos)
+
+    def skip_words(self, count):
+        """advance the stream by `count` words"""
+        have = len(self._buf) - self._pos
+        if count <= have:
+            self._pos += count
+            return
+        target = self.word_position() + count
+        self._block = target // 16
+        self._buf = np.zeros(0, dtype=np.uint32)
+        self._pos = 0
+        if target % 16:
+            self._words(16)  # refill with the block holding the target
+            self._pos = target % 16
 
     def next_u32(self):
         return int(self._words(1)[0])

@@ -1,0 +1,182 @@
+"""Proof serving with continuous batching.
+
+This is the request loop of the reference's proof server
+(proof-server/src/prover_backend.rs:88-107 enters proof execution per
+request; transient-crypto/src/proofs.rs:196-230 selects the accelerator).
+It is rebuilt around one GPU:
+
+  * every circuit's proving key (fixed columns, cosets, permutation data)
+    and the SRS bases of every size stay resident on the device, and are
+    built once when the server starts;
+  * `slots` worker threads each own an execution lane, which has its own
+    CUDA stream, so the kernels of proofs in flight overlap on the device
+    and their host steps overlap with other proofs' device work;
+  * admission is continuous. A request starts as soon as a worker is free
+    and its estimated device footprint fits in what is left of the HBM
+    budget. The oldest waiting request that fits goes first, and nothing
+    waits for a batch to fill;
+  * each request's bytes depend only on the request (its witness and its
+    prover-rng seed), never on what else is in flight.
+"""
+import collections
+import threading
+import time
+from concurrent.futures import Future
+
+from . import api
+from .kzg import CircuitTranscript
+from .plonk import GpuBackend, create_proof
+from .rng import ChaCha20Rng
+
+
+def proof_footprint_bytes(circuit):
+    """Device bytes one proof of this circuit holds at its peak: extended
+    cosets of the advice, permutation and lookup columns and the numerator;
+    Lagrange and coefficient forms; MSM scratch for the largest batch."""
+    n = circuit.n
+    ext = n * (1 << max(1, (circuit.cs_degree - 2).bit_length()))
+    L, m, sets = circuit.lookups, circuit.m, circuit.permutation_sets
+    ext_cols = m + sets + 3 * L + 2
+    n_cols = 3 * (m + sets + 3 * L) + 12
+    msm_scratch = n * max(m, 4) * 24 * 4
+    return 32 * (ext * ext_cols + n * n_cols) + msm_scratch
+
+
+class Request:
+    __slots__ = ("circuit_id", "witness", "seed", "arrival", "start", "finish", "future", "bytes", "proof")
+
+    def __init__(self, circuit_id, witness, seed, nbytes):
+        self.circuit_id, self.witness, self.seed, self.bytes = circuit_id, witness, seed, nbytes
+        self.arrival = time.perf_counter()
+        self.start = self.finish = None
+        self.future = Future()
+        self.proof = None
+
+
+class ProofServer:
+    """entries: {circuit_id: (params, pk)}; slots: proofs in flight;
+    hbm_budget: bytes the proofs in flight may hold together (None = no
+    limit beyond the slots)."""
+
+    def __init__(self, entries, slots=4, hbm_budget=None, backend_factory=GpuBackend, lane_base=1,
+                 set_lane=api.execution_lane_set):
+        self.entries = entries
+        self.slots = slots
+        self.budget = hbm_budget
+        self.backends = {cid: backend_factory(params) for cid, (params, _) in entries.items()}
+        for params, _ in entries.values():
+            if hasattr(params, "context"):
+                params.context(True)
+                params.context(False)
+        self._pending = collections.deque()
+        self._cv = threading.Condition()
+        self._in_use = 0
+        self._running = 0
+        self.peak_in_use = 0
+        self.peak_running = 0
+        self._stop = False
+        self._set_lane = set_lane
+        self.completed = []
+        self._workers = [threading.Thread(target=self._worker, args=(lane_base + i,), daemon=True)
+                         for i in range(slots)]
+        for t in self._workers:
+            t.start()
+
+    def submit(self, circuit_id, witness, seed):
+        params, pk = self.entries[circuit_id]
+        req = Request(circuit_id, witness, seed, proof_footprint_bytes(pk.circuit))
+        if self.budget is not None and req.bytes > self.budget:
+            raise ValueError("request needs more device memory than the whole budget")
+        with self._cv:
+            self._pending.append(req)
+            self._cv.notify_all()
+        return req
+
+    def _take(self):
+        """the oldest pending request that fits in the budget left"""
+        for i, req in enumerate(self._pending):
+            if self.budget is None or self._in_use + req.bytes <= self.budget:
+                del self._pending[i]
+                return req
+        return None
+
+    def _worker(self, lane):
+        if self._set_lane is not None:
+            self._set_lane(lane)
+        while True:
+            with self._cv:
+                while True:
+                    if self._stop and not self._pending:
+                        return
+                    req = self._take()
+                    if req is not None:
+                        break
+                    self._cv.wait()
+                self._in_use += req.bytes
+                self._running += 1
+                self.peak_in_use = max(self.peak_in_use, self._in_use)
+                self.peak_running = max(self.peak_running, self._running)
+            try:
+                params, pk = self.entries[req.circuit_id]
+                req.start = time.perf_counter()
+                req.proof = create_proof(params, pk, req.witness, self.backends[req.circuit_id],
+                                         CircuitTranscript(), ChaCha20Rng.from_label(req.seed))
+                req.finish = time.perf_counter()
+                req.future.set_result(req.proof)
+            except BaseException as e:  # the request fails, the server keeps serving
+                req.finish = time.perf_counter()
+                req.future.set_exception(e)
+            finally:
+                with self._cv:
+                    self._in_use -= req.bytes
+                    self._running -= 1
+                    self.completed.append(req)
+                    self._cv.notify_all()
+
+    def drain(self):
+        """wait until nothing is pending or running"""
+        with self._cv:
+            while self._pending or self._running:
+                self._cv.wait()
+
+    def close(self):
+        with self._cv:
+            self._stop = True
+            self._cv.notify_all()
+        for t in self._workers:
+            t.join()
+
+
+def poisson_arrivals(rng, rate, count):
+    """arrival offsets (seconds) of a Poisson stream; rng a numpy Generator"""
+    gaps = rng.exponential(1.0 / rate, size=count)
+    out, t = [], 0.0
+    for g in gaps:
+        t += g
+        out.append(t)
+    return out
+
+
+def run_stream(server, requests, arrivals):
+    """Submit (circuit_id, witness, seed) requests at the given offsets from
+    now; returns the finished Request objects in submission order."""
+    t0 = time.perf_counter()
+    subs = []
+    for (cid, wit, seed), at in zip(requests, arrivals):
+        delay = t0 + at - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        req = server.submit(cid, wit, seed)
+        req.arrival = t0 + at
+        subs.append(req)
+    for r in subs:
+        r.future.exception()
+    return subs, t0
+
+
+def latency_summary(reqs, t0):
+    lat = sorted((r.finish - r.arrival) for r in reqs)
+    span = max(r.finish for r in reqs) - t0
+    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]  # noqa: E731
+    return {"proofs": len(reqs), "proofs_per_s": len(reqs) / span, "p50_ms": pct(0.5) * 1e3,
+            "p99_ms": pct(0.99) * 1e3, "mean_ms": sum(lat) / len(lat) * 1e3, "makespan_s": span}

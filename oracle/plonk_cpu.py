@@ -147,8 +147,22 @@ class OracleBackend:
         from gb_prover.rng import R2_LIMBS
         return HostPoly(orc.fr_mul_assign(raw, R2_LIMBS))
 
+    def random_mont(self, rng, n):
+        from gb_prover.rng import fr_random
+        return HostPoly(fr_random(rng, n))
+
     def to_host(self, h, n, i):
         return h.a[i * n:(i + 1) * n].copy()
+
+    def permute_lookups(self, comp_h, n, u, L, input_blinds, table_blinds):
+        from gb_prover.plonk import _permute_expression_pair
+        nb = n - u
+        out = []
+        for li in range(L):
+            out += list(_permute_expression_pair(self, self.to_host(comp_h, n, 2 * li), self.to_host(comp_h, n, 2 * li + 1),
+                                                 u, input_blinds[li * nb:(li + 1) * nb],
+                                                 table_blinds[li * nb:(li + 1) * nb]))
+        return HostPoly(np.concatenate(out))
 
     def sort_canonical(self, arr):
         return orc.fr_sort_canonical(arr)

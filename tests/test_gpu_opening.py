@@ -43,3 +43,19 @@ def test_kate_divide(gb, orc, ln, count, zero):
         assert (got[p, ln - 1] == 0).all()
     q.free()
     dv.free()
+
+
+@pytest.mark.parametrize("pre_words,n", [(0, 5000), (6, 4096), (8, 1 << 16), (14, 12345)])
+def test_device_random_draw_matches_host(gb, pre_words, n):
+    """gb_fr_random_chacha20 gives the values fr_random would draw from the
+    same rng state, and the host rng ends at the same word."""
+    from gb_prover.rng import ChaCha20Rng, fr_random
+    a, b = ChaCha20Rng.from_label("draw"), ChaCha20Rng.from_label("draw")
+    a._words(pre_words)
+    b._words(pre_words)
+    want = fr_random(a, n)
+    vec, used = gb.fr_random_chacha20(b.seed, b.word_position(), n)
+    b.skip_words(used)
+    assert (vec.download() == want).all()
+    assert a.word_position() == b.word_position()
+    vec.free()

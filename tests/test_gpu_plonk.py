@@ -52,3 +52,40 @@ def test_config3_full_proof(gb):
     hpk, gproof, hproof = prove_both(config3_circuit())
     assert gproof == hproof
     assert plonk_verify.verify(hpk, gproof, TAU)
+
+
+@pytest.mark.parametrize("u,n,tsize,dup", [(250, 256, 32, False), (4090, 4096, 4000, False), (65529, 65536, 4096, True),
+                                           (1000, 1024, 1, True)])
+def test_device_lookup_permutation_matches_host(gb, orc, u, n, tsize, dup):
+    """gb_fr_lookup_permute_device against the host permute_expression_pair
+    for two lookups at once: small tables with heavy repetition, a table
+    of one value, a full k=16 column."""
+    import numpy as np
+    from oracle.plonk_cpu import OracleBackend
+    rng = np.random.default_rng(u + tsize)
+    cols = []
+    for _ in range(2):
+        table_vals = orc.fr_random(tsize, rng)
+        tab = table_vals[rng.integers(0, tsize, size=n)]
+        tab[:tsize] = table_vals  # every table value present
+        pick = rng.integers(0, min(tsize, 7) if dup else tsize, size=n)
+        inp = table_vals[pick]
+        cols += [inp, tab]
+    comp = np.concatenate(cols)
+    nb = n - u
+    ib, tb = orc.fr_random(2 * nb, rng), orc.fr_random(2 * nb, rng)
+    want = OracleBackend(None).permute_lookups(OracleBackend(None).put(comp), n, u, 2, ib, tb).a
+    got = gb.fr_lookup_permute_device(gb.Bls12_381FrDeviceVec.upload(comp), n, u, 2, ib, tb).download()
+    assert (got == want).all()
+
+
+def test_device_lookup_permutation_rejects_missing_input(gb, orc):
+    import numpy as np
+    rng = np.random.default_rng(3)
+    n, u = 256, 250
+    tab = orc.fr_random(n, rng)
+    inp = tab.copy()
+    inp[17] = orc.fr_random(1, rng)[0]
+    with pytest.raises(gb.MsmError):
+        gb.fr_lookup_permute_device(gb.Bls12_381FrDeviceVec.upload(np.concatenate([inp, tab])), n, u, 1,
+                                    orc.fr_random(n - u, rng), orc.fr_random(n - u, rng))

@@ -1,0 +1,36 @@
+"""Proof serving on the GPU: proofs made by the continuous-batching server
+(several lanes in flight) are byte-identical to the same requests proved
+alone, and the HBM budget bounds the proofs in flight."""
+import numpy as np
+import pytest
+
+from plonk_cases import TAU, circuit
+
+from gb_prover import plonk, serve
+from gb_prover.kzg import CircuitTranscript, ParamsKZG
+from gb_prover.rng import ChaCha20Rng, ints_to_mont
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_serving_mix_equals_alone(gb):
+    srs = ParamsKZG.unsafe_setup(10, plonk.fr_mont(TAU))
+    entries, wit = {}, {}
+    for cid, shape in enumerate([(8, 3, 3, 0), (9, 3, 3, 1), (10, 4, 5, 2)]):
+        c = circuit(*shape)
+        fixed, advice, copies = c.synthesize()
+        p = srs.downsize(c.k)
+        entries[cid] = (p, plonk.keygen(p, c, plonk.GpuBackend(p), fixed, copies))
+        wit[cid] = ints_to_mont([v for col in advice for v in col])
+    sizes = [serve.proof_footprint_bytes(pk.circuit) for _, pk in entries.values()]
+    budget = 2 * max(sizes)
+    rng = np.random.default_rng(9)
+    reqs = [(int(c), wit[int(c)], "r%d" % i) for i, c in enumerate(rng.integers(0, 3, size=24))]
+    srv = serve.ProofServer(entries, slots=4, hbm_budget=budget)
+    done, _ = serve.run_stream(srv, reqs, serve.poisson_arrivals(rng, 500.0, len(reqs)))
+    srv.close()
+    assert srv.peak_in_use <= budget
+    for (cid, w, seed), r in zip(reqs, done):
+        p, pk = entries[cid]
+        alone = plonk.create_proof(p, pk, w, plonk.GpuBackend(p), CircuitTranscript(), ChaCha20Rng.from_label(seed))
+        assert r.future.result() == alone

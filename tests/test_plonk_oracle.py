@@ -47,6 +47,25 @@ def test_fr_random_rejection_stream():
     assert all(v < R for v in mont_to_ints(a))
 
 
+def test_rng_word_position_and_skip():
+    a = ChaCha20Rng.from_label("skip")
+    b = ChaCha20Rng.from_label("skip")
+    a.next_u64_array(3)
+    for count in (0, 1, 5, 16, 17, 300, 5000):
+        want = a._words(count).copy() if count else None
+        b.skip_words(0)
+        pos = b.word_position()
+        b.skip_words(count)
+        assert b.word_position() == pos + count
+        if count:
+            c = ChaCha20Rng.from_label("skip")
+            c.skip_words(pos)
+            assert (c._words(count) == want).all()
+        b = ChaCha20Rng.from_label("skip")
+        b.skip_words(a.word_position())
+        assert [b.next_u32() for _ in range(3)] == [a.next_u32() for _ in range(3)]
+
+
 def test_graph_matches_expression(orc):
     """The compiled gate graph, run by the oracle's graph interpreter, equals
     the expression evaluated on the host, row by row."""
