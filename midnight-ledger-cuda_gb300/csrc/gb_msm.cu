@@ -38,13 +38,17 @@ static constexpr int kMaxWindowBits = 16;  // 2^15 u32 counters = 128 KB smem
 
 static int windows_for(int c) { return 255 / c + 1; }
 
-// Window size: minimise mixed additions plus bucket-reduction additions.
+// Window size: minimise mixed additions plus bucket-reduction additions,
+// over the sizes whose top window keeps at least 5 of the scalar's 255 bits
+// (8, 10, 13, 16).  With fewer, nearly every point's top digit falls in a
+// handful of buckets, which then span thousands of accumulation chunks.
 static int choose_window(size_t n, bool precomputed)
 {
     if (n <= 1) return 8;
     int best = 8;
     double best_cost = 1e300;
     for (int c = 8; c <= kMaxWindowBits; c++) {
+        if (255 % c < 5) continue;
         double w = windows_for(c);
         double adds = (double)n * w;
         double red = (precomputed ? 1.0 : w) * std::ldexp(1.0, c) * 1.4;
@@ -334,10 +338,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) msm_accumulate_kernel(
     if (open) tail[t] = acc;
 }
 
-// 7. buckets spanning several chunks; empty buckets become infinity
+// 7. buckets spanning several chunks; empty buckets become infinity.  A
+//    bucket spanning up to kShortSpan chunks is summed by its own thread;
+//    longer ones (skewed digit distributions: a sparse top window,
+//    structured scalars) are appended to `longs` for msm_fixup_long_kernel.
+static constexpr uint32_t kShortSpan = 32;
+
 __global__ void msm_fixup_kernel(const uint32_t *__restrict__ starts, uint32_t G, uint32_t L,
                                  const xyzz_t *__restrict__ head, const xyzz_t *__restrict__ tail,
-                                 xyzz_t *__restrict__ buckets)
+                                 xyzz_t *__restrict__ buckets, uint32_t *__restrict__ longs,
+                                 uint32_t *__restrict__ nlong)
 {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
@@ -348,10 +358,47 @@ __global__ void msm_fixup_kernel(const uint32_t *__restrict__ starts, uint32_t G
     }
     uint32_t cs = s / L, ce = (e - 1) / L;
     if (cs == ce) return;
+    if (ce - cs > kShortSpan) {
+        longs[atomicAdd(nlong, 1u)] = g;
+        return;
+    }
     xyzz_t acc = tail[cs];
     for (uint32_t c = cs + 1; c < ce; c++) acc.add(tail[c]);
     acc.add(head[ce]);
     buckets[g] = acc;
+}
+
+// 7b. long buckets, one block each (grid-stride over the list): every
+//     thread sums a strided share of the bucket's chunk partials, then a
+//     shared-memory tree adds the 256 shares
+__global__ void __launch_bounds__(256) msm_fixup_long_kernel(const uint32_t *__restrict__ starts, uint32_t L,
+                                                            const xyzz_t *__restrict__ head,
+                                                            const xyzz_t *__restrict__ tail,
+                                                            const uint32_t *__restrict__ longs,
+                                                            const uint32_t *__restrict__ nlong,
+                                                            xyzz_t *__restrict__ buckets)
+{
+    __shared__ xyzz_t sh[256];
+    const uint32_t count = *nlong;
+    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const uint32_t g = longs[i];
+        const uint32_t cs = starts[g] / L, ce = (starts[g + 1] - 1) / L;
+        // partials: tail[cs], tail[cs+1 .. ce-1], head[ce]
+        xyzz_t acc = xyzz_t::inf();
+        for (uint32_t c = cs + threadIdx.x; c <= ce; c += blockDim.x) acc.add(c == ce ? head[c] : tail[c]);
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (uint32_t off = 128; off > 0; off >>= 1) {
+            if (threadIdx.x < off) {
+                xyzz_t v = sh[threadIdx.x];
+                v.add(sh[threadIdx.x + off]);
+                sh[threadIdx.x] = v;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) buckets[g] = sh[0];
+        __syncthreads();
+    }
 }
 
 // 8a. per (segment, sub-segment): U = sum_{k in sub} (k+1) B_k
@@ -566,8 +613,16 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     }
     GB_CHECK_LAUNCH();
     timed_end(tok, s, GB_SLOT_MSM_ACCUMULATE);
-    msm_fixup_kernel<<<blocks_for(G, 128), 128, 0, s>>>(starts, G, L, head, tail, buckets);
-    GB_CHECK_LAUNCH();
+    {
+        dev_buf<uint32_t> longs(G, s), nlong(1, s);
+        GB_CUDA_OK(cudaMemsetAsync(nlong.get(), 0, sizeof(uint32_t), s));
+        msm_fixup_kernel<<<blocks_for(G, 128), 128, 0, s>>>(starts, G, L, head, tail, buckets, longs, nlong);
+        GB_CHECK_LAUNCH();
+        int sms = 0;
+        GB_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, current_device()));
+        msm_fixup_long_kernel<<<(unsigned)sms * 2, 256, 0, s>>>(starts, L, head, tail, longs, nlong, buckets);
+        GB_CHECK_LAUNCH();
+    }
     msm_reduce_partial_kernel<<<blocks_for((size_t)nseg * S, 128), 128, 0, s>>>(buckets, K, S, nseg, partial);
     GB_CHECK_LAUNCH();
     {
@@ -659,10 +714,11 @@ static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *
     timed_collect();
 }
 
-// MSMs below this size skip the context's precomputed windows: a
-// precomputed MSM always pays for 2^(c-1) buckets (c = 16 at full size),
-// while a small plain MSM with its own small window pays far less.
-static constexpr size_t kPrecomputedMin = (size_t)1 << 13;
+// An MSM far smaller than the context's bucket count (2^(c-1)) skips the
+// precomputed windows: a precomputed MSM always pays for all the buckets,
+// while a small plain MSM with its own small window pays far less.  Below
+// this ratio of points to buckets the plain path is taken.
+static constexpr size_t kPrecomputedMinRatio = 8;
 
 // A batch against the context; results to the host.  Large items use the
 // precomputed table; small ones run as one plain batch over table row 0 (the
@@ -675,7 +731,7 @@ static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const st
     std::vector<size_t> big_idx, small_idx;
     size_t small_max = 0;
     for (size_t i = 0; i < items.size(); i++) {
-        if (items[i].n >= kPrecomputedMin || items.size() == 1) {
+        if (items[i].n * kPrecomputedMinRatio >= ((size_t)1 << (ctx->c - 1)) || items.size() == 1) {
             big.push_back(items[i]);
             big_idx.push_back(i);
         } else {

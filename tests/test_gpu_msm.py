@@ -215,3 +215,37 @@ def test_batch_plain_matches_single_calls(gb, orc):
     for i in range(5):
         assert (affine_of(orc, got[i]) == affine_of(orc, gb.bls12_381_g1_msm(b, sb[i]))).all()
         assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all()
+
+
+@pytest.mark.parametrize("kind", ["ones", "two_values", "sparse_small"])
+def test_skewed_buckets(gb, orc, kind):
+    """Digit distributions that pile most points into a few buckets (every
+    scalar 1, two values, small values): long buckets are summed in
+    parallel and the result equals the oracle's, for the plain path and the
+    precomputed context path."""
+    rng = np.random.default_rng(31)
+    n = 1 << 16
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    if kind == "ones":
+        s = orc.fr_from_ints([1] * n)
+    elif kind == "two_values":
+        s = orc.fr_from_ints([int(v) for v in rng.choice([3, 5], size=n)])
+    else:
+        s = orc.fr_from_ints([int(v) for v in rng.integers(0, 16, size=n)])
+    want = affine_of(orc, orc.g1_msm(b, s))
+    assert (affine_of(orc, gb.bls12_381_g1_msm(b, s)) == want).all()
+    ctx = gb.Bls12_381G1MsmContext(b)
+    assert (affine_of(orc, ctx.msm(s)) == want).all()
+    ctx.close()
+
+
+def test_sparse_top_window_config(gb, orc):
+    """window_bits 15: the 18th window holds only the carry out of bit 254,
+    so about half the points share one bucket of the top window."""
+    rng = np.random.default_rng(15)
+    n = 1 << 15
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    s = orc.fr_random(n, rng)
+    ctx = gb.Bls12_381G1MsmContext(b, gb.RawMsmConfig.default(n, 15))
+    assert (affine_of(orc, ctx.msm(s)) == affine_of(orc, orc.g1_msm(b, s))).all()
+    ctx.close()
