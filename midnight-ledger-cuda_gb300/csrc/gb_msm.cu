@@ -401,23 +401,40 @@ __global__ void __launch_bounds__(256) msm_fixup_long_kernel(const uint32_t *__r
     }
 }
 
-// 8a. per (segment, sub-segment): U = sum_{k in sub} (k+1) B_k
-__global__ void msm_reduce_partial_kernel(const xyzz_t *__restrict__ buckets, uint32_t K, uint32_t S,
-                                          uint32_t nseg, xyzz_t *__restrict__ partial)
+// 8a. per (segment, sub-segment): U = sum_{k in sub} (k+1) B_k; then each
+//     aligned group of min(S, 128) sub-segments of a block is summed in
+//     shared memory, so `partial` holds nseg * S / group points
+__global__ void __launch_bounds__(128) msm_reduce_partial_kernel(const xyzz_t *__restrict__ buckets, uint32_t K,
+                                                                 uint32_t S, uint32_t nseg,
+                                                                 xyzz_t *__restrict__ partial)
 {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nseg * S) return;
-    uint32_t seg = t / S, s = t % S;
-    uint32_t m = K / S;
-    uint32_t k0 = s * m;
-    const xyzz_t *B = buckets + (size_t)seg * K;
-    xyzz_t run = xyzz_t::inf(), sum = xyzz_t::inf();
-    for (uint32_t k = k0 + m; k-- > k0;) {
-        run.add(B[k]);
-        sum.add(run);
+    __shared__ xyzz_t sh[128];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    xyzz_t sum = xyzz_t::inf();
+    if (t < nseg * S) {
+        uint32_t seg = t / S, s = t % S;
+        uint32_t m = K / S;
+        uint32_t k0 = s * m;
+        const xyzz_t *B = buckets + (size_t)seg * K;
+        xyzz_t run = xyzz_t::inf();
+        for (uint32_t k = k0 + m; k-- > k0;) {
+            run.add(B[k]);
+            sum.add(run);
+        }
+        if (k0) sum.add(xyzz_mul_small(run, k0));
     }
-    if (k0) sum.add(xyzz_mul_small(run, k0));
-    partial[t] = sum;
+    sh[threadIdx.x] = sum;
+    __syncthreads();
+    const uint32_t group = S < 128 ? S : 128;
+    for (uint32_t off = group / 2; off > 0; off >>= 1) {
+        if ((threadIdx.x & (group - 1)) < off) {
+            xyzz_t v = sh[threadIdx.x];
+            v.add(sh[threadIdx.x + off]);
+            sh[threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+    if ((threadIdx.x & (group - 1)) == 0 && t < nseg * S) partial[t / group] = sh[threadIdx.x];
 }
 
 // 8b. tree sum: out[seg * gridDim.x + b] = sum of the 512-element slice b of
@@ -626,9 +643,9 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     msm_reduce_partial_kernel<<<blocks_for((size_t)nseg * S, 128), 128, 0, s>>>(buckets, K, S, nseg, partial);
     GB_CHECK_LAUNCH();
     {
-        // tree-sum each segment's S partials down to one point
+        // tree-sum each segment's S / group partials down to one point
         const xyzz_t *src = partial;
-        uint32_t len = S;
+        uint32_t len = S / std::min<uint32_t>(S, 128);
         dev_buf<xyzz_t> tmp_a, tmp_b;
         bool use_a = true;
         while (len > 1) {

@@ -251,12 +251,48 @@ __global__ void power_factors_kernel(fr_t *d, fr_t w, size_t n)
     if (i < n) d[i] = i ? w : fr_t::one();
 }
 
+// Power tables up to 2^24 entries: w^i = T0[i & 255] * T1[(i >> 8) & 255] *
+// T2[i >> 16], where T0[j] = w^j, T1[j] = w^(256 j), T2[j] = w^(65536 j).
+// One block builds the three 256-entry tables with block scans (exclusive:
+// T[j] = base^j); the apply kernel spends two products per element.
+__global__ void __launch_bounds__(256) power_tables_kernel(fr_t w, fr_t *__restrict__ tables)
+{
+    __shared__ fr_t sh[256];
+    fr_t base = w;
+    for (int level = 0; level < 3; level++) {
+        fr_t incl = block_scan_mul(base, sh);  // base^(t+1)
+        __syncthreads();
+        tables[level * 256 + threadIdx.x] = threadIdx.x ? sh[threadIdx.x - 1] : fr_t::one();
+        base = sh[255];  // base^256, the next level's base
+        __syncthreads();
+        (void)incl;
+    }
+}
+
+__global__ void power_apply_kernel(const fr_t *__restrict__ tables, size_t n, fr_t *__restrict__ d)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    fr_t v = tables[i & 255];
+    if (i >> 8) v = v * tables[256 + ((i >> 8) & 255)];
+    if (i >> 16) v = v * tables[512 + (i >> 16)];
+    d[i] = v;
+}
+
 void omega_powers(fr_t *d, const fr_t &w, size_t n, cudaStream_t s)
 {
     if (!n) return;
-    power_factors_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d, w, n);
+    if (n > ((size_t)1 << 24)) {
+        power_factors_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d, w, n);
+        GB_CHECK_LAUNCH();
+        prefix_product(d, d, n, s);
+        return;
+    }
+    dev_buf<fr_t> tables(3 * 256, s);
+    power_tables_kernel<<<1, 256, 0, s>>>(w, tables);
     GB_CHECK_LAUNCH();
-    prefix_product(d, d, n, s);
+    power_apply_kernel<<<blocks_for(n, 256), 256, 0, s>>>(tables, n, d);
+    GB_CHECK_LAUNCH();
 }
 
 // ------------------------------------------------------------ products

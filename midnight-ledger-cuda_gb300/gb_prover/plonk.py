@@ -645,16 +645,17 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
                                           w(dom.omega), deltas, perm_blinds, bf)
     if L:
         z_lk = backend.lookup_products(comp, perm_l, n, L, w(beta), w(gamma), lk_blinds, bf)
-    for cm in backend.commit_lagrange(z_perm, n, sets):
-        transcript.write_point(cm)
-    if L:
-        for cm in backend.commit_lagrange(z_lk, n, L):
-            transcript.write_point(cm)
-    transcript.squeeze_challenge()  # trash challenge (no trash arguments)
-
-    # ---- vanishing argument: random polynomial (vanishing/prover.rs:41-97)
+    # the vanishing argument's random polynomial (vanishing/prover.rs:41-97)
+    # comes from the rng alone, so its commitment joins the products' in one
+    # batched MSM: committing its Lagrange values against g_lagrange gives the
+    # same point as its coefficients against g
     random_poly = backend.random_mont(rng, n)
-    transcript.write_point(backend.commit(random_poly, n, 1)[0])
+    parts = [z_perm] + ([z_lk] if L else []) + [backend.coeff_to_lagrange(random_poly, k, 1)]
+    cms = backend.commit_lagrange(backend.cat(parts), n, sets + L + 1)
+    for cm in cms[:sets + L]:
+        transcript.write_point(cm)
+    transcript.squeeze_challenge()  # trash challenge (no trash arguments)
+    transcript.write_point(cms[sets + L])
     y = fr_int(transcript.squeeze_challenge())
 
     # ---- quotient (prover.rs:1743-1990, evaluation.rs:3114-3528)
@@ -846,6 +847,12 @@ class GpuBackend:
         out = h.gather_polys(1 << k, list(range(count)))
         one = fr_mont(1)
         out.ntt_zeta_batch(k, count, True, one, one, one)
+        return out
+
+    def coeff_to_lagrange(self, h, k, count):
+        out = h.gather_polys(1 << k, list(range(count)))
+        one = fr_mont(1)
+        out.ntt_zeta_batch(k, count, False, one, one, one)
         return out
 
     def coeff_to_extended(self, h, k, count, ek):

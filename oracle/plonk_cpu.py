@@ -105,6 +105,11 @@ class OracleBackend:
         return HostPoly(np.concatenate([orc.fr_ntt(h.a[i * n:(i + 1) * n], k, True, self.threads)
                                         for i in range(count)]))
 
+    def coeff_to_lagrange(self, h, k, count):
+        n = 1 << k
+        return HostPoly(np.concatenate([orc.fr_ntt(h.a[i * n:(i + 1) * n], k, False, self.threads)
+                                        for i in range(count)]))
+
     def coeff_to_extended(self, h, k, count, ek):
         from gb_prover.plonk import ZETA
         z1, z2 = ints_to_mont([ZETA, ZETA * ZETA % R])
