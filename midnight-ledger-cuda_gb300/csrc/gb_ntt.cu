@@ -8,6 +8,7 @@
 // DIF output is in bit-reversed order; a final pass permutes it to natural
 // order and applies the optional scale (1/n for the inverse).  Twiddles
 // w^j, j < n/2, are tabulated once per (log_n, direction) and kept resident.
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -79,6 +80,83 @@ __global__ void ntt_dif_pass_kernel(fr_t *data, uint32_t log_n, int s_hi, int g,
         __syncthreads();
     }
     for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x) d[base + ((size_t)t << s_lo)] = sm[t];
+}
+
+// The same pass with E = 2^EL elements per thread: the pass's g stages run
+// in groups of up to EL (radix-E steps).  For a group over local bits
+// [B, B + R), thread u holds the E elements whose local index has, outside
+// those bits, the value (u << (EL - R)) | (k >> R), and k & (2^R - 1) inside
+// them; it runs the group's R stages in registers, and the block exchanges
+// through shared memory between groups.  Needs g >= EL (2^g / E threads).
+// Shared memory is padded with one element per 8 (position t + t/8) so the
+// strided gathers of the low groups spread over all banks.
+__device__ __forceinline__ uint32_t ntt_pad(uint32_t t) { return t + (t >> 3); }
+
+template <int EL, int R>
+__device__ __forceinline__ void ntt_reg_group(fr_t *sm, uint32_t u, int B, int s_lo, size_t lo, uint32_t log_n,
+                                              const fr_t *__restrict__ tw)
+{
+    constexpr int E = 1 << EL;
+    uint32_t tl[E];
+    fr_t x[E];
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+        const uint32_t rest = (u << (EL - R)) | ((uint32_t)k >> R);
+        const uint32_t klo = (uint32_t)k & ((1u << R) - 1);
+        tl[k] = (rest & ((1u << B) - 1)) | (klo << B) | ((rest >> B) << (B + R));
+        x[k] = sm[ntt_pad(tl[k])];
+    }
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+        const int p = B + R - 1 - st;  // local bit of this stage
+        const int sidx = s_lo + p;     // global stage
+        const int hk = 1 << (R - 1 - st);
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            if ((k & hk) == 0) {
+                const int k1 = k + hk;
+                const size_t j = ((size_t)(tl[k] & ((1u << p) - 1)) << s_lo) + lo;
+                const fr_t a = x[k], c = x[k1];
+                x[k] = a + c;
+                fr_t diff = a - c;
+                if (j) diff = diff * tw[j << (log_n - 1 - sidx)];
+                x[k1] = diff;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < E; k++) sm[ntt_pad(tl[k])] = x[k];
+}
+
+template <int EL>
+__global__ void ntt_dif_pass_reg_kernel(fr_t *data, uint32_t log_n, int s_hi, int g, const fr_t *__restrict__ tw)
+{
+    extern __shared__ fr_t sm[];
+    const int s_lo = s_hi - g + 1;
+    const size_t n = (size_t)1 << log_n;
+    fr_t *d = data + (size_t)blockIdx.y * n;
+    const size_t b = blockIdx.x;
+    const size_t lo = b & (((size_t)1 << s_lo) - 1);
+    const size_t hi = b >> s_lo;
+    const size_t base = (hi << (s_hi + 1)) + lo;
+    const uint32_t cnt = 1u << g;
+    for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x) sm[ntt_pad(t)] = d[base + ((size_t)t << s_lo)];
+    __syncthreads();
+    int top = g;  // local bits still to process: [0, top)
+    while (top > 0) {
+        if (top >= EL) {
+            ntt_reg_group<EL, EL>(sm, threadIdx.x, top - EL, s_lo, lo, log_n, tw);
+            top -= EL;
+        } else if (EL == 3 && top == 2) {
+            ntt_reg_group<EL, (EL == 3 ? 2 : 1)>(sm, threadIdx.x, 0, s_lo, lo, log_n, tw);
+            top = 0;
+        } else {
+            ntt_reg_group<EL, 1>(sm, threadIdx.x, 0, s_lo, lo, log_n, tw);
+            top = 0;
+        }
+        __syncthreads();
+    }
+    for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x) d[base + ((size_t)t << s_lo)] = sm[ntt_pad(t)];
 }
 
 __device__ __forceinline__ size_t bitrev_n(size_t x, uint32_t bits)
@@ -182,6 +260,10 @@ void set_ntt_smem()
     std::call_once(once, [] {
         cudaFuncSetAttribute(ntt_dif_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (1 << kPassBits) * (int)sizeof(fr_t));
+        cudaFuncSetAttribute(ntt_dif_pass_reg_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (1 << kPassBits) / 8 * 9 * (int)sizeof(fr_t));
+        cudaFuncSetAttribute(ntt_dif_pass_reg_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (1 << kPassBits) / 8 * 9 * (int)sizeof(fr_t));
     });
 }
 }  // namespace
@@ -197,9 +279,24 @@ void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t
         while (s_hi >= 0) {
             int g = s_hi + 1 < kPassBits ? s_hi + 1 : kPassBits;
             uint32_t cnt = 1u << g;
-            unsigned threads = cnt / 2 < 512 ? (cnt / 2 ? cnt / 2 : 1) : 512;
             dim3 grid((unsigned)(n >> g), (unsigned)count);
-            ntt_dif_pass_kernel<<<grid, threads, cnt * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+            // elements per thread: 4 (radix-4 register steps) from 2^18 up,
+            // where it is fastest on GB300; below that the radix-2 pass with
+            // 512 threads keeps more warps resident.  GB_NTT_ELEMS_LOG
+            // (1, 2, 3) overrides for measurement.
+            static const int el_env = [] {
+                const char *e = getenv("GB_NTT_ELEMS_LOG");
+                return e && (e[0] == '1' || e[0] == '2' || e[0] == '3') ? e[0] - '0' : 0;
+            }();
+            const int el = el_env ? el_env : (log_n >= 18 ? 2 : 1);
+            if (g >= 3 && el == 3) {
+                ntt_dif_pass_reg_kernel<3><<<grid, cnt / 8, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+            } else if (g >= 3 && el == 2) {
+                ntt_dif_pass_reg_kernel<2><<<grid, cnt / 4, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+            } else {
+                unsigned threads = cnt / 2 ? cnt / 2 : 1;
+                ntt_dif_pass_kernel<<<grid, threads, cnt * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+            }
             GB_CHECK_LAUNCH();
             s_hi -= g;
         }
