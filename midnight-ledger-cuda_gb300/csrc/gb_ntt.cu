@@ -8,6 +8,9 @@
 // DIF output is in bit-reversed order; a final pass permutes it to natural
 // order and applies the optional scale (1/n for the inverse).  Twiddles
 // w^j, j < n/2, are tabulated once per (log_n, direction) and kept resident.
+// Within a pass, either each thread runs one radix-2 butterfly per stage
+// (a barrier per stage), or each thread holds 4 or 8 elements and runs 2 or 3
+// stages in registers between exchanges through shared memory.
 #include <cstdlib>
 #include <map>
 #include <mutex>
