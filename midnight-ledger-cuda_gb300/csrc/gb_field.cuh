@@ -23,9 +23,14 @@
 #if defined(__CUDACC__)
 #define GB_HD __host__ __device__ __forceinline__
 #define GB_D __device__ __forceinline__
-// out-of-line on the device: for operations off the hot loops, so each kernel
-// does not inline hundreds of carry-chain field products
+// operations off the hot loops (point doubling, full addition, conversions).
+// With the Fp product out of line they inline cheaply; GB_COLD_NOINLINE keeps
+// them as calls.
+#if defined(GB_COLD_NOINLINE)
 #define GB_COLD inline __host__ __device__ __noinline__
+#else
+#define GB_COLD __host__ __device__ __forceinline__
+#endif
 #else
 #define GB_HD inline
 #define GB_D inline
