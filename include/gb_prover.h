@@ -342,6 +342,14 @@ GB_API RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, R
  * bls12_381_g1_msm.cu:1923-1959), into a new device vector */
 GB_API RustError gb_fr_device_kate_divide(void **out, const void *device_vec, size_t poly_len, size_t poly_count,
                                           RawFr point);
+/* Autotuner: when enabled, the plain MSM path times the window sizes
+ * {8, 10, 13, 16} and the NTT its pass variants the first time it meets a
+ * (size, batch, scalar-sparsity) key, and keeps the fastest; off by default */
+GB_API void gb_autotune_set(int enabled);
+GB_API void gb_autotune_reset(void);
+/* "key=value;" per tuned key into buf (NUL-terminated, truncated); returns
+ * the full length */
+GB_API size_t gb_autotune_report(char *buf, size_t len);
 /* measured device throughput of 32x32->64 multiply-adds per second */
 GB_API RustError gb_imad_peak(double *out_per_sec);
 /* cumulative host<->device bytes moved by this library */

@@ -715,6 +715,68 @@ static int plan_window(size_t n, bool precomputed, uint32_t requested)
 
 // Plain MSMs of host bases + host scalars [nmsms][n] (nothing resident):
 // one batch through the engine.
+// Autotuner for the plain path: the key is the size class of the largest
+// item, the batch-size class and the sparsity of a sample of the scalars
+// (zero scalars, scalars below 2^64: both empty the high windows); a new key
+// times every window size with a populated top window on this batch.
+__global__ void scalar_sample_kernel(const fr_t *__restrict__ scalars, size_t n, unsigned *counts)
+{
+    unsigned zero = 0, small = 0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+        fr_t c = scalars[i].from_mont();
+        bool hi_zero = true;
+#pragma unroll
+        for (int k = 2; k < 8; k++) hi_zero &= c.v[k] == 0;
+        if (hi_zero) {
+            if (c.v[0] == 0 && c.v[1] == 0) zero++;
+            else small++;
+        }
+    }
+    atomicAdd(&counts[0], zero);
+    atomicAdd(&counts[1], small);
+}
+
+static int tuned_window(const std::vector<msm_item> &items, const affine_t *points, size_t stride, cudaStream_t s)
+{
+    size_t n_max = 0, total = 0;
+    for (const msm_item &it : items) {
+        n_max = std::max(n_max, it.n);
+        total += it.n;
+    }
+    int c = choose_window(n_max, false);
+    if (!autotune_enabled() || n_max < 256) return c;
+    const msm_item &first = *std::max_element(items.begin(), items.end(),
+                                              [](const msm_item &a, const msm_item &b) { return a.n < b.n; });
+    const size_t sample = std::min<size_t>(first.n, 4096);
+    dev_buf<unsigned> counts(2, s);
+    GB_CUDA_OK(cudaMemsetAsync(counts.get(), 0, 2 * sizeof(unsigned), s));
+    scalar_sample_kernel<<<1, 256, 0, s>>>(first.scalars, sample, counts);
+    GB_CHECK_LAUNCH();
+    unsigned h[2] = {0, 0};
+    d2h(h, counts, sizeof(h), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    auto cls = [&](unsigned v) { return v * 20 < sample ? 0 : (v * 10 < sample * 3 ? 1 : 2); };
+    int lg = 0;
+    while (((size_t)1 << (lg + 1)) <= n_max) lg++;
+    const size_t nitems = items.size();
+    const int bclass = nitems == 1 ? 0 : nitems <= 8 ? 1 : nitems <= 64 ? 2 : 3;
+    const std::string key = "msm:2^" + std::to_string(lg) + ":b" + std::to_string(bclass) + ":z" +
+                            std::to_string(cls(h[0])) + ":s" + std::to_string(cls(h[1]));
+    if (autotune_lookup(key, &c)) return c;
+    dev_buf<jacobian_t> scratch(nitems, s);
+    float best = 1e30f;
+    for (int cand : {8, 10, 13, 16}) {
+        if (cand > kMaxWindowBits || ((size_t)1 << (cand - 1)) > 8 * total) continue;
+        float ms = time_on_stream(s, [&] { msm_run_batch(items, cand, false, points, stride, scratch, s); });
+        if (ms < best) {
+            best = ms;
+            c = cand;
+        }
+    }
+    autotune_store(key, c);
+    return c;
+}
+
 static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *scalars, size_t n, size_t nmsms)
 {
     cudaStream_t s = lane_stream();
@@ -725,7 +787,7 @@ static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *
     h2d(d_scalars, scalars, n * nmsms * sizeof(fr_t), s);
     std::vector<msm_item> items;
     for (size_t m = 0; m < nmsms; m++) items.push_back(msm_item{d_scalars.get() + m * n, n, 0});
-    msm_run_batch(items, choose_window(n, false), false, d_points, 0, d_out, s);
+    msm_run_batch(items, tuned_window(items, d_points, 0, s), false, d_points, 0, d_out, s);
     d2h(out, d_out, nmsms * sizeof(jacobian_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
     timed_collect();
@@ -759,7 +821,7 @@ static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const st
     }
     dev_buf<jacobian_t> d_big(std::max<size_t>(big.size(), 1), s), d_small(std::max<size_t>(small.size(), 1), s);
     if (!big.empty()) msm_run_batch(big, ctx->c, true, ctx->table, ctx->npoints, d_big, s);
-    if (!small.empty()) msm_run_batch(small, choose_window(small_max, false), false, ctx->table, 0, d_small, s);
+    if (!small.empty()) msm_run_batch(small, tuned_window(small, ctx->table, 0, s), false, ctx->table, 0, d_small, s);
     std::vector<jacobian_t> hb(big.size()), hs(small.size());
     d2h(hb.data(), d_big, big.size() * sizeof(jacobian_t), s);
     d2h(hs.data(), d_small, small.size() * sizeof(jacobian_t), s);

@@ -271,6 +271,60 @@ void set_ntt_smem()
 }
 }  // namespace
 
+// the DIF passes of `count` transforms in place; el = log2(elements per
+// thread) of the register-blocked pass (1 = one butterfly per thread)
+static void ntt_passes(fr_t *d, uint32_t log_n, size_t count, const fr_t *tw, int el, cudaStream_t s)
+{
+    const size_t n = (size_t)1 << log_n;
+    int s_hi = (int)log_n - 1;
+    while (s_hi >= 0) {
+        int g = s_hi + 1 < kPassBits ? s_hi + 1 : kPassBits;
+        uint32_t cnt = 1u << g;
+        dim3 grid((unsigned)(n >> g), (unsigned)count);
+        if (g >= 3 && el == 3) {
+            ntt_dif_pass_reg_kernel<3><<<grid, cnt / 8, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+        } else if (g >= 3 && el == 2) {
+            ntt_dif_pass_reg_kernel<2><<<grid, cnt / 4, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+        } else {
+            unsigned threads = cnt / 2 < 512 ? (cnt / 2 ? cnt / 2 : 1) : 512;
+            ntt_dif_pass_kernel<<<grid, threads, cnt * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
+        }
+        GB_CHECK_LAUNCH();
+        s_hi -= g;
+    }
+}
+
+// Pass variant: 4 elements per thread (radix-4 register steps) from 2^18 up,
+// where it is fastest on GB300; below that the radix-2 pass with up to 512
+// threads keeps more warps resident.  GB_NTT_ELEMS_LOG (1, 2, 3) overrides;
+// with the autotuner on, each size times the three variants once on a
+// scratch copy of one transform.
+static int ntt_variant(fr_t *d, uint32_t log_n, const fr_t *tw, cudaStream_t s)
+{
+    static const int el_env = [] {
+        const char *e = getenv("GB_NTT_ELEMS_LOG");
+        return e && (e[0] == '1' || e[0] == '2' || e[0] == '3') ? e[0] - '0' : 0;
+    }();
+    if (el_env) return el_env;
+    int el = log_n >= 18 ? 2 : 1;
+    if (!autotune_enabled() || log_n < 10) return el;
+    const std::string key = "ntt:2^" + std::to_string(log_n);
+    if (autotune_lookup(key, &el)) return el;
+    const size_t n = (size_t)1 << log_n;
+    dev_buf<fr_t> scratch(n, s);
+    float best = 1e30f;
+    for (int cand = 1; cand <= 3; cand++) {
+        GB_CUDA_OK(cudaMemcpyAsync(scratch.get(), d, n * sizeof(fr_t), cudaMemcpyDeviceToDevice, s));
+        float ms = time_on_stream(s, [&] { ntt_passes(scratch, log_n, 1, tw, cand, s); });
+        if (ms < best) {
+            best = ms;
+            el = cand;
+        }
+    }
+    autotune_store(key, el);
+    return el;
+}
+
 void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, cudaStream_t s)
 {
     if (count == 0) return;
@@ -278,31 +332,7 @@ void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t
     if (log_n > 0) {
         set_ntt_smem();
         const fr_t *tw = twiddles(log_n, inverse, s);
-        int s_hi = (int)log_n - 1;
-        while (s_hi >= 0) {
-            int g = s_hi + 1 < kPassBits ? s_hi + 1 : kPassBits;
-            uint32_t cnt = 1u << g;
-            dim3 grid((unsigned)(n >> g), (unsigned)count);
-            // elements per thread: 4 (radix-4 register steps) from 2^18 up,
-            // where it is fastest on GB300; below that the radix-2 pass with
-            // 512 threads keeps more warps resident.  GB_NTT_ELEMS_LOG
-            // (1, 2, 3) overrides for measurement.
-            static const int el_env = [] {
-                const char *e = getenv("GB_NTT_ELEMS_LOG");
-                return e && (e[0] == '1' || e[0] == '2' || e[0] == '3') ? e[0] - '0' : 0;
-            }();
-            const int el = el_env ? el_env : (log_n >= 18 ? 2 : 1);
-            if (g >= 3 && el == 3) {
-                ntt_dif_pass_reg_kernel<3><<<grid, cnt / 8, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
-            } else if (g >= 3 && el == 2) {
-                ntt_dif_pass_reg_kernel<2><<<grid, cnt / 4, cnt / 8 * 9 * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
-            } else {
-                unsigned threads = cnt / 2 ? cnt / 2 : 1;
-                ntt_dif_pass_kernel<<<grid, threads, cnt * sizeof(fr_t), s>>>(d, log_n, s_hi, g, tw);
-            }
-            GB_CHECK_LAUNCH();
-            s_hi -= g;
-        }
+        ntt_passes(d, log_n, count, tw, ntt_variant(d, log_n, tw, s), s);
     }
     dim3 grid(blocks_for(n, 256), (unsigned)count);
     bitrev_scale_kernel<<<grid, 256, 0, s>>>(d, log_n, scale != nullptr, scale ? *scale : fr_t::one());

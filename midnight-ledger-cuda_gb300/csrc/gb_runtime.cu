@@ -1,6 +1,10 @@
 // Host runtime: lanes, stream-ordered memory, device vectors, transfer
 // counters and the lane / device-vector entry points of the C ABI.
 #include <atomic>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -196,7 +200,58 @@ void timed_collect()
 
 using namespace gb;
 
+// ---------------------------------------------------------------- autotuner
+namespace {
+std::atomic<bool> g_autotune{false};
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+}  // namespace
+
+bool autotune_enabled() { return g_autotune.load(std::memory_order_relaxed); }
+
+bool autotune_lookup(const std::string &key, int *value)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    *value = it->second;
+    return true;
+}
+
+void autotune_store(const std::string &key, int value)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = value;
+}
+
 extern "C" {
+
+void gb_autotune_set(int enabled) { g_autotune.store(enabled != 0); }
+
+void gb_autotune_reset(void)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+
+// "key=value;" for every tuned key, truncated to len - 1 characters;
+// returns the full length
+size_t gb_autotune_report(char *buf, size_t len)
+{
+    std::string out;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (auto &kv : g_tune) out += kv.first + "=" + std::to_string(kv.second) + ";";
+    }
+    if (buf && len) {
+        size_t k = std::min(len - 1, out.size());
+        memcpy(buf, out.data(), k);
+        buf[k] = 0;
+    }
+    return out.size();
+}
+
+
 
 // midnight-sppark-msm/src/bls12_381_g1_msm.cu:134-146
 RustError midnight_sppark_execution_lane_set(uint32_t lane)

@@ -163,6 +163,31 @@ void timed_end(int token, cudaStream_t s, int slot);
 void timed_collect();
 enum { GB_SLOT_MSM_ACCUMULATE = 0, GB_SLOT_MSM_TOTAL = 1, GB_SLOT_NTT = 2, GB_SLOTS = 8 };
 
+// Autotuner: when enabled, an operation with several launch shapes (the MSM
+// window, the NTT pass variant) times its candidates the first time it meets
+// a key and remembers the fastest.  Off by default: the cost models decide.
+bool autotune_enabled();
+bool autotune_lookup(const std::string &key, int *value);
+void autotune_store(const std::string &key, int value);
+
+// elapsed milliseconds of fn() on stream s (CUDA events, synchronises)
+template <class F>
+float time_on_stream(cudaStream_t s, F fn)
+{
+    cudaEvent_t a, b;
+    GB_CUDA_OK(cudaEventCreate(&a));
+    GB_CUDA_OK(cudaEventCreate(&b));
+    GB_CUDA_OK(cudaEventRecord(a, s));
+    fn();
+    GB_CUDA_OK(cudaEventRecord(b, s));
+    GB_CUDA_OK(cudaEventSynchronize(b));
+    float ms = 0;
+    GB_CUDA_OK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
 inline unsigned blocks_for(size_t n, unsigned threads)
 {
     return (unsigned)((n + threads - 1) / threads);

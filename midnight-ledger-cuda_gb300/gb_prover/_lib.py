@@ -138,6 +138,9 @@ def _declare(L):
         "gb_fr_permutation_products_device": (E, [vp, vp, vp, sz, sz, sz, fr, fr, fr, vp, vp, sz]),
         "gb_fr_random_chacha20": (E, [vp, vp, ctypes.c_uint64, sz, vp]),
         "gb_fr_lookup_permute_device": (E, [vp, vp, sz, sz, sz, vp, vp]),
+        "gb_autotune_set": (None, [ctypes.c_int]),
+        "gb_autotune_reset": (None, []),
+        "gb_autotune_report": (sz, [vp, sz]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)

@@ -24,7 +24,7 @@ __all__ = [
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
-    "fr_lookup_permute_device",
+    "fr_lookup_permute_device", "autotune_set", "autotune_reset", "autotune_report",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -572,3 +572,26 @@ def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, inpu
     check(lib().gb_fr_lookup_permute_device(ctypes.byref(h), compressed.raw, length, usable_rows, lookup_count,
                                             _ptr(ib), _ptr(tb)))
     return Bls12_381FrDeviceVec(h)
+
+
+# ---------------------------------------------------------------- autotuner
+
+def autotune_set(enabled=True):
+    lib().gb_autotune_set(1 if enabled else 0)
+
+
+def autotune_reset():
+    lib().gb_autotune_reset()
+
+
+def autotune_report():
+    """{key: chosen value} of every tuned key"""
+    n = lib().gb_autotune_report(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib().gb_autotune_report(buf, n + 1)
+    out = {}
+    for item in buf.value.decode().split(";"):
+        if "=" in item:
+            k, v = item.split("=")
+            out[k] = int(v)
+    return out

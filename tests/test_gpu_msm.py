@@ -249,3 +249,33 @@ def test_sparse_top_window_config(gb, orc):
     ctx = gb.Bls12_381G1MsmContext(b, gb.RawMsmConfig.default(n, 15))
     assert (affine_of(orc, ctx.msm(s)) == affine_of(orc, orc.g1_msm(b, s))).all()
     ctx.close()
+
+
+def test_autotuned_paths_match_oracle(gb, orc):
+    """With the autotuner on, the window and NTT variant it picks change
+    nothing in the results: plain batch, small ragged items, NTTs."""
+    rng = np.random.default_rng(77)
+    gb.autotune_reset()
+    gb.autotune_set(True)
+    try:
+        n = 3000
+        b = gb.g1_generator_mul(orc.fr_random(n, rng))
+        sb = np.stack([_mixed_scalars(orc, n, rng) for _ in range(3)])
+        got = gb.bls12_381_g1_msm_batch(b, sb)
+        for i in range(3):
+            assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all()
+        big = gb.g1_generator_mul(orc.fr_random(1 << 14, rng))
+        ctx = gb.Bls12_381G1MsmContext(big)
+        flat = np.concatenate([_mixed_scalars(orc, 700, rng), _mixed_scalars(orc, 500, rng)])
+        dv = gb.Bls12_381FrDeviceVec.upload(flat)
+        got = ctx.device_ragged(dv, [(0, 0, 700), (700, 100, 500)])
+        assert (affine_of(orc, got[0]) == affine_of(orc, orc.g1_msm(big[:700], flat[:700]))).all()
+        assert (affine_of(orc, got[1]) == affine_of(orc, orc.g1_msm(big[100:600], flat[700:]))).all()
+        ctx.close()
+        for log_n in (12, 18):
+            v = orc.fr_random(1 << log_n, rng)
+            assert (gb.bls12_381_fr_ntt(v, inverse=False) == orc.fr_ntt(v, log_n, False)).all()
+        rep = gb.autotune_report()
+        assert any(k.startswith("msm:") for k in rep) and any(k.startswith("ntt:") for k in rep)
+    finally:
+        gb.autotune_set(False)
