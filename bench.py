@@ -408,6 +408,17 @@ def batched_config(gb, torch, rng):
                                              for lg in vecs])
     out["ntt64_one_at_a_time_ms"] = timed(lambda: [v.ntt_zeta(lg, False, one, one, one)
                                                    for lg in singles for v in singles[lg]])
+    # the same two batches with the autotuner choosing the window and the NTT
+    # pass variant (the first call of each key tunes; then timed as above)
+    gb.autotune_reset()
+    gb.autotune_set(True)
+    try:
+        out["msm64_autotuned_ms"] = timed(lambda: ctx.device_ragged(dv, slices))
+        out["ntt64_autotuned_ms"] = timed(lambda: [vecs[lg].ntt_zeta_batch(lg, logs.count(lg), False, one, one, one)
+                                                   for lg in vecs])
+        out["autotuned"] = gb.autotune_report()
+    finally:
+        gb.autotune_set(False)
     del ctx, dv
     return out
 

@@ -201,6 +201,7 @@ void timed_collect()
 using namespace gb;
 
 // ---------------------------------------------------------------- autotuner
+namespace gb {
 namespace {
 std::atomic<bool> g_autotune{false};
 std::mutex g_tune_mu;
@@ -223,6 +224,8 @@ void autotune_store(const std::string &key, int value)
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = value;
 }
+
+}  // namespace gb
 
 extern "C" {
 
