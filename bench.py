@@ -190,11 +190,14 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(dts) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 limbs (exact Fp/Fr)",
         "data": "synthetic (seeded uniform Fr scalars, bases [r_i]G)",
-        "config": {"workload": "G1 MSM n=2^%d, uniform Fr, bases [r_i]G (KZG commitment of the NTT+LDE "
-                               "configuration)" % (n.bit_length() - 1), "n": n},
+        "config": {"workload": "G1 MSM n=2^%d, uniform Fr scalars, bases [r_i]G: KZG commitment of the "
+                               "16x2^20 NTT + coset LDE configuration" % args.log_n,
+                   "n": args.n, "sample_n": n, "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": threads, "kind": "port",
-                         "sample": "one full n=2^%d MSM per step (oracle C Pippenger, all host threads); "
-                                   "the reference's Rust CPU path is not buildable here" % (n.bit_length() - 1)},
+                         "sample": "one n=2^%d MSM of the same scalar/base distribution per step (bounded sample "
+                                   "of the 2^%d workload; oracle C Pippenger on all host threads); the "
+                                   "reference's Rust CPU path is not buildable here"
+                                   % (n.bit_length() - 1, args.log_n)},
         "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
