@@ -2,7 +2,7 @@
  * CPU oracle for the BLS12-381 prover hot path -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference's CPU semantics, used by tests/,
- * __graft_entry__.smoke() and bench.py's cpu_baseline leg as the checker.
+ * __graft_entry__.smoke() and bench.py's cpu_baseline leg to check results.
  * Nothing in the product links it.  Each function names the reference
  * file:line it follows (paths relative to the dcSpark/midnight-ledger-cuda
  * tree).  The reference CPU arithmetic lives in blst 0.3.16 (a Cargo.lock

@@ -1,7 +1,7 @@
 """ctypes bindings of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as
-the checker.  Arrays are numpy uint64 with the reference's memory layout:
+Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg to
+check results.  Arrays are numpy uint64 with the reference's memory layout:
 Fr (n, 4), G1 affine (n, 12), G1 Jacobian (n, 18), all Montgomery form.
 """
 import ctypes

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY. The reference verifier needs a pairing
 (plonk/verifier.rs, poly/kzg/mod.rs:1806-1976 multi_prepare followed by
 the pairing check). The SRS of these tests comes from a known tau, so this
-checker replaces the pairing with the equivalent check in G1:
+verifier replaces the pairing with the equivalent check in G1:
 
     (tau - x3) * pi == final_com - v * G
 
