@@ -89,3 +89,20 @@ def test_device_lookup_permutation_rejects_missing_input(gb, orc):
     with pytest.raises(gb.MsmError):
         gb.fr_lookup_permute_device(gb.Bls12_381FrDeviceVec.upload(np.concatenate([inp, tab])), n, u, 1,
                                     orc.fr_random(n - u, rng), orc.fr_random(n - u, rng))
+
+
+def test_proof_on_the_reference_srs(gb, srs):
+    """The reference's own k = 14 SRS (bls_midnight_2p14: g and g_lagrange)
+    as the commitment key of both backends: identical proof bytes. Its tau
+    is unknown, so this checks parity on real bases, not validity."""
+    k, g, gl = srs
+    c = circuit(14, 3, 3, 1, copies=1 << 12, table_log=10, label="reference srs circuit")
+    fixed, advice, copies = c.synthesize()
+    gp = ParamsKZG(k, g, gl)
+    hp = plonk_cpu.HostParams(k, g, gl)
+    gbe, hbe = plonk.GpuBackend(gp), plonk_cpu.OracleBackend(hp)
+    gpk = plonk.keygen(gp, c, gbe, fixed, copies)
+    hpk = plonk.keygen(hp, c, hbe, fixed, copies)
+    gproof = plonk.create_proof(gp, gpk, advice, gbe, CircuitTranscript(), ChaCha20Rng.from_label("real-srs"))
+    hproof = plonk.create_proof(hp, hpk, advice, hbe, CircuitTranscript(), ChaCha20Rng.from_label("real-srs"))
+    assert gproof == hproof
