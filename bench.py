@@ -242,7 +242,8 @@ def main():
 
     for i in range(args.warmup):
         step(i)
-    peak = gb.imad_peak()
+    probe_forms = [gb.imad_probe(f) for f in range(4)]
+    peak = max(probe_forms)
 
     # ---- timed region: device-resident scalars
     gb.profile_reset()
@@ -294,7 +295,11 @@ def main():
         "bound": "imad", "unit": "Tmadd/s",
         "kernel": "msm_accumulate_kernel",
         "achieved": achieved, "peak": peak / 1e12, "frac": achieved / (peak / 1e12) if achieved else None,
-        "peak_source": "measured live: gb_imad_peak, best of mad.wide.u32 chains and carry-chained 12-limb rows with operands that change every iteration, all SMs",
+        "peak_source": "measured live: gb_imad_probe, the fastest of mad.wide.u32 chains and carry-chained 12-limb "
+                       "rows (1, 2, 4 accumulator sets per thread) with operands that change every iteration, all SMs; "
+                       "unit = one 32x32->64 product",
+        "peak_forms": {"wide": probe_forms[0] / 1e12, "rows1": probe_forms[1] / 1e12,
+                       "rows2": probe_forms[2] / 1e12, "rows4": probe_forms[3] / 1e12},
         "algorithmic_per_launch": "10 Fp-mul x n x W(c*) mixed additions, c*=%d, W=%d, 300 madd per Fp-mul"
                                   % (c_star, windows(c_star)),
         "avg_launch_ms": acc_avg_s * 1e3, "launches": acc_n,
@@ -313,7 +318,7 @@ def main():
 
     extra = {}
     if not args.no_extras:
-        extra = extras(gb, torch, n, rng, bases, args)
+        extra = extras(gb, torch, n, rng, bases, args, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -549,7 +554,7 @@ def cpu_baseline_proof():
     return time.perf_counter() - t0
 
 
-def extras(gb, torch, n, rng, bases, args):
+def extras(gb, torch, n, rng, bases, args, peak):
     """Secondary numbers of the same configuration (not the headline)."""
     out = {}
     # plain MSM: bases and scalars from host, nothing resident
@@ -572,6 +577,12 @@ def extras(gb, torch, n, rng, bases, args):
         e1.record(stream)
         e1.synchronize()
         out[name] = e0.elapsed_time(e1)
+    # (n/2) log n Fr products per transform, 136 multiply-adds each
+    ntt_madd = count * (1 << (log_n - 1)) * log_n * 136
+    achieved = ntt_madd / (out["ntt_2p20_x16_fwd_ms"] * 1e-3) / 1e12
+    out["roofline_ntt"] = {"bound": "imad", "unit": "Tmadd/s", "kernel": "16 x NTT 2^20, all passes",
+                           "achieved": achieved, "peak": peak / 1e12, "frac": achieved / (peak / 1e12),
+                           "algorithmic": "(n/2) log2 n Fr products x 136 madd per transform"}
     del dv
     src = gb.Bls12_381FrDeviceVec.upload(polys)
     # coefficients resident -> 16 extended cosets resident (CUDA events)

@@ -346,12 +346,25 @@ GB_API RustError gb_fr_device_kate_divide(void **out, const void *device_vec, si
  * {8, 10, 13, 16} and the NTT its pass variants the first time it meets a
  * (size, batch, scalar-sparsity) key, and keeps the fastest; off by default */
 GB_API void gb_autotune_set(int enabled);
+/* Forces the NTT pass variant, process-wide: 1 = one radix-2 butterfly per
+ * thread, 2 / 3 = 4 / 8 elements per thread with twiddles from the global
+ * table, 4 / 5 = 4 / 8 elements per thread with each pass's twiddles staged
+ * in shared memory by a bulk copy; 0 restores the default (4) or the
+ * autotuned choice */
+GB_API void gb_ntt_variant_set(int variant);
+/* staged NTT passes whose twiddle copy did not complete within the spin
+ * limit since the last call (their output is invalid); resets the count */
+GB_API RustError gb_ntt_wait_timeouts(uint32_t *out);
 GB_API void gb_autotune_reset(void);
 /* "key=value;" per tuned key into buf (NUL-terminated, truncated); returns
  * the full length */
 GB_API size_t gb_autotune_report(char *buf, size_t len);
-/* measured device throughput of 32x32->64 multiply-adds per second */
+/* measured device throughput of 32x32->64 multiply-adds (64-bit products)
+ * per second: the fastest probe form */
 GB_API RustError gb_imad_peak(double *out_per_sec);
+/* one probe form: 0 = mad.wide chains, 1..3 = carry-chained 12-limb rows
+ * with 1, 2 or 4 independent accumulator sets per thread */
+GB_API RustError gb_imad_probe(int form, double *out_per_sec);
 /* cumulative host<->device bytes moved by this library */
 GB_API void gb_transfer_counters(uint64_t *h2d_bytes, uint64_t *d2h_bytes);
 GB_API void gb_transfer_counters_reset(void);

@@ -290,6 +290,115 @@ GB_D void row_mac<8>(uint32_t *acc, const uint32_t *x, int parity, uint32_t y)
     if (parity == 0) row_mac8(acc, x[0], x[2], x[4], x[6], y);
     else row_mac8(acc, x[1], x[3], x[5], x[7], y);
 }
+
+// acc[0..N] += x_even * y + carry(c0 + c1): the even-limb row whose chain
+// starts with the carry of the previous step's word 0 (c0 + c1 is 0 or 2^32)
+GB_D void row_mac12_cin(uint32_t *acc, const uint32_t *x, uint32_t y, uint32_t c0, uint32_t c1)
+{
+    uint32_t t;
+    asm("add.cc.u32 %13, %20, %21;\n\t"
+        "madc.lo.cc.u32 %0, %14, %22, %0;\n\t"
+        "madc.hi.cc.u32 %1, %14, %22, %1;\n\t"
+        "madc.lo.cc.u32 %2, %15, %22, %2;\n\t"
+        "madc.hi.cc.u32 %3, %15, %22, %3;\n\t"
+        "madc.lo.cc.u32 %4, %16, %22, %4;\n\t"
+        "madc.hi.cc.u32 %5, %16, %22, %5;\n\t"
+        "madc.lo.cc.u32 %6, %17, %22, %6;\n\t"
+        "madc.hi.cc.u32 %7, %17, %22, %7;\n\t"
+        "madc.lo.cc.u32 %8, %18, %22, %8;\n\t"
+        "madc.hi.cc.u32 %9, %18, %22, %9;\n\t"
+        "madc.lo.cc.u32 %10, %19, %22, %10;\n\t"
+        "madc.hi.cc.u32 %11, %19, %22, %11;\n\t"
+        "addc.u32 %12, %12, 0;"
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+          "+r"(acc[7]), "+r"(acc[8]), "+r"(acc[9]), "+r"(acc[10]), "+r"(acc[11]), "+r"(acc[12]), "=r"(t)
+        : "r"(x[0]), "r"(x[2]), "r"(x[4]), "r"(x[6]), "r"(x[8]), "r"(x[10]), "r"(c0), "r"(c1), "r"(y));
+}
+
+GB_D void row_mac8_cin(uint32_t *acc, const uint32_t *x, uint32_t y, uint32_t c0, uint32_t c1)
+{
+    uint32_t t;
+    asm("add.cc.u32 %9, %14, %15;\n\t"
+        "madc.lo.cc.u32 %0, %10, %16, %0;\n\t"
+        "madc.hi.cc.u32 %1, %10, %16, %1;\n\t"
+        "madc.lo.cc.u32 %2, %11, %16, %2;\n\t"
+        "madc.hi.cc.u32 %3, %11, %16, %3;\n\t"
+        "madc.lo.cc.u32 %4, %12, %16, %4;\n\t"
+        "madc.hi.cc.u32 %5, %12, %16, %5;\n\t"
+        "madc.lo.cc.u32 %6, %13, %16, %6;\n\t"
+        "madc.hi.cc.u32 %7, %13, %16, %7;\n\t"
+        "addc.u32 %8, %8, 0;"
+        : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+          "+r"(acc[7]), "+r"(acc[8]), "=r"(t)
+        : "r"(x[0]), "r"(x[2]), "r"(x[4]), "r"(x[6]), "r"(c0), "r"(c1), "r"(y));
+}
+
+template <int N>
+GB_D void row_mac_cin(uint32_t *acc, const uint32_t *x, uint32_t y, uint32_t c0, uint32_t c1);
+template <>
+GB_D void row_mac_cin<12>(uint32_t *acc, const uint32_t *x, uint32_t y, uint32_t c0, uint32_t c1)
+{
+    row_mac12_cin(acc, x, y, c0, c1);
+}
+template <>
+GB_D void row_mac_cin<8>(uint32_t *acc, const uint32_t *x, uint32_t y, uint32_t c0, uint32_t c1)
+{
+    row_mac8_cin(acc, x, y, c0, c1);
+}
+
+// out[0..N-1] = lo-word sum e[1..N] + o[1..N] + carry(e[0] + o[0]), top
+// word out[N] = o[N+1] + carry: the one combination of the two accumulators
+GB_D void final_sum12(uint32_t *out, const uint32_t *e, const uint32_t *o)
+{
+    uint32_t t;
+    asm("add.cc.u32 %13, %14, %15;\n\t"
+        "addc.cc.u32 %0, %16, %17;\n\t"
+        "addc.cc.u32 %1, %18, %19;\n\t"
+        "addc.cc.u32 %2, %20, %21;\n\t"
+        "addc.cc.u32 %3, %22, %23;\n\t"
+        "addc.cc.u32 %4, %24, %25;\n\t"
+        "addc.cc.u32 %5, %26, %27;\n\t"
+        "addc.cc.u32 %6, %28, %29;\n\t"
+        "addc.cc.u32 %7, %30, %31;\n\t"
+        "addc.cc.u32 %8, %32, %33;\n\t"
+        "addc.cc.u32 %9, %34, %35;\n\t"
+        "addc.cc.u32 %10, %36, %37;\n\t"
+        "addc.cc.u32 %11, %38, %39;\n\t"
+        "addc.u32 %12, %40, 0;"
+        : "=r"(out[0]), "=r"(out[1]), "=r"(out[2]), "=r"(out[3]), "=r"(out[4]), "=r"(out[5]), "=r"(out[6]),
+          "=r"(out[7]), "=r"(out[8]), "=r"(out[9]), "=r"(out[10]), "=r"(out[11]), "=r"(out[12]), "=r"(t)
+        : "r"(e[0]), "r"(o[0]), "r"(e[1]), "r"(o[1]), "r"(e[2]), "r"(o[2]), "r"(e[3]), "r"(o[3]), "r"(e[4]),
+          "r"(o[4]), "r"(e[5]), "r"(o[5]), "r"(e[6]), "r"(o[6]), "r"(e[7]), "r"(o[7]), "r"(e[8]), "r"(o[8]),
+          "r"(e[9]), "r"(o[9]), "r"(e[10]), "r"(o[10]), "r"(e[11]), "r"(o[11]), "r"(e[12]), "r"(o[12]),
+          "r"(o[13]));
+}
+
+GB_D void final_sum8(uint32_t *out, const uint32_t *e, const uint32_t *o)
+{
+    uint32_t t;
+    asm("add.cc.u32 %9, %10, %11;\n\t"
+        "addc.cc.u32 %0, %12, %13;\n\t"
+        "addc.cc.u32 %1, %14, %15;\n\t"
+        "addc.cc.u32 %2, %16, %17;\n\t"
+        "addc.cc.u32 %3, %18, %19;\n\t"
+        "addc.cc.u32 %4, %20, %21;\n\t"
+        "addc.cc.u32 %5, %22, %23;\n\t"
+        "addc.cc.u32 %6, %24, %25;\n\t"
+        "addc.cc.u32 %7, %26, %27;\n\t"
+        "addc.u32 %8, %28, 0;"
+        : "=r"(out[0]), "=r"(out[1]), "=r"(out[2]), "=r"(out[3]), "=r"(out[4]), "=r"(out[5]), "=r"(out[6]),
+          "=r"(out[7]), "=r"(out[8]), "=r"(t)
+        : "r"(e[0]), "r"(o[0]), "r"(e[1]), "r"(o[1]), "r"(e[2]), "r"(o[2]), "r"(e[3]), "r"(o[3]), "r"(e[4]),
+          "r"(o[4]), "r"(e[5]), "r"(o[5]), "r"(e[6]), "r"(o[6]), "r"(e[7]), "r"(o[7]), "r"(e[8]), "r"(o[8]),
+          "r"(o[9]));
+}
+
+template <int N>
+GB_D void final_sum(uint32_t *out, const uint32_t *e, const uint32_t *o);
+template <>
+GB_D void final_sum<12>(uint32_t *out, const uint32_t *e, const uint32_t *o) { final_sum12(out, e, o); }
+template <>
+GB_D void final_sum<8>(uint32_t *out, const uint32_t *e, const uint32_t *o) { final_sum8(out, e, o); }
 #endif
 
 template <class Cfg>
@@ -465,6 +574,59 @@ GB_D void mont_step(uint32_t *even, uint32_t *odd, const uint32_t *a, uint32_t b
     fold<N>(even, odd);
 }
 
+#if defined(GB_MUL_NOFOLD)
+// CIOS without a per-step fold.  The running sum is kept as two accumulators
+// at the same word offset, T = E + O, where the products of a's odd limbs
+// land one word up in O.  After the Montgomery step T's word 0 is
+// E[0] + O[0], which is 0 or 2^32; instead of folding, both accumulators are
+// shifted down one word and the carry of E[0] + O[0] enters the next step's
+// even-limb chain as its carry-in.  The two accumulators are added once, at
+// the end (checked word by word against the integer definition on the host).
+template <class Cfg>
+GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
+{
+    constexpr int N = Cfg::N;
+    uint32_t e[N + 1], o[N + 2];
+    // step 0: plain products, no carries
+    const uint32_t b0 = b[0];
+#pragma unroll
+    for (int k = 0; k < N / 2; k++) {
+        e[2 * k] = a[2 * k] * b0;
+        e[2 * k + 1] = __umulhi(a[2 * k], b0);
+        o[2 * k + 1] = a[2 * k + 1] * b0;
+        o[2 * k + 2] = __umulhi(a[2 * k + 1], b0);
+    }
+    e[N] = 0;
+    o[0] = 0;
+    o[N + 1] = 0;
+    {
+        const uint32_t m = e[0] * Cfg::INV;
+        row_mac_mod<Cfg>(e, 0, m);
+        row_mac_mod<Cfg>(o + 1, 1, m);
+    }
+#pragma unroll
+    for (int i = 1; i < N; i++) {
+        const uint32_t c0 = e[0], c1 = o[0];
+#pragma unroll
+        for (int j = 0; j < N; j++) e[j] = e[j + 1];
+        e[N] = 0;
+#pragma unroll
+        for (int j = 0; j < N + 1; j++) o[j] = o[j + 1];
+        o[N + 1] = 0;
+        row_mac_cin<N>(e, a, b[i], c0, c1);
+        row_mac<N>(o + 1, a, 1, b[i]);
+        const uint32_t m = (e[0] + o[0]) * Cfg::INV;
+        row_mac_mod<Cfg>(e, 0, m);
+        row_mac_mod<Cfg>(o + 1, 1, m);
+    }
+    uint32_t r[N + 1];
+    final_sum<N>(r, e, o);
+    // r < 2m; final conditional subtraction
+    mont_t<Cfg>::reduce_once(r, r[N]);
+#pragma unroll
+    for (int i = 0; i < N; i++) out[i] = r[i];
+}
+#else
 template <class Cfg>
 GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 {
@@ -495,6 +657,7 @@ GB_D void mont_mul_device(uint32_t *out, const uint32_t *a, const uint32_t *b)
 #pragma unroll
     for (int i = 0; i < N; i++) out[i] = even[i];
 }
+#endif  // GB_MUL_NOFOLD
 #endif
 
 // Out-of-line products.  A point addition inlines ten Fp products; fully

@@ -105,13 +105,16 @@ void generator_mul_device(affine_t *d_out, const fr_t *d_scalars, size_t n, cuda
 }
 
 // ---------------------------------------------------------------- peak probe
-// Throughput of 32x32->64 multiply-adds, the unit in which the MSM's
+// Throughput of 32x32->64 multiply-adds, the unit in which the hot path's
 // algorithmic work is counted (one Fp Montgomery product = 2*12^2 + 12 = 300
-// of them).  Two instruction forms are timed and the faster one is the peak:
+// of them, one Fr product = 2*8^2 + 8 = 136).  A multiply-add is one 64-bit
+// product: a mad.lo / madc.hi instruction pair, or one mad.wide.  Two
+// instruction forms are timed and the fastest configuration is the peak:
 //   * mad.wide.u32 chains: acc = lo32(acc) * y + acc, 8 chains per thread;
-//   * carry-chained rows as in a CIOS Montgomery step: 12 products
-//     (mad.lo.cc / madc.hi.cc) of a 12-limb operand by a multiplier that
-//     each row derives from the previous row's result.
+//   * carry-chained rows as in a CIOS Montgomery step: a 12-limb operand
+//     times a multiplier, as an even-limb and an odd-limb row of 6 products
+//     each (mad.lo.cc / madc.hi.cc), on SETS independent accumulators per
+//     thread; each accumulator's next multiplier derives from its own result.
 // Every product depends on a value produced inside the loop, so no form can
 // be hoisted or strength-reduced; results are folded into `sink`.
 __global__ void peak_wide_kernel(uint32_t y, int iters, unsigned long long *sink)
@@ -130,46 +133,34 @@ __global__ void peak_wide_kernel(uint32_t y, int iters, unsigned long long *sink
     if (r == 0x123456789ull) atomicAdd(sink, r);
 }
 
+template <int SETS>
 __global__ void peak_row_kernel(uint32_t y, int iters, unsigned long long *sink)
 {
-    uint32_t t[13], a[12];
+    uint32_t e[SETS][13], o[SETS][13], a[12], bi[SETS];
 #pragma unroll
-    for (int k = 0; k < 12; k++) {
-        a[k] = (threadIdx.x + 1u) * 0x9E3779B9u + (uint32_t)k;
-        t[k] = (uint32_t)k;
+    for (int k = 0; k < 12; k++) a[k] = (threadIdx.x + 1u) * 0x9E3779B9u + (uint32_t)k;
+#pragma unroll
+    for (int q = 0; q < SETS; q++) {
+#pragma unroll
+        for (int k = 0; k < 13; k++) {
+            e[q][k] = (uint32_t)(k + 13 * q);
+            o[q][k] = (uint32_t)(3 * k + q);
+        }
+        bi[q] = y ^ (threadIdx.x * (uint32_t)(q + 1));
     }
-    t[12] = 0;
-    uint32_t bi = y ^ threadIdx.x;
     for (int it = 0; it < iters; it++) {
-        // even limbs: lo into t[2k], hi into t[2k+1]
-        asm volatile(
-            "mad.lo.cc.u32 %0, %13, %25, %0; madc.hi.cc.u32 %1, %13, %25, %1;"
-            "madc.lo.cc.u32 %2, %15, %25, %2; madc.hi.cc.u32 %3, %15, %25, %3;"
-            "madc.lo.cc.u32 %4, %17, %25, %4; madc.hi.cc.u32 %5, %17, %25, %5;"
-            "madc.lo.cc.u32 %6, %19, %25, %6; madc.hi.cc.u32 %7, %19, %25, %7;"
-            "madc.lo.cc.u32 %8, %21, %25, %8; madc.hi.cc.u32 %9, %21, %25, %9;"
-            "madc.lo.cc.u32 %10, %23, %25, %10; madc.hi.cc.u32 %11, %23, %25, %11; addc.u32 %12, %12, 0;"
-            : "+r"(t[0]), "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]),
-              "+r"(t[8]), "+r"(t[9]), "+r"(t[10]), "+r"(t[11]), "+r"(t[12])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]),
-              "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(bi));
-        // odd limbs
-        asm volatile(
-            "mad.lo.cc.u32 %1, %14, %25, %1; madc.hi.cc.u32 %2, %14, %25, %2;"
-            "madc.lo.cc.u32 %3, %16, %25, %3; madc.hi.cc.u32 %4, %16, %25, %4;"
-            "madc.lo.cc.u32 %5, %18, %25, %5; madc.hi.cc.u32 %6, %18, %25, %6;"
-            "madc.lo.cc.u32 %7, %20, %25, %7; madc.hi.cc.u32 %8, %20, %25, %8;"
-            "madc.lo.cc.u32 %9, %22, %25, %9; madc.hi.cc.u32 %10, %22, %25, %10;"
-            "madc.lo.cc.u32 %11, %24, %25, %11; madc.hi.cc.u32 %12, %24, %25, %12; addc.u32 %0, %0, 0;"
-            : "+r"(t[0]), "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]),
-              "+r"(t[8]), "+r"(t[9]), "+r"(t[10]), "+r"(t[11]), "+r"(t[12])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]),
-              "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(bi));
-        bi = t[0] ^ t[12];
+#pragma unroll
+        for (int q = 0; q < SETS; q++) {
+            row_mac12(e[q], a[0], a[2], a[4], a[6], a[8], a[10], bi[q]);
+            row_mac12(o[q], a[1], a[3], a[5], a[7], a[9], a[11], bi[q]);
+            bi[q] = e[q][0] ^ o[q][12];
+        }
     }
     uint32_t r = 0;
 #pragma unroll
-    for (int k = 0; k < 13; k++) r ^= t[k];
+    for (int q = 0; q < SETS; q++)
+#pragma unroll
+        for (int k = 0; k < 13; k++) r ^= e[q][k] ^ o[q][k];
     if (r == 0x1234567u) atomicAdd(sink, (unsigned long long)r);
 }
 
@@ -211,11 +202,12 @@ RustError gb_g1_generator_mul_device(RawG1Affine *d_out_raw, const RawFr *d_scal
     GB_ENTRY_END
 }
 
-// Measured multiply-add peak: times both probe forms and returns the faster
-// one's multiply-adds per second (whole device) in *out_per_sec.
-RustError gb_imad_peak(double *out_per_sec)
+// Multiply-add throughput of one probe form (whole device, 32x32->64
+// products per second): form 0 = mad.wide chains, forms 1..3 = carry-chained
+// rows with 1, 2 or 4 independent accumulator sets per thread.
+RustError gb_imad_probe(int form, double *out_per_sec)
 {
-    if (!out_per_sec) return make_error((int)cudaErrorInvalidValue, "null output");
+    if (!out_per_sec || form < 0 || form > 3) return make_error((int)cudaErrorInvalidValue, "invalid probe form");
     GB_ENTRY_BEGIN
     cudaStream_t s = lane_stream();
     int dev = current_device(), sms = 0;
@@ -223,23 +215,23 @@ RustError gb_imad_peak(double *out_per_sec)
     unsigned long long *sink = nullptr;
     GB_CUDA_OK(cudaMallocAsync((void **)&sink, sizeof(*sink), s));
     const int threads = 256, blocks = sms * 8, iters = 2048;
+    const double per_iter = form == 0 ? 8.0 : 12.0 * (1 << (form - 1));
     cudaEvent_t e0, e1;
     GB_CUDA_OK(cudaEventCreate(&e0));
     GB_CUDA_OK(cudaEventCreate(&e1));
     double best = 0;
-    for (int form = 0; form < 2; form++) {
-        for (int rep = 0; rep < 2; rep++) {  // the first run warms up
-            GB_CUDA_OK(cudaEventRecord(e0, s));
-            if (form == 0) peak_wide_kernel<<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
-            else peak_row_kernel<<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
-            GB_CHECK_LAUNCH();
-            GB_CUDA_OK(cudaEventRecord(e1, s));
-            GB_CUDA_OK(cudaEventSynchronize(e1));
-            float ms = 0;
-            GB_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
-            const double per_iter = form == 0 ? 8.0 : 24.0;
-            if (rep) best = std::max(best, (double)blocks * threads * iters * per_iter / (ms * 1e-3));
-        }
+    for (int rep = 0; rep < 3; rep++) {  // the first run warms up
+        GB_CUDA_OK(cudaEventRecord(e0, s));
+        if (form == 0) peak_wide_kernel<<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
+        else if (form == 1) peak_row_kernel<1><<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
+        else if (form == 2) peak_row_kernel<2><<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
+        else peak_row_kernel<4><<<blocks, threads, 0, s>>>(0x9E3779B9u, iters, sink);
+        GB_CHECK_LAUNCH();
+        GB_CUDA_OK(cudaEventRecord(e1, s));
+        GB_CUDA_OK(cudaEventSynchronize(e1));
+        float ms = 0;
+        GB_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep) best = std::max(best, (double)blocks * threads * iters * per_iter / (ms * 1e-3));
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -247,6 +239,21 @@ RustError gb_imad_peak(double *out_per_sec)
     *out_per_sec = best;
     return ok();
     GB_ENTRY_END
+}
+
+// Measured multiply-add peak: the fastest of the probe forms.
+RustError gb_imad_peak(double *out_per_sec)
+{
+    if (!out_per_sec) return make_error((int)cudaErrorInvalidValue, "null output");
+    double best = 0;
+    for (int form = 0; form < 4; form++) {
+        double r = 0;
+        RustError e = gb_imad_probe(form, &r);
+        if (e.code) return e;
+        best = std::max(best, r);
+    }
+    *out_per_sec = best;
+    return ok();
 }
 
 }  // extern "C"

@@ -14,7 +14,9 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <algorithm>
 #include <tuple>
+#include <vector>
 
 #include "gb_ntt.cuh"
 
@@ -162,6 +164,352 @@ __global__ void ntt_dif_pass_reg_kernel(fr_t *data, uint32_t log_n, int s_hi, in
     for (uint32_t t = threadIdx.x; t < cnt; t += blockDim.x) d[base + ((size_t)t << s_lo)] = sm[ntt_pad(t)];
 }
 
+// ---------------------------------------------------------------- staged passes
+// The pass with its twiddles staged in shared memory.  A CTA holds Q = 2^q
+// sub-blocks of 2^g elements (Q * 2^g <= 1024) and its own contiguous chunk
+// of the pass's twiddle table, which one thread copies in with a TMA bulk
+// copy (cp.async.bulk + mbarrier) while the block gathers the data.
+//
+// Pass twiddle table: for a pass over global stages s_lo .. s_lo+g-1, chunk
+// lo (lo < 2^s_lo, the sub-block's offset below the pass) has 2^g entries;
+// entry m = 2^p + t' (t' < 2^p) is the twiddle of local stage p for the
+// butterflies whose local index is t' mod 2^p:
+//     w^(((t' << s_lo) + lo) << (log_n - 1 - s_lo - p))
+// (entry 0 is unused).  A pass with s_lo = 0 has the single chunk lo = 0.
+//
+// Shared memory is addressed in 16-byte chunks.  Element t of a sub-block
+// occupies chunks 2t and 2t+1 of its 128-byte row r = t/4, permuted inside
+// the row by r ^ (r >> 1) ^ (r >> 2) and, for the data, by a twist of the
+// sub-block number, so that the gathers of every radix-2^R group (the
+// remainder group first, at the top bits), the twiddle reads and the
+// strided global loads are free of bank conflicts for g >= 5.  The global
+// twiddle table is stored in the same permuted order, so the bulk copy
+// lands it ready to use.
+__host__ __device__ __forceinline__ uint32_t ntt_swz_row(uint32_t r) { return (r ^ (r >> 1) ^ (r >> 2)) & 7u; }
+__host__ __device__ __forceinline__ uint32_t ntt_twist(uint32_t q) { return (q & 1u) | ((q & 2u) << 1) | ((q & 4u) >> 1); }
+__host__ __device__ __forceinline__ uint32_t ntt_chunk(uint32_t t, uint32_t h, uint32_t x)
+{
+    const uint32_t r = t >> 2;
+    return (r << 3) | ((((t & 3u) << 1) | h) ^ ntt_swz_row(r) ^ x);
+}
+
+__device__ __forceinline__ fr_t ntt_ld(const uint4 *s, uint32_t t, uint32_t x)
+{
+    const uint4 a = s[ntt_chunk(t, 0, x)], b = s[ntt_chunk(t, 1, x)];
+    fr_t r;
+    r.v[0] = a.x, r.v[1] = a.y, r.v[2] = a.z, r.v[3] = a.w;
+    r.v[4] = b.x, r.v[5] = b.y, r.v[6] = b.z, r.v[7] = b.w;
+    return r;
+}
+
+__device__ __forceinline__ void ntt_st(uint4 *s, uint32_t t, uint32_t x, const fr_t &v)
+{
+    s[ntt_chunk(t, 0, x)] = make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
+    s[ntt_chunk(t, 1, x)] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
+}
+
+// chunk(t, h, x) = lin(t) ^ h ^ x, with lin linear over GF(2) in the bits
+// of t: addresses of elements whose indices differ in known bits are found
+// by XOR-ing precomputed images of those bits.
+__device__ __forceinline__ uint32_t ntt_lin(uint32_t t)
+{
+    const uint32_t r = t >> 2;
+    return (r << 3) | (((t & 3u) << 1) ^ ntt_swz_row(r));
+}
+
+__device__ __forceinline__ fr_t ntt_ld_c(const uint4 *s, uint32_t c)
+{
+    const uint4 a = s[c], b = s[c ^ 1u];
+    fr_t r;
+    r.v[0] = a.x, r.v[1] = a.y, r.v[2] = a.z, r.v[3] = a.w;
+    r.v[4] = b.x, r.v[5] = b.y, r.v[6] = b.z, r.v[7] = b.w;
+    return r;
+}
+
+__device__ __forceinline__ void ntt_st_c(uint4 *s, uint32_t c, const fr_t &v)
+{
+    s[c] = make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
+    s[c ^ 1u] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
+}
+
+// One radix-2^R group over local bits [B, B + R) of a sub-block; thread u
+// (within the sub-block) holds E = 2^EL elements, which need B >= EL - R.
+// Element k of the thread has local index
+//     tl[k] = tl[0] ^ (k >> R) ^ ((k mod 2^R) << B)
+// (the bits of k >> R sit below B), so its chunk address is lin(tl[0]) XOR
+// images of single bits.  The butterflies of one stage that share a twiddle
+// (same local index mod 2^p) read it once.
+template <int EL, int R>
+__device__ __forceinline__ void ntt_tw_group(uint4 *sd, const uint4 *stw, uint32_t u, int B, uint32_t twist,
+                                             bool lo_zero)
+{
+    constexpr int E = 1 << EL;
+    const uint32_t rest0 = u << (EL - R);
+    const uint32_t tl0 = (rest0 & ((1u << B) - 1)) | ((rest0 >> B) << (B + R));
+    const uint32_t base = ntt_lin(tl0) ^ twist;
+    uint32_t img_b[R];  // lin(1 << (B + j))
+#pragma unroll
+    for (int j = 0; j < R; j++) img_b[j] = ntt_lin(1u << (B + j));
+    // lin of the bits k >> R (below B): constants
+    auto img_lo = [](uint32_t v) { return ntt_lin(v); };
+    uint32_t off[E];
+    fr_t x[E];
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+        uint32_t o = img_lo((uint32_t)k >> R);
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if ((k >> j) & 1) o ^= img_b[j];
+        off[k] = o;
+        x[k] = ntt_ld_c(sd, base ^ o);
+    }
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+        const int p = B + R - 1 - st;  // local bit of this stage
+        const int lh = R - 1 - st, hk = 1 << lh;
+        // twiddle entry of key (kl, kr): m = 2^p ^ (tl0 mod 2^p) ^ kr ^ (kl << B)
+        const uint32_t tp0 = tl0 & ((1u << p) - 1);
+        const uint32_t tbase = ntt_lin((1u << p) ^ tp0);
+        fr_t w[E / 2];
+        bool one[E / 2];
+#pragma unroll
+        for (int key = 0; key < (hk << (EL - R)); key++) {
+            const uint32_t kl = (uint32_t)key & (hk - 1), kr = (uint32_t)key >> lh;
+            uint32_t o = img_lo(kr);
+#pragma unroll
+            for (int j = 0; j < lh; j++)
+                if ((kl >> j) & 1) o ^= img_b[j];
+            one[key] = lo_zero && (tp0 | kr | kl) == 0;
+            w[key] = ntt_ld_c(stw, tbase ^ o);
+        }
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            if ((k & hk) == 0) {
+                const int k1 = k + hk;
+                const int key = (k & (hk - 1)) | ((k >> R) << lh);
+                const fr_t a = x[k], c = x[k1];
+                x[k] = a + c;
+                fr_t diff = a - c;
+                if (!one[key]) diff = diff * w[key];
+                x[k1] = diff;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < E; k++) ntt_st_c(sd, base ^ off[k], x[k]);
+}
+
+static constexpr unsigned kWaitSpins = 1u << 24;
+
+// bounded wait on phase 0 of an mbarrier; true when the phase completed
+__device__ __forceinline__ bool mbar_wait0(uint32_t mbar)
+{
+    for (unsigned i = 0; i < kWaitSpins; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ unsigned int g_ntt_wait_timeouts;
+
+// output factors of the last pass: natural index i of a transform is
+// multiplied by f[i mod 3] (the ZETA coset distribution times the scale)
+struct ntt_factors {
+    fr_t f[3];
+    int on;
+};
+
+__device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bits ? __brev(x) >> (32 - bits) : 0u; }
+
+// One staged pass.  src and dst may alias (in place) except in the LAST
+// pass, which reads the DIF order from src and writes natural order to dst.
+//
+// Grid, for a pass with s_lo > 0: CTA c covers sub-blocks (c / count) * Q ..
+// + Q - 1 of transform c % count, so CTAs sharing a twiddle chunk run
+// together.  For s_lo = 0 the batch is one run of count * 2^(log_n - g)
+// sub-blocks and CTA c covers run positions c * Q .. c * Q + Q - 1 (those
+// past the end are skipped).  In the LAST pass run position F of transform
+// F / NB (NB = 2^(log_n - g) sub-blocks per transform) is the sub-block whose
+// outputs land in column F mod NB of the natural order, i.e. sub-block
+// bitrev(F mod NB): element t of it is output bitrev(t) * NB + (F mod NB),
+// so the Q sub-blocks of a CTA write Q adjacent outputs per row.
+template <int EL, bool LAST>
+__global__ void __launch_bounds__(1024 >> EL, 3)
+    ntt_dif_pass_tw_kernel(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q, size_t count,
+                           const fr_t *__restrict__ twt, ntt_factors fac)
+{
+    extern __shared__ uint4 smem[];
+    __shared__ uint64_t mbar_store;
+    __shared__ int copy_ok;
+    const int s_lo = s_hi - g + 1;
+    const uint32_t sub = 1u << g, Q = 1u << q, nd = Q << g;
+    const size_t n = (size_t)1 << log_n;
+    const uint32_t tw_entries = s_lo > 0 ? nd : sub;
+    uint4 *sd = smem;
+    uint4 *stw = smem + 2 * (size_t)nd;
+    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_store);
+    const int nb_log = (int)log_n - g;                 // log2 sub-blocks per transform
+    const size_t total = count << nb_log;              // sub-blocks in the batch
+    const bool q_fast = !LAST || nb_log >= q;          // LAST: Q adjacent columns of one transform
+
+    size_t poly = 0, b0 = 0;
+    const fr_t *twsrc = twt;
+    if (s_lo > 0) {
+        poly = blockIdx.x % count;
+        b0 = (size_t)(blockIdx.x / count) << q;
+        twsrc = twt + ((b0 & (((size_t)1 << s_lo) - 1)) << g);
+    } else {
+        b0 = (size_t)blockIdx.x << q;
+    }
+
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = tw_entries * (uint32_t)sizeof(fr_t);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(stw)),
+            "l"(twsrc), "r"(bytes), "r"(mbar)
+            : "memory");
+    }
+
+    // gather the sub-blocks into shared memory
+    for (uint32_t idx = threadIdx.x; idx < nd; idx += blockDim.x) {
+        uint32_t qq, t;
+        size_t addr;
+        bool valid = true;
+        if (s_lo > 0) {
+            qq = idx & (Q - 1);
+            t = idx >> q;
+            const size_t b = b0 + qq;
+            addr = poly * n + ((b >> s_lo) << (s_hi + 1)) + (b & (((size_t)1 << s_lo) - 1)) + ((size_t)t << s_lo);
+        } else {
+            qq = idx >> g;
+            t = idx & (sub - 1);
+            const size_t F = b0 + qq;
+            valid = F < total;
+            if (LAST) {
+                const size_t col = F & (((size_t)1 << nb_log) - 1);
+                addr = ((F >> nb_log) << log_n) + ((size_t)brev_bits((uint32_t)col, nb_log) << g) + t;
+            } else {
+                addr = (F << g) + t;
+            }
+        }
+        const fr_t v = valid ? src[addr] : fr_t::zero();
+        ntt_st(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u), v);
+    }
+    if (threadIdx.x == 0) {
+        bool ok = mbar_wait0(mbar);
+        if (!ok) {
+            atomicAdd(&g_ntt_wait_timeouts, 1u);
+            mbar_wait0(mbar);  // let the copy in flight land before the CTA exits
+        }
+        copy_ok = ok;
+    }
+    __syncthreads();
+    if (!copy_ok) return;
+
+    // radix-2^EL groups; the remainder group first, at the top bits
+    {
+        const uint32_t per_sub = sub >> EL;  // threads per sub-block; blockDim.x = nd >> EL
+        const uint32_t qq = threadIdx.x / per_sub, ul = threadIdx.x % per_sub;
+        uint4 *sdq = sd + 2 * (size_t)qq * sub;
+        const uint4 *stq = stw + (s_lo > 0 ? 2 * (size_t)qq * sub : 0);
+        const uint32_t twist = ntt_twist(qq & 7u);
+        const bool lo_zero = s_lo == 0 || (((b0 + qq) & (((size_t)1 << s_lo) - 1)) == 0);
+        int top = g;
+        const int rem = g % EL;
+        if (rem) {
+            if (EL == 3 && rem == 2) ntt_tw_group<EL, (EL == 3 ? 2 : 1)>(sdq, stq, ul, g - rem, twist, lo_zero);
+            else ntt_tw_group<EL, 1>(sdq, stq, ul, g - rem, twist, lo_zero);
+            top -= rem;
+            __syncthreads();
+        }
+        while (top > 0) {
+            ntt_tw_group<EL, EL>(sdq, stq, ul, top - EL, twist, lo_zero);
+            top -= EL;
+            __syncthreads();
+        }
+    }
+
+    // write back
+    for (uint32_t idx = threadIdx.x; idx < nd; idx += blockDim.x) {
+        uint32_t qq, t;
+        size_t addr;
+        if (s_lo > 0) {
+            qq = idx & (Q - 1);
+            t = idx >> q;
+            const size_t b = b0 + qq;
+            addr = poly * n + ((b >> s_lo) << (s_hi + 1)) + (b & (((size_t)1 << s_lo) - 1)) + ((size_t)t << s_lo);
+        } else if (!LAST) {
+            qq = idx >> g;
+            t = idx & (sub - 1);
+            if (b0 + qq >= total) continue;
+            addr = ((b0 + qq) << g) + t;
+        } else {
+            uint32_t r;  // output row
+            if (q_fast) {
+                qq = idx & (Q - 1);
+                r = idx >> q;
+            } else {
+                qq = idx >> g;
+                r = idx & (sub - 1);
+            }
+            const size_t F = b0 + qq;
+            if (F >= total) continue;
+            t = brev_bits(r, g);
+            const size_t col = F & (((size_t)1 << nb_log) - 1);
+            const size_t i_nat = ((size_t)r << nb_log) + col;
+            addr = ((F >> nb_log) << log_n) + i_nat;
+            fr_t v = ntt_ld(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u));
+            if (fac.on) {
+                const uint32_t c = (uint32_t)(i_nat % 3);
+                fr_t f;
+#pragma unroll
+                for (int w = 0; w < 8; w++) f.v[w] = c == 0 ? fac.f[0].v[w] : c == 1 ? fac.f[1].v[w] : fac.f[2].v[w];
+                v = v * f;
+            }
+            dst[addr] = v;
+            continue;
+        }
+        dst[addr] = ntt_ld(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u));
+    }
+}
+
+// pass twiddle table entries from the base table tw[e] = w^e (e < n/2),
+// written in the permuted chunk order (see above)
+__global__ void pass_twiddle_kernel(fr_t *out, const fr_t *__restrict__ tw, uint32_t log_n, int s_lo, int g,
+                                    size_t chunks)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t sub = (size_t)1 << g;
+    if (i >= chunks * sub) return;
+    const size_t lo = i >> g;
+    const uint32_t m = (uint32_t)(i & (sub - 1));
+    fr_t v = fr_t::one();
+    if (m) {
+        const int p = 31 - __clz(m);
+        const size_t tp = m - (1u << p);
+        const size_t e = ((tp << s_lo) + lo) << (log_n - 1 - s_lo - p);
+        v = tw[e];
+    }
+    uint4 *o = reinterpret_cast<uint4 *>(out + (lo << g));
+    o[ntt_chunk(m, 0, 0)] = make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
+    o[ntt_chunk(m, 1, 0)] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
+}
+
 __device__ __forceinline__ size_t bitrev_n(size_t x, uint32_t bits)
 {
     return (size_t)(__brevll((unsigned long long)x) >> (64 - bits));
@@ -217,6 +565,15 @@ __global__ void scale_zeta_kernel(fr_t *d, fr_t scale, fr_t first, fr_t second, 
     d[i] = v;
 }
 
+// d[i] *= f[(i mod period_len) mod 3]
+__global__ void mul_period3_kernel(fr_t *d, fr_t f0, fr_t f1, fr_t f2, size_t len, size_t period_len)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    const size_t c = (i % period_len) % 3;
+    d[i] = d[i] * (c == 0 ? f0 : c == 1 ? f1 : f2);
+}
+
 __global__ void c2e_prepare_kernel(fr_t *out, const fr_t *__restrict__ in, fr_t first, fr_t second,
                                    size_t input_len, size_t output_len, size_t count)
 {
@@ -267,9 +624,103 @@ void set_ntt_smem()
                              (1 << kPassBits) / 8 * 9 * (int)sizeof(fr_t));
         cudaFuncSetAttribute(ntt_dif_pass_reg_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (1 << kPassBits) / 8 * 9 * (int)sizeof(fr_t));
+        const int staged = 2 * (1 << kPassBits) * (int)sizeof(fr_t);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
     });
 }
+
+// (s_hi, g) of each pass: ceil(log_n / 10) passes of near-equal size, the
+// larger ones first
+std::vector<std::pair<int, int>> pass_split(uint32_t log_n)
+{
+    std::vector<std::pair<int, int>> out;
+    const int L = (int)log_n, P = (L + kPassBits - 1) / kPassBits;
+    int s_hi = L - 1;
+    for (int i = 0; i < P; i++) {
+        const int g = L / P + (i < L % P ? 1 : 0);
+        out.emplace_back(s_hi, g);
+        s_hi -= g;
+    }
+    return out;
+}
+
+std::map<std::tuple<int, uint32_t, bool, int>, fr_t *> g_pass_tw;
+
+// the pass twiddle table of the pass with top stage s_hi (cached per device)
+const fr_t *pass_twiddles(uint32_t log_n, bool inverse, int s_hi, int g, const fr_t *tw, cudaStream_t s)
+{
+    int dev = current_device();
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    auto key = std::make_tuple(dev, log_n, inverse, s_hi);
+    auto it = g_pass_tw.find(key);
+    if (it != g_pass_tw.end()) return it->second;
+    const int s_lo = s_hi - g + 1;
+    const size_t chunks = s_lo > 0 ? (size_t)1 << s_lo : 1;
+    const size_t entries = chunks << g;
+    fr_t *t = nullptr;
+    GB_CUDA_OK(cudaMalloc(&t, entries * sizeof(fr_t)));
+    pass_twiddle_kernel<<<blocks_for(entries, 256), 256, 0, s>>>(t, tw, log_n, s_lo, g, chunks);
+    GB_CHECK_LAUNCH();
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    g_pass_tw[key] = t;
+    return t;
+}
 }  // namespace
+
+// The staged-twiddle transform (variants 4 and 5: 4 or 8 elements per
+// thread), natural order out with the output factors applied.  With two or
+// more passes the first pass writes to a scratch buffer, the middle ones work
+// there in place and the last one writes natural order back to d, so no
+// separate bit-reversal pass is needed; a single pass works in place.
+static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *tw, int el,
+                       const ntt_factors &fac, cudaStream_t s)
+{
+    const auto passes = pass_split(log_n);
+    const size_t P = passes.size();
+    dev_buf<fr_t> tmp(P > 1 ? count << log_n : 0, s);
+    const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+    for (size_t i = 0; i < P; i++) {
+        const int s_hi = passes[i].first, g = passes[i].second;
+        const int s_lo = s_hi - g + 1;
+        const bool last = i + 1 == P;
+        const fr_t *src = i == 0 ? d : tmp.get();
+        fr_t *dst = last ? d : tmp.get();
+        const fr_t *tab = pass_twiddles(log_n, inverse, s_hi, g, tw, s);
+        int q = kPassBits - g;
+        size_t ctas;
+        if (s_lo > 0) {
+            q = std::min(q, s_lo);
+            ctas = (count << (log_n - g)) >> q;
+        } else {
+            const size_t total = count << (log_n - g);
+            while (q > 0 && ((size_t)1 << (q - 1)) >= total) q--;
+            ctas = (total + ((size_t)1 << q) - 1) >> q;
+        }
+        const uint32_t nd = 1u << (g + q);
+        const uint32_t tw_entries = s_lo > 0 ? nd : 1u << g;
+        const size_t smem = ((size_t)nd + tw_entries) * sizeof(fr_t);
+        const unsigned threads = nd >> el;
+        if (el == 3) {
+            if (last)
+                ntt_dif_pass_tw_kernel<3, true><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
+                                                                                       count, tab, fac);
+            else
+                ntt_dif_pass_tw_kernel<3, false><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
+                                                                                        count, tab, none);
+        } else {
+            if (last)
+                ntt_dif_pass_tw_kernel<2, true><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
+                                                                                       count, tab, fac);
+            else
+                ntt_dif_pass_tw_kernel<2, false><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
+                                                                                        count, tab, none);
+        }
+        GB_CHECK_LAUNCH();
+    }
+}
 
 // the DIF passes of `count` transforms in place; el = log2(elements per
 // thread) of the register-blocked pass (1 = one butterfly per thread)
@@ -294,49 +745,78 @@ static void ntt_passes(fr_t *d, uint32_t log_n, size_t count, const fr_t *tw, in
     }
 }
 
-// Pass variant: 4 elements per thread (radix-4 register steps) from 2^18 up,
-// where it is fastest on GB300; below that the radix-2 pass with up to 512
-// threads keeps more warps resident.  GB_NTT_ELEMS_LOG (1, 2, 3) overrides;
-// with the autotuner on, each size times the three variants once on a
-// scratch copy of one transform.
-static int ntt_variant(fr_t *d, uint32_t log_n, const fr_t *tw, cudaStream_t s)
+// The whole transform of `count` polynomials with variant v, natural order
+// out, then out[i] *= fac.f[(i mod n) mod 3] when fac.on.  Variants: 1 = one
+// radix-2 butterfly per thread, 2 / 3 = 4 / 8 elements per thread with
+// twiddles read from the global table (these three in place, followed by a
+// bit-reversal pass and a factor pass), 4 / 5 = 4 / 8 elements per thread with
+// the pass's twiddles staged in shared memory (fused as above).
+static void ntt_transform(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *tw, int v,
+                          const ntt_factors &fac, cudaStream_t s)
 {
-    static const int el_env = [] {
-        const char *e = getenv("GB_NTT_ELEMS_LOG");
-        return e && (e[0] == '1' || e[0] == '2' || e[0] == '3') ? e[0] - '0' : 0;
+    const size_t n = (size_t)1 << log_n;
+    if (v >= 4 && log_n >= 3) {
+        ntt_staged(d, log_n, count, inverse, tw, v == 5 ? 3 : 2, fac, s);
+        return;
+    }
+    if (log_n > 0) ntt_passes(d, log_n, count, tw, v >= 4 ? 2 : v, s);
+    dim3 grid(blocks_for(n, 256), (unsigned)count);
+    bitrev_scale_kernel<<<grid, 256, 0, s>>>(d, log_n, false, fr_t::one());
+    GB_CHECK_LAUNCH();
+    if (fac.on) {
+        mul_period3_kernel<<<blocks_for(n * count, 256), 256, 0, s>>>(d, fac.f[0], fac.f[1], fac.f[2], n * count, n);
+        GB_CHECK_LAUNCH();
+    }
+}
+
+static int g_variant_forced = 0;
+
+// Variant: the staged-twiddle passes with 4 elements per thread, unless
+// GB_NTT_VARIANT (1..5) or gb_ntt_variant_set overrides; with the autotuner
+// on, each size times the five variants once on a scratch copy of one
+// transform.
+static int ntt_variant(fr_t *d, uint32_t log_n, bool inverse, const fr_t *tw, cudaStream_t s)
+{
+    static const int v_env = [] {
+        const char *e = getenv("GB_NTT_VARIANT");
+        return e && e[0] >= '1' && e[0] <= '5' ? e[0] - '0' : 0;
     }();
-    if (el_env) return el_env;
-    int el = log_n >= 18 ? 2 : 1;
-    if (!autotune_enabled() || log_n < 10) return el;
+    if (g_variant_forced) return g_variant_forced;
+    if (v_env) return v_env;
+    int v = log_n >= 3 ? 4 : 1;
+    if (!autotune_enabled() || log_n < 10) return v;
     const std::string key = "ntt:2^" + std::to_string(log_n);
-    if (autotune_lookup(key, &el)) return el;
+    if (autotune_lookup(key, &v)) return v;
     const size_t n = (size_t)1 << log_n;
     dev_buf<fr_t> scratch(n, s);
+    const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
     float best = 1e30f;
-    for (int cand = 1; cand <= 3; cand++) {
+    for (int cand = 1; cand <= 5; cand++) {
         GB_CUDA_OK(cudaMemcpyAsync(scratch.get(), d, n * sizeof(fr_t), cudaMemcpyDeviceToDevice, s));
-        float ms = time_on_stream(s, [&] { ntt_passes(scratch, log_n, 1, tw, cand, s); });
+        float ms = time_on_stream(s, [&] { ntt_transform(scratch, log_n, 1, inverse, tw, cand, none, s); });
         if (ms < best) {
             best = ms;
-            el = cand;
+            v = cand;
         }
     }
-    autotune_store(key, el);
-    return el;
+    autotune_store(key, v);
+    return v;
+}
+
+static void ntt_apply(fr_t *d, uint32_t log_n, size_t count, bool inverse, const ntt_factors &fac, cudaStream_t s)
+{
+    if (count == 0) return;
+    set_ntt_smem();
+    const fr_t *tw = log_n ? twiddles(log_n, inverse, s) : nullptr;
+    const int v = log_n ? ntt_variant(d, log_n, inverse, tw, s) : 1;
+    ntt_transform(d, log_n, count, inverse, tw, v, fac, s);
 }
 
 void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, cudaStream_t s)
 {
-    if (count == 0) return;
-    const size_t n = (size_t)1 << log_n;
-    if (log_n > 0) {
-        set_ntt_smem();
-        const fr_t *tw = twiddles(log_n, inverse, s);
-        ntt_passes(d, log_n, count, tw, ntt_variant(d, log_n, tw, s), s);
-    }
-    dim3 grid(blocks_for(n, 256), (unsigned)count);
-    bitrev_scale_kernel<<<grid, 256, 0, s>>>(d, log_n, scale != nullptr, scale ? *scale : fr_t::one());
-    GB_CHECK_LAUNCH();
+    ntt_factors fac{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+    if (scale) fac = ntt_factors{{*scale, *scale, *scale}, 1};
+    ntt_apply(d, log_n, count, inverse, fac, s);
 }
 
 void launch_mul_assign(fr_t *d, const fr_t &k, size_t len, cudaStream_t s)
@@ -379,6 +859,22 @@ void launch_coeff_to_extended_prepare(fr_t *out, const fr_t *in, const fr_t &fir
     GB_CHECK_LAUNCH();
 }
 
+// reads and clears the count of staged-pass CTAs whose twiddle copy did not
+// land within the spin limit; throws when there was one
+static uint32_t ntt_take_waits(cudaStream_t s)
+{
+    uint32_t h = 0, zero = 0;
+    GB_CUDA_OK(cudaMemcpyFromSymbolAsync(&h, g_ntt_wait_timeouts, sizeof(h), 0, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_OK(cudaMemcpyToSymbolAsync(g_ntt_wait_timeouts, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return h;
+}
+
+static void ntt_check_waits(cudaStream_t s)
+{
+    if (ntt_take_waits(s)) throw cuda_error((int)cudaErrorLaunchTimeout, "NTT twiddle copy did not complete");
+}
+
 // reference NTT semantics: inverse includes 1/n
 static void ntt_ref(fr_t *d, uint32_t log_n, size_t count, bool inverse, cudaStream_t s)
 {
@@ -388,6 +884,18 @@ static void ntt_ref(fr_t *d, uint32_t log_n, size_t count, bool inverse, cudaStr
     } else {
         ntt_inplace(d, log_n, count, false, nullptr, s);
     }
+}
+
+// ntt_ref, then out[i] *= scale * [1, first, second][(i mod n) mod 3] (the
+// reference's NTT followed by its scale-and-ZETA pass), with the factors
+// applied by the transform's last pass
+static void ntt_ref_zeta(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t &scale, const fr_t &first,
+                         const fr_t &second, cudaStream_t s)
+{
+    fr_t sc = scale;
+    if (inverse) sc = sc * host_fr_inverse(host_fr_from_u64((uint64_t)1 << log_n));
+    const ntt_factors fac{{sc, sc * first, sc * second}, 1};
+    ntt_apply(d, log_n, count, inverse, fac, s);
 }
 
 }  // namespace gb
@@ -410,6 +918,7 @@ RustError midnight_sppark_bls12_381_fr_ntt(RawFr *values_raw, uint32_t log_n, bo
     ntt_ref(d, log_n, 1, inverse, s);
     d2h(values, d, n * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    ntt_check_waits(s);
     return ok();
     GB_ENTRY_END
 }
@@ -428,10 +937,10 @@ RustError midnight_sppark_bls12_381_fr_ntt_zeta(RawFr *values_raw, uint32_t log_
     cudaStream_t s = lane_stream();
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
-    ntt_ref(d, log_n, 1, inverse, s);
-    launch_scale_zeta(d, scale, first, second, n, n, s);
+    ntt_ref_zeta(d, log_n, 1, inverse, scale, first, second, s);
     d2h(values, d, n * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    ntt_check_waits(s);
     return ok();
     GB_ENTRY_END
 }
@@ -453,10 +962,10 @@ RustError midnight_sppark_bls12_381_fr_divide_ntt_zeta(RawFr *values_raw, uint32
     h2d(d, values, n * sizeof(fr_t), s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(d, f, factor_len, n, s);
-    ntt_ref(d, log_n, 1, true, s);
-    launch_scale_zeta(d, scale, first, second, n, n, s);
+    ntt_ref_zeta(d, log_n, 1, true, scale, first, second, s);
     d2h(values, d, n * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    ntt_check_waits(s);
     return ok();
     GB_ENTRY_END
 }
@@ -481,6 +990,7 @@ RustError midnight_sppark_bls12_381_fr_coeff_to_extended_batch(RawFr *out_raw, c
     ntt_ref(dout, extended_log_n, count, false, s);
     d2h(out, dout, output_len * count * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
+    ntt_check_waits(s);
     return ok();
     GB_ENTRY_END
 }
@@ -560,8 +1070,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(void *device_vec, uin
     if (log_n > 31 || v->len != n) return make_error((int)cudaErrorInvalidValue, "resident NTT length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_ref(v->values, log_n, 1, inverse, s);
-    launch_scale_zeta(v->values, scale, first, second, n, n, s);
+    ntt_ref_zeta(v->values, log_n, 1, inverse, scale, first, second, s);
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -582,8 +1091,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(void *device_ve
     if (v->len != n * count) return make_error((int)cudaErrorInvalidValue, "resident NTT batch length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_ref(v->values, log_n, count, inverse, s);
-    launch_scale_zeta(v->values, scale, first, second, n * count, n, s);
+    ntt_ref_zeta(v->values, log_n, count, inverse, scale, first, second, s);
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -607,9 +1115,23 @@ RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_v
     dev_buf<fr_t> f(factor_len, s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(v->values, f, factor_len, n, s);
-    ntt_ref(v->values, log_n, 1, true, s);
-    launch_scale_zeta(v->values, scale, first, second, n, n, s);
+    ntt_ref_zeta(v->values, log_n, 1, true, scale, first, second, s);
     device_vec_mark_ready(v, s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// Forces the NTT pass variant (1..5; see ntt_transform), or 0 for the default
+// or autotuned choice.  Process-wide.
+void gb_ntt_variant_set(int variant) { g_variant_forced = variant >= 1 && variant <= 5 ? variant : 0; }
+
+// Staged-pass CTAs, since the last call, whose twiddle copy did not complete
+// within the spin limit (their transform is not valid); the count is reset.
+RustError gb_ntt_wait_timeouts(uint32_t *out)
+{
+    if (!out) return make_error((int)cudaErrorInvalidValue, "null output");
+    GB_ENTRY_BEGIN
+    *out = ntt_take_waits(lane_stream());
     return ok();
     GB_ENTRY_END
 }

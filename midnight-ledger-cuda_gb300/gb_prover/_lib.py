@@ -112,6 +112,7 @@ def _declare(L):
         "gb_g1_generator_mul": (E, [vp, vp, sz]),
         "gb_g1_generator_mul_device": (E, [vp, vp, sz]),
         "gb_imad_peak": (E, [ctypes.POINTER(ctypes.c_double)]),
+        "gb_imad_probe": (E, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
         "gb_g1_to_lagrange": (E, [vp, vp, u32]),
         "midnight_sppark_bls12_381_fr_device_eval_polys": (E, [vp, vp, sz, sz, fr]),
         "gb_fr_device_kate_divide": (E, [vp, vp, sz, sz, fr]),
@@ -139,6 +140,8 @@ def _declare(L):
         "gb_fr_random_chacha20": (E, [vp, vp, ctypes.c_uint64, sz, vp]),
         "gb_fr_lookup_permute_device": (E, [vp, vp, sz, sz, sz, vp, vp]),
         "gb_autotune_set": (None, [ctypes.c_int]),
+        "gb_ntt_variant_set": (None, [ctypes.c_int]),
+        "gb_ntt_wait_timeouts": (E, [ctypes.POINTER(ctypes.c_uint32)]),
         "gb_autotune_reset": (None, []),
         "gb_autotune_report": (sz, [vp, sz]),
     }

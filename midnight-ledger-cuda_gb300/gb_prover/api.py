@@ -19,7 +19,7 @@ __all__ = [
     "bls12_381_fr_invert_assign", "bls12_381_fr_sort_canonical", "bls12_381_fr_poly_lincomb",
     "bls12_381_fr_shifted_prefix_product", "bls12_381_fr_permutation_products", "bls12_381_fr_lookup_products",
     "bls12_381_fr_lookup_products_device", "bls12_381_fr_device_quotient_pieces",
-    "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "transfer_counters",
+    "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "imad_probe", "ntt_variant_set", "ntt_wait_timeouts", "transfer_counters",
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
@@ -376,6 +376,14 @@ def imad_peak():
     return v.value
 
 
+def imad_probe(form):
+    """Multiply-adds per second of one probe form (0 = mad.wide chains,
+    1..3 = carry-chained rows with 1, 2, 4 accumulator sets per thread)."""
+    v = ctypes.c_double()
+    check(lib().gb_imad_probe(int(form), ctypes.byref(v)))
+    return v.value
+
+
 def transfer_counters():
     a, b = ctypes.c_uint64(), ctypes.c_uint64()
     lib().gb_transfer_counters(ctypes.byref(a), ctypes.byref(b))
@@ -575,6 +583,18 @@ def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, inpu
 
 
 # ---------------------------------------------------------------- autotuner
+
+def ntt_variant_set(variant):
+    """Force the NTT pass variant (1..5, see gb_ntt_variant_set); 0 = default."""
+    lib().gb_ntt_variant_set(int(variant))
+
+
+def ntt_wait_timeouts():
+    """Staged NTT passes whose twiddle copy timed out since the last call."""
+    v = ctypes.c_uint32()
+    check(lib().gb_ntt_wait_timeouts(ctypes.byref(v)))
+    return v.value
+
 
 def autotune_set(enabled=True):
     lib().gb_autotune_set(1 if enabled else 0)

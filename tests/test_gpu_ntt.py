@@ -88,6 +88,29 @@ def test_lde_round_trip_with_zeta(gb, orc):
     assert (back[1 << k:] == 0).all()
 
 
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
+def test_ntt_variants(gb, orc, variant):
+    """Every pass variant, bit-exact: single transforms at sizes whose pass
+    splits differ (one pass, 5+5, 6+5, 8+8, 7+7+7 ...) and a batch of 3 (the
+    staged passes pack several sub-blocks, and several transforms, per CTA)."""
+    gb.ntt_variant_set(variant)
+    try:
+        for log_n, count in ((3, 1), (7, 3), (10, 2), (11, 1), (13, 3), (16, 2), (21, 1)):
+            rng = np.random.default_rng(100 * variant + log_n)
+            v = orc.fr_random(count << log_n, rng)
+            one = orc.fr_const(orc.CONST_ONE)
+            for inverse in (False, True):
+                dv = gb.Bls12_381FrDeviceVec.upload(v)
+                dv.ntt_zeta_batch(log_n, count, inverse, one, one, one)
+                got = dv.download()
+                for p in range(count):
+                    seg = v[p << log_n:(p + 1) << log_n]
+                    assert (got[p << log_n:(p + 1) << log_n] == orc.fr_ntt(seg, log_n, inverse)).all(), (log_n, p)
+        assert gb.ntt_wait_timeouts() == 0
+    finally:
+        gb.ntt_variant_set(0)
+
+
 def test_device_vec_batch_ntt(gb, orc):
     log_n, count = 10, 5
     rng = np.random.default_rng(33)

@@ -54,6 +54,16 @@ def test_config3_full_proof(gb):
     assert plonk_verify.verify(hpk, gproof, TAU)
 
 
+def test_k18_full_proof(gb):
+    """k = 18, 3 advice columns, the standard gate, 2^16 copy constraints,
+    one 2-column lookup into a 2^14-row table: identical proof bytes,
+    verified."""
+    c = circuit(18, 3, 3, 1, copies=1 << 16, table_log=14, label="synthetic PLONK/KZG proof, k=18")
+    hpk, gproof, hproof = prove_both(c)
+    assert gproof == hproof
+    assert plonk_verify.verify(hpk, gproof, TAU)
+
+
 @pytest.mark.parametrize("u,n,tsize,dup", [(250, 256, 32, False), (4090, 4096, 4000, False), (65529, 65536, 4096, True),
                                            (1000, 1024, 1, True)])
 def test_device_lookup_permutation_matches_host(gb, orc, u, n, tsize, dup):
