@@ -363,8 +363,8 @@ __global__ void msm_fixup_kernel(const uint32_t *__restrict__ starts, uint32_t G
         return;
     }
     xyzz_t acc = tail[cs];
-    for (uint32_t c = cs + 1; c < ce; c++) acc.add(tail[c]);
-    acc.add(head[ce]);
+    for (uint32_t c = cs + 1; c < ce; c++) acc.GB_ADD_LAT(tail[c]);
+    acc.GB_ADD_LAT(head[ce]);
     buckets[g] = acc;
 }
 
@@ -385,13 +385,13 @@ __global__ void __launch_bounds__(256) msm_fixup_long_kernel(const uint32_t *__r
         const uint32_t cs = starts[g] / L, ce = (starts[g + 1] - 1) / L;
         // partials: tail[cs], tail[cs+1 .. ce-1], head[ce]
         xyzz_t acc = xyzz_t::inf();
-        for (uint32_t c = cs + threadIdx.x; c <= ce; c += blockDim.x) acc.add(c == ce ? head[c] : tail[c]);
+        for (uint32_t c = cs + threadIdx.x; c <= ce; c += blockDim.x) acc.GB_ADD_LAT(c == ce ? head[c] : tail[c]);
         sh[threadIdx.x] = acc;
         __syncthreads();
         for (uint32_t off = 128; off > 0; off >>= 1) {
             if (threadIdx.x < off) {
                 xyzz_t v = sh[threadIdx.x];
-                v.add(sh[threadIdx.x + off]);
+                v.GB_ADD_LAT(sh[threadIdx.x + off]);
                 sh[threadIdx.x] = v;
             }
             __syncthreads();
@@ -418,10 +418,10 @@ __global__ void __launch_bounds__(128) msm_reduce_partial_kernel(const xyzz_t *_
         const xyzz_t *B = buckets + (size_t)seg * K;
         xyzz_t run = xyzz_t::inf();
         for (uint32_t k = k0 + m; k-- > k0;) {
-            run.add(B[k]);
-            sum.add(run);
+            run.GB_ADD_LAT(B[k]);
+            sum.GB_ADD_LAT(run);
         }
-        if (k0) sum.add(xyzz_mul_small(run, k0));
+        if (k0) sum.GB_ADD_LAT(xyzz_mul_small(run, k0));
     }
     sh[threadIdx.x] = sum;
     __syncthreads();
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(128) msm_reduce_partial_kernel(const xyzz_t *_
     for (uint32_t off = group / 2; off > 0; off >>= 1) {
         if ((threadIdx.x & (group - 1)) < off) {
             xyzz_t v = sh[threadIdx.x];
-            v.add(sh[threadIdx.x + off]);
+            v.GB_ADD_LAT(sh[threadIdx.x + off]);
             sh[threadIdx.x] = v;
         }
         __syncthreads();
@@ -447,13 +447,13 @@ __global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__rest
     const xyzz_t *src = in + (size_t)seg * n;
     uint32_t i0 = blockIdx.x * 512 + threadIdx.x, i1 = i0 + 256;
     xyzz_t acc = i0 < n ? src[i0] : xyzz_t::inf();
-    if (i1 < n) acc.add(src[i1]);
+    if (i1 < n) acc.GB_ADD_LAT(src[i1]);
     sh[threadIdx.x] = acc;
     __syncthreads();
     for (uint32_t off = 128; off > 0; off >>= 1) {
         if (threadIdx.x < off) {
             xyzz_t v = sh[threadIdx.x];
-            v.add(sh[threadIdx.x + off]);
+            v.GB_ADD_LAT(sh[threadIdx.x + off]);
             sh[threadIdx.x] = v;
         }
         __syncthreads();
@@ -471,8 +471,8 @@ __global__ void msm_combine_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t 
     xyzz_t acc = xyzz_t::inf();
     for (int w = (int)segs_per_item - 1; w >= 0; w--) {
         if (w != (int)segs_per_item - 1)
-            for (int k = 0; k < c; k++) acc = acc.dbl();
-        acc.add(ss[w]);
+            for (int k = 0; k < c; k++) acc = acc.GB_DBL_LAT();
+        acc.GB_ADD_LAT(ss[w]);
     }
     out[m] = acc.to_jacobian();
 }

@@ -179,13 +179,14 @@ __global__ void ntt_dif_pass_reg_kernel(fr_t *data, uint32_t log_n, int s_hi, in
 //
 // Shared memory is addressed in 16-byte chunks.  Element t of a sub-block
 // occupies chunks 2t and 2t+1 of its 128-byte row r = t/4, permuted inside
-// the row by r ^ (r >> 1) ^ (r >> 2) and, for the data, by a twist of the
-// sub-block number, so that the gathers of every radix-2^R group (the
-// remainder group first, at the top bits), the twiddle reads and the
-// strided global loads are free of bank conflicts for g >= 5.  The global
+// the row by r ^ (r >> 1) ^ (r >> 2) ^ (r >> 4) and, for the data, by a
+// twist of the sub-block number, so that the gathers of every radix-2^R
+// group (the remainder group first, at the top bits), the twiddle reads and
+// the strided global loads are free of bank conflicts for g >= 5 (the last
+// pass's bit-reversed reads keep a few).  The global
 // twiddle table is stored in the same permuted order, so the bulk copy
 // lands it ready to use.
-__host__ __device__ __forceinline__ uint32_t ntt_swz_row(uint32_t r) { return (r ^ (r >> 1) ^ (r >> 2)) & 7u; }
+__host__ __device__ __forceinline__ uint32_t ntt_swz_row(uint32_t r) { return (r ^ (r >> 1) ^ (r >> 2) ^ (r >> 4)) & 7u; }
 __host__ __device__ __forceinline__ uint32_t ntt_twist(uint32_t q) { return (q & 1u) | ((q & 2u) << 1) | ((q & 4u) >> 1); }
 __host__ __device__ __forceinline__ uint32_t ntt_chunk(uint32_t t, uint32_t h, uint32_t x)
 {
@@ -207,6 +208,100 @@ __device__ __forceinline__ void ntt_st(uint4 *s, uint32_t t, uint32_t x, const f
     s[ntt_chunk(t, 0, x)] = make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
     s[ntt_chunk(t, 1, x)] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
 }
+
+// Butterfly arithmetic of the staged passes.  The values between stages and
+// passes are kept in [0, 2r) (Harvey's lazy butterflies): a product x * w
+// with x < 2r and a twiddle w < r is below 2r without the Montgomery
+// product's final subtraction, and sums and differences are reduced mod 2r;
+// the last pass reduces its outputs to [0, r).  Measured on GB300 this makes
+// the transform 7% faster than reducing every result; GB_NTT_EAGER selects
+// the fully reduced form.
+#if !defined(GB_NTT_EAGER)
+__device__ __forceinline__ fr_t bfly_add(const fr_t &a, const fr_t &b)
+{
+    fr_t r;
+    uint32_t s[8], t[8], c, br;
+    asm("add.cc.u32 %0, %9, %17;\n\t"
+        "addc.cc.u32 %1, %10, %18;\n\t"
+        "addc.cc.u32 %2, %11, %19;\n\t"
+        "addc.cc.u32 %3, %12, %20;\n\t"
+        "addc.cc.u32 %4, %13, %21;\n\t"
+        "addc.cc.u32 %5, %14, %22;\n\t"
+        "addc.cc.u32 %6, %15, %23;\n\t"
+        "addc.cc.u32 %7, %16, %24;\n\t"
+        "addc.u32 %8, 0, 0;"
+        : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]), "=r"(c)
+        : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+          "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+    // 2r = 0xe7db4ea6 533afa90 6673b010 1343b00a a77b4805 fffcb7fd fffffffe 00000002
+    asm("sub.cc.u32 %0, %9, 0x00000002;\n\t"
+        "subc.cc.u32 %1, %10, 0xfffffffe;\n\t"
+        "subc.cc.u32 %2, %11, 0xfffcb7fd;\n\t"
+        "subc.cc.u32 %3, %12, 0xa77b4805;\n\t"
+        "subc.cc.u32 %4, %13, 0x1343b00a;\n\t"
+        "subc.cc.u32 %5, %14, 0x6673b010;\n\t"
+        "subc.cc.u32 %6, %15, 0x533afa90;\n\t"
+        "subc.cc.u32 %7, %16, 0xe7db4ea6;\n\t"
+        "subc.u32 %8, %17, 0;"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]), "=r"(br)
+        : "r"(s[0]), "r"(s[1]), "r"(s[2]), "r"(s[3]), "r"(s[4]), "r"(s[5]), "r"(s[6]), "r"(s[7]), "r"(c));
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = br ? s[i] : t[i];
+    return r;
+}
+
+__device__ __forceinline__ fr_t bfly_sub(const fr_t &a, const fr_t &b)
+{
+    fr_t r;
+    uint32_t d[8], t[8], br;
+    asm("sub.cc.u32 %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32 %8, 0, 0;"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]), "=r"(br)
+        : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+          "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+    asm("add.cc.u32 %0, %8, 0x00000002;\n\t"
+        "addc.cc.u32 %1, %9, 0xfffffffe;\n\t"
+        "addc.cc.u32 %2, %10, 0xfffcb7fd;\n\t"
+        "addc.cc.u32 %3, %11, 0xa77b4805;\n\t"
+        "addc.cc.u32 %4, %12, 0x1343b00a;\n\t"
+        "addc.cc.u32 %5, %13, 0x6673b010;\n\t"
+        "addc.cc.u32 %6, %14, 0x533afa90;\n\t"
+        "addc.u32 %7, %15, 0xe7db4ea6;"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
+        : "r"(d[0]), "r"(d[1]), "r"(d[2]), "r"(d[3]), "r"(d[4]), "r"(d[5]), "r"(d[6]), "r"(d[7]));
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = br ? t[i] : d[i];
+    return r;
+}
+
+__device__ __forceinline__ fr_t bfly_mul(const fr_t &x, const fr_t &w)
+{
+    fr_t r;
+#if defined(__CUDA_ARCH__)
+    mont_mul_device<FrCfg, false>(r.v, x.v, w.v);
+#endif
+    return r;
+}
+
+// [0, 2r) -> [0, r)
+__device__ __forceinline__ fr_t bfly_out(fr_t v)
+{
+    fr_t::reduce_once(v.v, 0);
+    return v;
+}
+#else
+__device__ __forceinline__ fr_t bfly_add(const fr_t &a, const fr_t &b) { return a + b; }
+__device__ __forceinline__ fr_t bfly_sub(const fr_t &a, const fr_t &b) { return a - b; }
+__device__ __forceinline__ fr_t bfly_mul(const fr_t &x, const fr_t &w) { return x * w; }
+__device__ __forceinline__ fr_t bfly_out(fr_t v) { return v; }
+#endif
 
 // chunk(t, h, x) = lin(t) ^ h ^ x, with lin linear over GF(2) in the bits
 // of t: addresses of elements whose indices differ in known bits are found
@@ -288,9 +383,9 @@ __device__ __forceinline__ void ntt_tw_group(uint4 *sd, const uint4 *stw, uint32
                 const int k1 = k + hk;
                 const int key = (k & (hk - 1)) | ((k >> R) << lh);
                 const fr_t a = x[k], c = x[k1];
-                x[k] = a + c;
-                fr_t diff = a - c;
-                if (!one[key]) diff = diff * w[key];
+                x[k] = bfly_add(a, c);
+                fr_t diff = bfly_sub(a, c);
+                if (!one[key]) diff = bfly_mul(diff, w[key]);
                 x[k1] = diff;
             }
         }
@@ -474,6 +569,8 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
             const size_t i_nat = ((size_t)r << nb_log) + col;
             addr = ((F >> nb_log) << log_n) + i_nat;
             fr_t v = ntt_ld(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u));
+            // x * f with x < 2r, f < r is fully reduced by the product
+            if (!fac.on) v = bfly_out(v);
             if (fac.on) {
                 const uint32_t c = (uint32_t)(i_nat % 3);
                 fr_t f;
