@@ -214,6 +214,11 @@ def main():
     ap.add_argument("--log-n", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--case", default="msm", choices=["msm", "ntt", "ntt-queue"],
+                    help="msm: the benchmark line; ntt / ntt-queue: only the resident NTT batch of --count "
+                         "transforms of 2^--log-n, or the 64-transform ragged batch in one launch (small "
+                         "cases for profilers; one JSON line of timings)")
+    ap.add_argument("--count", type=int, default=16)
     args = ap.parse_args()
     args.n = 1 << args.log_n
     args.n_ref = min(args.n, 1 << 18)  # bounded CPU sample: one 2^18 MSM (~3 s on 8 cores)
@@ -221,6 +226,9 @@ def main():
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.case != "msm":
+        run_ntt_case(args)
         return
 
     import torch
@@ -356,6 +364,45 @@ def main():
         dist.destroy_process_group()
 
 
+def run_ntt_case(args):
+    """--case ntt | ntt-queue: resident forward NTTs only, timed with CUDA
+    events on the library's lane stream (W untimed, K timed calls)."""
+    import torch
+    import gb_prover as gb
+    torch.cuda.set_device(0)
+    gb.lib()
+    rng = np.random.default_rng(7)
+    one = np.array([0x00000001FFFFFFFE, 0x5884B7FA00034802, 0x998C4FEFECBC4FF5, 0x1824B159ACC5056F], np.uint64)
+    if args.case == "ntt":
+        logs = [args.log_n] * args.count
+    else:
+        logs = sorted((max(1, (int(round(2 ** u)) - 1).bit_length()) for u in rng.uniform(10, 18, size=64)),
+                      reverse=True)
+    offs = np.concatenate([[0], np.cumsum([1 << lg for lg in logs])[:-1]]).astype(np.uint64)
+    dv = gb.Bls12_381FrDeviceVec.upload(fr_uniform(int(sum(1 << lg for lg in logs)), rng))
+
+    def call():
+        if args.case == "ntt":
+            dv.ntt_zeta_batch(args.log_n, args.count, False, one, one, one)
+        else:
+            dv.ntt_ragged(offs, logs, False, one, one, one)
+
+    stream = torch.cuda.ExternalStream(gb.lane_stream())
+    for _ in range(args.warmup):
+        call()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    fr_mul = sum((1 << (lg - 1)) * lg for lg in logs)
+    print(json.dumps({"case": args.case, "transforms": len(logs), "elements": int(sum(1 << lg for lg in logs)),
+                      "ms": ms, "best_ms": min(ms), "tmadd_per_s": fr_mul * 136 / min(ms) / 1e9}))
+
+
 def mixed_scalars(n, rng):
     """70% uniform Fr, 20% uniform below 2^64, 10% zero."""
     s = fr_uniform(n, rng)
@@ -418,6 +465,15 @@ def batched_config(gb, torch, rng):
                                              for lg in vecs])
     out["ntt64_one_at_a_time_ms"] = timed(lambda: [v.ntt_zeta(lg, False, one, one, one)
                                                    for lg in singles for v in singles[lg]])
+    # all 64 NTTs, of every size, in one persistent launch fed by the device
+    # work queue (one vector holding the 64 polynomials back to back)
+    order = sorted(range(64), key=lambda j: -logs[j])
+    q_logs = [logs[j] for j in order]
+    q_offs = np.concatenate([[0], np.cumsum([1 << lg for lg in q_logs])[:-1]]).astype(np.uint64)
+    qv = gb.Bls12_381FrDeviceVec.upload(fr_uniform(int(sum(1 << lg for lg in q_logs)), rng))
+    out["ntt64_queue_ms"] = timed(lambda: qv.ntt_ragged(q_offs, q_logs, False, one, one, one))
+    out["ntt64_queue_launches"] = 1
+    del qv
     # the same two batches with the autotuner choosing the window and the NTT
     # pass variant (the first call of each key tunes; then timed as above)
     gb.autotune_reset()

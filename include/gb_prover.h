@@ -353,8 +353,19 @@ GB_API void gb_autotune_set(int enabled);
  * autotuned choice */
 GB_API void gb_ntt_variant_set(int variant);
 /* staged NTT passes whose twiddle copy did not complete within the spin
- * limit since the last call (their output is invalid); resets the count */
+ * limit, plus work-queue waits that ran out, since the last call (their
+ * output is invalid); resets the count */
 GB_API RustError gb_ntt_wait_timeouts(uint32_t *out);
+/* NTTs of `count` polynomials of different sizes held in one device vector,
+ * in one persistent launch fed by a device work queue: polynomial j is the
+ * 2^log_ns[j] values at element offset offsets[j] (ranges inside the vector,
+ * not overlapping, log_ns[j] <= 30) and gets the semantics of
+ * midnight_sppark_bls12_381_fr_device_vec_ntt_zeta (inverse includes 1/n,
+ * then out[i] *= scale * [1, first, second][i mod 3]; a single value is
+ * left unchanged).  Sizes of 2 and 4 values take the plain path.  The batched form of the reference's
+ * one-transform-per-call device NTT (bls12_381_g1_msm.cu:3280-3380). */
+GB_API RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, const uint32_t *log_ns,
+                                             size_t count, bool inverse, RawFr scale, RawFr first, RawFr second);
 GB_API void gb_autotune_reset(void);
 /* "key=value;" per tuned key into buf (NUL-terminated, truncated); returns
  * the full length */

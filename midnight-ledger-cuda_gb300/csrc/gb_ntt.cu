@@ -396,17 +396,18 @@ __device__ __forceinline__ void ntt_tw_group(uint4 *sd, const uint4 *stw, uint32
 
 static constexpr unsigned kWaitSpins = 1u << 24;
 
-// bounded wait on phase 0 of an mbarrier; true when the phase completed
-__device__ __forceinline__ bool mbar_wait0(uint32_t mbar)
+// bounded wait on the phase of an mbarrier with the given parity; true when
+// the phase completed
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
 {
     for (unsigned i = 0; i < kWaitSpins; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(mbar)
+            : "r"(mbar), "r"(parity)
             : "memory");
         if (done) return true;
     }
@@ -436,21 +437,24 @@ __device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bit
 // outputs land in column F mod NB of the natural order, i.e. sub-block
 // bitrev(F mod NB): element t of it is output bitrev(t) * NB + (F mod NB),
 // so the Q sub-blocks of a CTA write Q adjacent outputs per row.
-template <int EL, bool LAST>
-__global__ void __launch_bounds__(1024 >> EL, 3)
-    ntt_dif_pass_tw_kernel(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q, size_t count,
-                           const fr_t *__restrict__ twt, ntt_factors fac)
+//
+// ntt_tw_piece runs the part of a pass that CTA `cta` of the per-pass grid
+// covers; it returns false (for every thread) when the twiddle copy did not
+// land.  QUEUE selects the form that the persistent work-queue kernel runs:
+// the block may be wider than the piece (the extra threads sit out the
+// butterfly groups), the sources are read through L2 because other CTAs of
+// the same launch wrote them, and the mbarrier completes one phase per piece.
+template <int EL, bool LAST, bool QUEUE>
+__device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q,
+                                             size_t count, const fr_t *__restrict__ twt, const ntt_factors &fac,
+                                             size_t cta, uint4 *smem, uint32_t mbar, uint32_t parity, int &copy_ok)
 {
-    extern __shared__ uint4 smem[];
-    __shared__ uint64_t mbar_store;
-    __shared__ int copy_ok;
     const int s_lo = s_hi - g + 1;
     const uint32_t sub = 1u << g, Q = 1u << q, nd = Q << g;
     const size_t n = (size_t)1 << log_n;
     const uint32_t tw_entries = s_lo > 0 ? nd : sub;
     uint4 *sd = smem;
     uint4 *stw = smem + 2 * (size_t)nd;
-    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_store);
     const int nb_log = (int)log_n - g;                 // log2 sub-blocks per transform
     const size_t total = count << nb_log;              // sub-blocks in the batch
     const bool q_fast = !LAST || nb_log >= q;          // LAST: Q adjacent columns of one transform
@@ -458,19 +462,17 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
     size_t poly = 0, b0 = 0;
     const fr_t *twsrc = twt;
     if (s_lo > 0) {
-        poly = blockIdx.x % count;
-        b0 = (size_t)(blockIdx.x / count) << q;
+        poly = cta % count;
+        b0 = (size_t)(cta / count) << q;
         twsrc = twt + ((b0 & (((size_t)1 << s_lo) - 1)) << g);
     } else {
-        b0 = (size_t)blockIdx.x << q;
+        b0 = cta << q;
     }
 
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+        // the previous piece's generic reads of the twiddle buffer are done
+        // (barrier); order them before the async-proxy write
+        if (QUEUE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const uint32_t bytes = tw_entries * (uint32_t)sizeof(fr_t);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
         asm volatile(
@@ -502,24 +504,35 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
                 addr = (F << g) + t;
             }
         }
-        const fr_t v = valid ? src[addr] : fr_t::zero();
+        fr_t v = fr_t::zero();
+        if (valid) {
+            if (QUEUE) {
+                const uint4 *p = reinterpret_cast<const uint4 *>(src + addr);
+                const uint4 lo = __ldcg(p), hi = __ldcg(p + 1);
+                v.v[0] = lo.x, v.v[1] = lo.y, v.v[2] = lo.z, v.v[3] = lo.w;
+                v.v[4] = hi.x, v.v[5] = hi.y, v.v[6] = hi.z, v.v[7] = hi.w;
+            } else {
+                v = src[addr];
+            }
+        }
         ntt_st(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u), v);
     }
     if (threadIdx.x == 0) {
-        bool ok = mbar_wait0(mbar);
+        bool ok = mbar_wait(mbar, parity);
         if (!ok) {
             atomicAdd(&g_ntt_wait_timeouts, 1u);
-            mbar_wait0(mbar);  // let the copy in flight land before the CTA exits
+            mbar_wait(mbar, parity);  // let the copy in flight land before the CTA exits
         }
         copy_ok = ok;
     }
     __syncthreads();
-    if (!copy_ok) return;
+    if (!copy_ok) return false;
 
     // radix-2^EL groups; the remainder group first, at the top bits
     {
-        const uint32_t per_sub = sub >> EL;  // threads per sub-block; blockDim.x = nd >> EL
-        const uint32_t qq = threadIdx.x / per_sub, ul = threadIdx.x % per_sub;
+        const uint32_t per_sub = sub >> EL;  // threads per sub-block; nd >> EL threads take part
+        const bool part = !QUEUE || threadIdx.x < (nd >> EL);
+        const uint32_t qq = part ? threadIdx.x / per_sub : 0, ul = threadIdx.x % per_sub;
         uint4 *sdq = sd + 2 * (size_t)qq * sub;
         const uint4 *stq = stw + (s_lo > 0 ? 2 * (size_t)qq * sub : 0);
         const uint32_t twist = ntt_twist(qq & 7u);
@@ -527,13 +540,17 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
         int top = g;
         const int rem = g % EL;
         if (rem) {
-            if (EL == 3 && rem == 2) ntt_tw_group<EL, (EL == 3 ? 2 : 1)>(sdq, stq, ul, g - rem, twist, lo_zero);
-            else ntt_tw_group<EL, 1>(sdq, stq, ul, g - rem, twist, lo_zero);
+            if (!part) {
+            } else if (EL == 3 && rem == 2) {
+                ntt_tw_group<EL, (EL == 3 ? 2 : 1)>(sdq, stq, ul, g - rem, twist, lo_zero);
+            } else {
+                ntt_tw_group<EL, 1>(sdq, stq, ul, g - rem, twist, lo_zero);
+            }
             top -= rem;
             __syncthreads();
         }
         while (top > 0) {
-            ntt_tw_group<EL, EL>(sdq, stq, ul, top - EL, twist, lo_zero);
+            if (part) ntt_tw_group<EL, EL>(sdq, stq, ul, top - EL, twist, lo_zero);
             top -= EL;
             __syncthreads();
         }
@@ -582,6 +599,137 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
             continue;
         }
         dst[addr] = ntt_ld(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u));
+    }
+    return true;
+}
+
+template <int EL, bool LAST>
+__global__ void __launch_bounds__(1024 >> EL, 3)
+    ntt_dif_pass_tw_kernel(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q, size_t count,
+                           const fr_t *__restrict__ twt, ntt_factors fac)
+{
+    extern __shared__ uint4 smem[];
+    __shared__ uint64_t mbar_store;
+    __shared__ int copy_ok;
+    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_store);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    ntt_tw_piece<EL, LAST, false>(src, dst, log_n, s_hi, g, q, count, twt, fac, blockIdx.x, smem, mbar, 0, copy_ok);
+}
+
+// ---------------------------------------------------------------- work queue
+// A ragged batch of transforms (different sizes) in one persistent launch.
+// The host lists every piece of every pass of every transform as a work item,
+// all first-pass pieces first, then all second-pass pieces, and so on.  Each
+// CTA takes the next item from a device counter; a piece of pass p > 0 waits
+// until all pieces of pass p - 1 of its transform are done (a per-(transform,
+// pass) completion counter).  Items are taken in list order, so an item only
+// ever waits for items taken earlier by CTAs that are running, and those wait
+// only for items taken before them: the launch cannot deadlock whatever the
+// number of resident CTAs.  Every wait is bounded; a wait that runs out, or a
+// twiddle copy that does not land, raises the abort flag, which ends the
+// launch early and is reported to the host.
+struct ntt_qpass {
+    const fr_t *src;
+    fr_t *dst;
+    const fr_t *tw;
+    uint32_t pieces;
+    int s_hi, g, q;
+};
+
+struct ntt_qjob {
+    ntt_qpass pass[3];
+    ntt_factors fac;
+    uint32_t log_n, npass, counter;  // counter: index of pass 0's completion counter
+};
+
+// control words of one launch: next item, abort flag, then the completion
+// counters (zeroed before the launch)
+enum { NTT_Q_NEXT = 0, NTT_Q_ABORT = 1, NTT_Q_COUNTERS = 2 };
+static constexpr unsigned kQueueSpins = 1u << 22;
+static constexpr uint32_t kQueuePieceBits = 24;
+
+__device__ unsigned int g_ntt_queue_timeouts;
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <int EL>
+__global__ void __launch_bounds__(1024 >> EL, 3)
+    ntt_queue_kernel(const ntt_qjob *__restrict__ jobs, const uint2 *__restrict__ items, uint32_t n_items,
+                     uint32_t *ctl)
+{
+    extern __shared__ uint4 smem[];
+    __shared__ uint64_t mbar_store;
+    __shared__ int copy_ok;
+    __shared__ uint32_t cur;
+    __shared__ int go;
+    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_store);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    uint32_t parity = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t it = atomicAdd(&ctl[NTT_Q_NEXT], 1u);
+            int ok = it < n_items && !ld_acquire_u32(&ctl[NTT_Q_ABORT]);
+            if (ok) {
+                const uint2 w = items[it];
+                const uint32_t pass = w.y >> kQueuePieceBits;
+                if (pass > 0) {
+                    const ntt_qjob &J = jobs[w.x];
+                    const uint32_t need = J.pass[pass - 1].pieces;
+                    const uint32_t *c = &ctl[NTT_Q_COUNTERS + J.counter + pass - 1];
+                    unsigned i = 0;
+                    for (; i < kQueueSpins; i++) {
+                        if (ld_acquire_u32(c) >= need) break;
+                        if (ld_acquire_u32(&ctl[NTT_Q_ABORT])) {
+                            ok = 0;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                    if (i == kQueueSpins) {
+                        atomicAdd(&g_ntt_queue_timeouts, 1u);
+                        atomicExch(&ctl[NTT_Q_ABORT], 1u);
+                        ok = 0;
+                    }
+                }
+            }
+            cur = it;
+            go = ok;
+        }
+        __syncthreads();
+        if (!go) break;
+        const uint2 w = items[cur];
+        const uint32_t pass = w.y >> kQueuePieceBits, piece = w.y & ((1u << kQueuePieceBits) - 1);
+        const ntt_qjob &J = jobs[w.x];
+        const ntt_qpass &P = J.pass[pass];
+        bool ok;
+        if (pass + 1 == J.npass) {
+            ok = ntt_tw_piece<EL, true, true>(P.src, P.dst, J.log_n, P.s_hi, P.g, P.q, 1, P.tw, J.fac, piece, smem,
+                                              mbar, parity, copy_ok);
+        } else {
+            const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+            ok = ntt_tw_piece<EL, false, true>(P.src, P.dst, J.log_n, P.s_hi, P.g, P.q, 1, P.tw, none, piece, smem,
+                                               mbar, parity, copy_ok);
+        }
+        parity ^= 1u;
+        __syncthreads();  // every store of the piece is issued
+        if (threadIdx.x == 0) {
+            if (!ok) atomicExch(&ctl[NTT_Q_ABORT], 1u);
+            __threadfence();
+            atomicAdd(&ctl[NTT_Q_COUNTERS + J.counter + pass], 1u);
+        }
+        if (!ok) break;
     }
 }
 
@@ -726,6 +874,7 @@ void set_ntt_smem()
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
+        cudaFuncSetAttribute(ntt_queue_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
     });
 }
 
@@ -817,6 +966,88 @@ static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, cons
         }
         GB_CHECK_LAUNCH();
     }
+}
+
+// A ragged batch: transform j is the 2^log_ns[j] values at d + offsets[j],
+// with the output factors fac[j], in one launch of the work-queue kernel
+// (staged passes, 4 elements per thread).  Transforms with two or more
+// passes run through a scratch copy as ntt_staged does; every size needs
+// log_ns[j] >= 3.  Returns the number of launches (0 or 1).
+static int ntt_ragged(fr_t *d, const size_t *offsets, const uint32_t *log_ns, const ntt_factors *fac, size_t count,
+                      bool inverse, cudaStream_t s)
+{
+    set_ntt_smem();
+    std::vector<ntt_qjob> jobs(count);
+    size_t tmp_len = 0;
+    uint32_t counters = 0;
+    for (size_t j = 0; j < count; j++)
+        if (pass_split(log_ns[j]).size() > 1) tmp_len += (size_t)1 << log_ns[j];
+    dev_buf<fr_t> tmp(tmp_len, s);
+    size_t tmp_off = 0, max_passes = 0;
+    for (size_t j = 0; j < count; j++) {
+        const uint32_t log_n = log_ns[j];
+        const auto passes = pass_split(log_n);
+        const size_t P = passes.size();
+        if (P > 3) throw cuda_error((int)cudaErrorInvalidValue, "ragged NTT size above 2^30");
+        const fr_t *tw = twiddles(log_n, inverse, s);
+        fr_t *dj = d + offsets[j];
+        fr_t *tj = P > 1 ? tmp.get() + tmp_off : nullptr;
+        if (P > 1) tmp_off += (size_t)1 << log_n;
+        ntt_qjob &J = jobs[j];
+        J.fac = fac[j];
+        J.log_n = log_n;
+        J.npass = (uint32_t)P;
+        J.counter = counters;
+        counters += (uint32_t)P;
+        max_passes = std::max(max_passes, P);
+        for (size_t i = 0; i < P; i++) {
+            const int s_hi = passes[i].first, g = passes[i].second, s_lo = s_hi - g + 1;
+            const bool last = i + 1 == P;
+            int q = kPassBits - g;
+            size_t pieces;
+            if (s_lo > 0) {
+                q = std::min(q, s_lo);
+                pieces = ((size_t)1 << (log_n - g)) >> q;
+            } else {
+                const size_t total = (size_t)1 << (log_n - g);
+                while (q > 0 && ((size_t)1 << (q - 1)) >= total) q--;
+                pieces = (total + ((size_t)1 << q) - 1) >> q;
+            }
+            if (pieces >= ((size_t)1 << kQueuePieceBits))
+                throw cuda_error((int)cudaErrorInvalidValue, "ragged NTT piece index overflow");
+            ntt_qpass &Pp = J.pass[i];
+            Pp.src = P == 1 || i == 0 ? dj : tj;
+            Pp.dst = P == 1 || last ? dj : tj;
+            Pp.tw = pass_twiddles(log_n, inverse, s_hi, g, tw, s);
+            Pp.pieces = (uint32_t)pieces;
+            Pp.s_hi = s_hi;
+            Pp.g = g;
+            Pp.q = q;
+        }
+    }
+    std::vector<uint2> items;
+    for (size_t p = 0; p < max_passes; p++)
+        for (size_t j = 0; j < count; j++)
+            if (p < jobs[j].npass)
+                for (uint32_t c = 0; c < jobs[j].pass[p].pieces; c++)
+                    items.push_back(make_uint2((uint32_t)j, ((uint32_t)p << kQueuePieceBits) | c));
+    if (items.empty()) return 0;
+    if (items.size() > 0xffffffffull) throw cuda_error((int)cudaErrorInvalidValue, "ragged NTT item overflow");
+    dev_buf<ntt_qjob> djobs(count, s);
+    dev_buf<uint2> ditems(items.size(), s);
+    dev_buf<uint32_t> ctl(NTT_Q_COUNTERS + counters, s);
+    h2d(djobs, jobs.data(), count * sizeof(ntt_qjob), s);
+    h2d(ditems, items.data(), items.size() * sizeof(uint2), s);
+    GB_CUDA_OK(cudaMemsetAsync(ctl, 0, (NTT_Q_COUNTERS + counters) * sizeof(uint32_t), s));
+    const unsigned threads = 1024 >> 2;
+    const size_t smem = 2 * ((size_t)1 << kPassBits) * sizeof(fr_t);
+    int per_sm = 0, sms = 0, dev = current_device();
+    GB_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ntt_queue_kernel<2>, threads, smem));
+    GB_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t grid = std::min(items.size(), (size_t)std::max(per_sm, 1) * (size_t)sms);
+    ntt_queue_kernel<2><<<(unsigned)grid, threads, smem, s>>>(djobs, ditems, (uint32_t)items.size(), ctl);
+    GB_CHECK_LAUNCH();
+    return 1;
 }
 
 // the DIF passes of `count` transforms in place; el = log2(elements per
@@ -957,14 +1188,18 @@ void launch_coeff_to_extended_prepare(fr_t *out, const fr_t *in, const fr_t &fir
 }
 
 // reads and clears the count of staged-pass CTAs whose twiddle copy did not
-// land within the spin limit; throws when there was one
+// land within the spin limit, plus the work-queue waits that ran out; throws
+// when there was one
 static uint32_t ntt_take_waits(cudaStream_t s)
 {
     uint32_t h = 0, zero = 0;
+    uint32_t hq = 0;
     GB_CUDA_OK(cudaMemcpyFromSymbolAsync(&h, g_ntt_wait_timeouts, sizeof(h), 0, cudaMemcpyDeviceToHost, s));
     GB_CUDA_OK(cudaMemcpyToSymbolAsync(g_ntt_wait_timeouts, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
+    GB_CUDA_OK(cudaMemcpyFromSymbolAsync(&hq, g_ntt_queue_timeouts, sizeof(hq), 0, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_OK(cudaMemcpyToSymbolAsync(g_ntt_queue_timeouts, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
     GB_CUDA_OK(cudaStreamSynchronize(s));
-    return h;
+    return h + hq;
 }
 
 static void ntt_check_waits(cudaStream_t s)
@@ -1165,6 +1400,8 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(void *device_vec, uin
     auto *v = reinterpret_cast<fr_device_vec *>(device_vec);
     size_t n = (size_t)1 << log_n;
     if (log_n > 31 || v->len != n) return make_error((int)cudaErrorInvalidValue, "resident NTT length mismatch");
+    // a single value is returned unscaled, as the reference does (.cu:3296-3298)
+    if (log_n == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
     ntt_ref_zeta(v->values, log_n, 1, inverse, scale, first, second, s);
@@ -1189,6 +1426,56 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(void *device_ve
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
     ntt_ref_zeta(v->values, log_n, count, inverse, scale, first, second, s);
+    device_vec_mark_ready(v, s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// Ragged batch in one persistent launch (no reference counterpart: the
+// reference runs one transform per call or a batch of equal sizes).
+RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, const uint32_t *log_ns, size_t count,
+                                      bool inverse, RawFr scale_raw, RawFr first_raw, RawFr second_raw)
+{
+    const fr_t scale = gb::from_raw(scale_raw);
+    const fr_t first = gb::from_raw(first_raw);
+    const fr_t second = gb::from_raw(second_raw);
+    if (!device_vec || (count && (!offsets || !log_ns)))
+        return make_error((int)cudaErrorInvalidValue, "invalid ragged NTT arguments");
+    GB_ENTRY_BEGIN
+    auto *v = reinterpret_cast<fr_device_vec *>(device_vec);
+    std::vector<std::pair<size_t, size_t>> ranges;
+    for (size_t j = 0; j < count; j++) {
+        if (log_ns[j] > 30) return make_error((int)cudaErrorInvalidValue, "ragged NTT size above 2^30");
+        const size_t n = (size_t)1 << log_ns[j];
+        if (offsets[j] > v->len || n > v->len - offsets[j])
+            return make_error((int)cudaErrorInvalidValue, "ragged NTT polynomial outside the device vector");
+        ranges.emplace_back(offsets[j], n);
+    }
+    std::sort(ranges.begin(), ranges.end());
+    for (size_t j = 1; j < ranges.size(); j++)
+        if (ranges[j - 1].first + ranges[j - 1].second > ranges[j].first)
+            return make_error((int)cudaErrorInvalidValue, "ragged NTT polynomials overlap");
+    if (count == 0) return ok();
+    cudaStream_t s = lane_stream();
+    device_vec_wait(v, s);
+    std::vector<size_t> q_off;
+    std::vector<uint32_t> q_log;
+    std::vector<ntt_factors> q_fac;
+    for (size_t j = 0; j < count; j++) {
+        if (log_ns[j] == 0) continue;  // one value: unchanged, as a single call leaves it
+        if (log_ns[j] < 3) {
+            // 2 or 4 values: the plain path
+            ntt_ref_zeta(v->values + offsets[j], log_ns[j], 1, inverse, scale, first, second, s);
+            continue;
+        }
+        fr_t sc = scale;
+        if (inverse) sc = sc * host_fr_inverse(host_fr_from_u64((uint64_t)1 << log_ns[j]));
+        q_off.push_back(offsets[j]);
+        q_log.push_back(log_ns[j]);
+        q_fac.push_back(ntt_factors{{sc, sc * first, sc * second}, 1});
+    }
+    ntt_ragged(v->values, q_off.data(), q_log.data(), q_fac.data(), q_off.size(), inverse, s);
+    ntt_check_waits(s);
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END

@@ -142,6 +142,7 @@ def _declare(L):
         "gb_autotune_set": (None, [ctypes.c_int]),
         "gb_ntt_variant_set": (None, [ctypes.c_int]),
         "gb_ntt_wait_timeouts": (E, [ctypes.POINTER(ctypes.c_uint32)]),
+        "gb_fr_device_vec_ntt_ragged": (E, [vp, vp, vp, sz, b, fr, fr, fr]),
         "gb_autotune_reset": (None, []),
         "gb_autotune_report": (sz, [vp, sz]),
     }

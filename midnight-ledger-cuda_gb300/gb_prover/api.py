@@ -197,6 +197,17 @@ class Bls12_381FrDeviceVec:
         check(lib().midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(self.raw, log_n, count, inverse,
                                                                             _fr(scale), _fr(first), _fr(second)))
 
+    def ntt_ragged(self, offsets, log_ns, inverse, scale, first, second):
+        """NTTs of polynomials of different sizes in this vector, one
+        persistent launch (gb_fr_device_vec_ntt_ragged): polynomial j is the
+        2^log_ns[j] values from offsets[j]."""
+        off = np.ascontiguousarray(offsets, dtype=np.uintp)
+        lg = np.ascontiguousarray(log_ns, dtype=np.uint32)
+        if len(off) != len(lg):
+            raise ValueError("offsets and log_ns differ in length")
+        check(lib().gb_fr_device_vec_ntt_ragged(self.raw, _ptr(off), _ptr(lg), len(off), inverse, _fr(scale),
+                                                _fr(first), _fr(second)))
+
     def divide_ntt_zeta(self, log_n, factors, scale, first, second):
         f = _fr_arr(factors)
         check(lib().midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(self.raw, log_n, _ptr(f), len(f),

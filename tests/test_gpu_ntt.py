@@ -123,3 +123,121 @@ def test_device_vec_batch_ntt(gb, orc):
     for p in range(count):
         seg = v[p << log_n:(p + 1) << log_n]
         assert (got[p << log_n:(p + 1) << log_n] == orc.fr_ntt_zeta(seg, log_n, True, scale, z1, z2)).all()
+
+
+def _ragged_layout(log_ns, rng, gap_max=37):
+    """Polynomials at shuffled offsets with gaps between them."""
+    order = rng.permutation(len(log_ns))
+    offsets = [0] * len(log_ns)
+    pos = 0
+    for j in order:
+        pos += int(rng.integers(0, gap_max))
+        offsets[j] = pos
+        pos += 1 << log_ns[j]
+    return offsets, pos + int(rng.integers(0, gap_max))
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_ntt_ragged_against_oracle(gb, orc, inverse):
+    """One persistent launch over transforms of one, two and three passes
+    (and 1 to 4 values: a single value stays unchanged as in a single call,
+    2 and 4 take the plain path), placed out of order with gaps; every
+    transform bit-exact against the oracle, gaps untouched."""
+    log_ns = [0, 1, 2, 3, 5, 7, 9, 10, 11, 13, 16, 21, 12, 3, 10]
+    rng = np.random.default_rng(71 + inverse)
+    offsets, total = _ragged_layout(log_ns, rng)
+    v = orc.fr_random(total, rng)
+    z1, z2 = _zeta_pair(orc)
+    scale = orc.fr_from_ints([9])[0]
+    dv = gb.Bls12_381FrDeviceVec.upload(v)
+    dv.ntt_ragged(offsets, log_ns, inverse, scale, z1, z2)
+    got = dv.download()
+    covered = np.zeros(total, dtype=bool)
+    for off, ln in zip(offsets, log_ns):
+        seg = slice(off, off + (1 << ln))
+        covered[seg] = True
+        assert (got[seg] == orc.fr_ntt_zeta(v[seg], ln, inverse, scale, z1, z2)).all(), ln
+    assert (got[~covered] == v[~covered]).all()
+    assert gb.ntt_wait_timeouts() == 0
+
+
+def test_ntt_ragged_batch_shape(gb, orc):
+    """64 transforms with the batched configuration's size distribution
+    (next powers of two of round(2^U), U uniform in [10, 18]): equal to one
+    call per transform, and the inverse restores the input."""
+    rng = np.random.default_rng(64)
+    log_ns = [max(1, (int(round(2 ** u)) - 1).bit_length()) for u in rng.uniform(10, 18, size=64)]
+    offsets, total = _ragged_layout(log_ns, rng, gap_max=3)
+    v = orc.fr_random(total, rng)
+    one = orc.fr_const(orc.CONST_ONE)
+    dv = gb.Bls12_381FrDeviceVec.upload(v)
+    dv.ntt_ragged(offsets, log_ns, False, one, one, one)
+    got = dv.download()
+    for j in rng.choice(64, size=8, replace=False):
+        off, ln = offsets[j], log_ns[j]
+        single = gb.Bls12_381FrDeviceVec.upload(v[off:off + (1 << ln)])
+        single.ntt_zeta(ln, False, one, one, one)
+        assert (got[off:off + (1 << ln)] == single.download()).all(), ln
+    small = [j for j in range(64) if log_ns[j] <= 12][:2]
+    for j in small:
+        off, ln = offsets[j], log_ns[j]
+        assert (got[off:off + (1 << ln)] == orc.fr_ntt(v[off:off + (1 << ln)], ln, False)).all()
+    dv.ntt_ragged(offsets, log_ns, True, one, one, one)
+    assert (dv.download() == v).all()
+    assert gb.ntt_wait_timeouts() == 0
+
+
+def test_ntt_ragged_full_size(gb, orc):
+    """16 x 2^20 and 2 x 2^22 transforms in one launch equal the per-size
+    batched path (itself pinned to the oracle at 2^20), and round-trip."""
+    rng = np.random.default_rng(2022)
+    log_ns = [20] * 16 + [22] * 2
+    offsets = list(np.cumsum([0] + [1 << ln for ln in log_ns[:-1]]))
+    total = int(offsets[-1]) + (1 << log_ns[-1])
+    v = orc.fr_random(total, rng)
+    z1, z2 = _zeta_pair(orc)
+    dv = gb.Bls12_381FrDeviceVec.upload(v)
+    dv.ntt_ragged(offsets, log_ns, False, z1, z1, z2)
+    got = dv.download()
+    a = gb.Bls12_381FrDeviceVec.upload(v[:16 << 20])
+    a.ntt_zeta_batch(20, 16, False, z1, z1, z2)
+    assert (got[:16 << 20] == a.download()).all()
+    b = gb.Bls12_381FrDeviceVec.upload(v[16 << 20:])
+    b.ntt_zeta_batch(22, 2, False, z1, z1, z2)
+    assert (got[16 << 20:] == b.download()).all()
+    del a, b, dv
+    # zeta^3 = 1: scaling by zeta forward and zeta^2 inverse restores v
+    one = orc.fr_const(orc.CONST_ONE)
+    rt = gb.Bls12_381FrDeviceVec.upload(v)
+    rt.ntt_ragged(offsets, log_ns, False, z1, one, one)
+    rt.ntt_ragged(offsets, log_ns, True, z2, one, one)
+    assert (rt.download() == v).all()
+    assert gb.ntt_wait_timeouts() == 0
+
+
+def test_ntt_ragged_rejects_bad_layouts(gb, orc):
+    v = orc.fr_random(64, np.random.default_rng(5))
+    one = orc.fr_const(orc.CONST_ONE)
+    dv = gb.Bls12_381FrDeviceVec.upload(v)
+    for offsets, log_ns in (([0, 16], [5, 4]),      # overlap
+                            ([40], [5]),             # past the end
+                            ([0], [31])):            # above 2^30
+        with pytest.raises(gb.MsmError):
+            dv.ntt_ragged(offsets, log_ns, False, one, one, one)
+    dv.ntt_ragged([], [], False, one, one, one)
+    assert (dv.download() == v).all()
+
+
+def test_device_ntt_single_value(gb, orc):
+    """log_n = 0: the single-transform device call leaves the value unscaled
+    (bls12_381_g1_msm.cu:3296-3298), the batch call scales it
+    (.cu:3360-3375 runs the postprocess for every size)."""
+    v = orc.fr_random(3, np.random.default_rng(8))
+    z1, z2 = _zeta_pair(orc)
+    scale = orc.fr_from_ints([6])[0]
+    one = gb.Bls12_381FrDeviceVec.upload(v[:1])
+    one.ntt_zeta(0, False, scale, z1, z2)
+    assert (one.download() == v[:1]).all()
+    batch = gb.Bls12_381FrDeviceVec.upload(v)
+    batch.ntt_zeta_batch(0, 3, True, scale, z1, z2)
+    assert (batch.download() == np.array([orc.fr_mul(x, scale) for x in v])).all()
