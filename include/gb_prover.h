@@ -384,7 +384,9 @@ GB_API uint64_t gb_launch_counter(void);
 /* the calling thread's lane stream (a cudaStream_t) */
 GB_API void *gb_lane_stream(void);
 /* CUDA-event timing of individual kernels on their launching stream;
- * slot 0 = MSM bucket accumulation, 1 = whole MSM, 2 = NTT passes */
+ * slot 0 = MSM bucket accumulation, 1 = whole MSM, 2 = NTT passes, 3 = MSM
+ * recode and sort, 4 = MSM bucket fix-up, 5 = MSM bucket reduction and window
+ * combination */
 GB_API void gb_profile_enable(int on);
 GB_API void gb_profile_read(int slot, double *total_ms, uint64_t *launches);
 GB_API void gb_profile_reset(void);

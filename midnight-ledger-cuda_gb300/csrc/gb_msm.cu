@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <initializer_list>
 #include <vector>
 
 #include "gb_runtime.cuh"
@@ -461,6 +462,244 @@ __global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__rest
     if (threadIdx.x == 0) out[(size_t)seg * gridDim.x + blockIdx.x] = sh[0];
 }
 
+// ---------------------------------------------------------------------------
+// Cooperative point arithmetic for the latency-bound reduction.  The bucket
+// reduction is a few chains of dependent XYZZ operations per segment, run on
+// few warps, so its time is the latency of one operation times the chain
+// length.  Here a group of 8 lanes (a quarter warp) runs one chain: the
+// products of a point operation that do not depend on each other are
+// computed by different lanes at the same time, with the operands and
+// results in the group's shared-memory slots.  An addition is then 4 product
+// levels deep (instead of 14 products in sequence) and a doubling 3 (instead
+// of 10).  Every decision (infinity, equal or opposite points) reads shared
+// values after a group barrier, so the 8 lanes always take the same path.
+static constexpr uint32_t kCoopLanes = 8;
+static constexpr uint32_t kCoopGroups = 16;  // groups per 128-thread block
+static constexpr uint64_t kCoopMaxBuckets = 8u << 15;  // cooperative reduction up to 8 x 2^15 buckets
+// slots of a group: RUN, SUM, OPD (operand), RES (4 each: X, Y, ZZ, ZZZ),
+// then 12 temporaries
+enum { CO_RUN = 0, CO_SUM = 4, CO_OPD = 8, CO_RES = 12, CO_TMP = 16, CO_SLOTS = 28 };
+
+struct coop_t {
+    fp_t *s;        // the group's slots
+    uint32_t lane;  // 0..7
+    uint32_t mask;  // the group's lanes in the warp
+    __device__ void sync() const { __syncwarp(mask); }
+};
+
+__device__ __forceinline__ void coop_set_inf(const coop_t &c, int a)
+{
+    if (c.lane == 0) {
+        const xyzz_t z = xyzz_t::inf();
+        c.s[a] = z.x, c.s[a + 1] = z.y, c.s[a + 2] = z.zz, c.s[a + 3] = z.zzz;
+    }
+    c.sync();
+}
+
+// 4 slots (48 words) from src to dst, 6 words per lane
+__device__ __forceinline__ void coop_copy(const coop_t &c, fp_t *dst, const fp_t *src)
+{
+    const uint2 *f = reinterpret_cast<const uint2 *>(src);
+    uint2 *t = reinterpret_cast<uint2 *>(dst);
+    const uint2 a = f[c.lane * 3], b = f[c.lane * 3 + 1], d = f[c.lane * 3 + 2];
+    c.sync();
+    t[c.lane * 3] = a, t[c.lane * 3 + 1] = b, t[c.lane * 3 + 2] = d;
+    c.sync();
+}
+
+__device__ __forceinline__ void coop_load(const coop_t &c, int a, const xyzz_t *g)
+{
+    const uint2 *f = reinterpret_cast<const uint2 *>(g);
+    uint2 *t = reinterpret_cast<uint2 *>(c.s + a);
+    t[c.lane * 3] = f[c.lane * 3], t[c.lane * 3 + 1] = f[c.lane * 3 + 1], t[c.lane * 3 + 2] = f[c.lane * 3 + 2];
+    c.sync();
+}
+
+__device__ __forceinline__ void coop_store(const coop_t &c, int a, xyzz_t *g)
+{
+    const uint2 *f = reinterpret_cast<const uint2 *>(c.s + a);
+    uint2 *t = reinterpret_cast<uint2 *>(g);
+    t[c.lane * 3] = f[c.lane * 3], t[c.lane * 3 + 1] = f[c.lane * 3 + 1], t[c.lane * 3 + 2] = f[c.lane * 3 + 2];
+}
+
+// One level of products: lane l < n computes s[xi[l]] * s[yi[l]] into
+// s[oi[l]].  All lanes run the same call with their own operands, so the
+// products of a level run side by side (a product per lane per branch would
+// run them one after another).  Operands are read before any result is
+// written.
+//
+// The slot indices of lane l sit in bits 5l .. 5l + 4 of x, y and o.
+__device__ __forceinline__ uint32_t coop_pack(std::initializer_list<int> v)
+{
+    uint32_t r = 0, sh = 0;
+    for (int i : v) r |= (uint32_t)i << sh, sh += 5;
+    return r;
+}
+
+__device__ __forceinline__ void coop_level(const coop_t &c, uint32_t n, uint32_t x, uint32_t y, uint32_t o)
+{
+    const uint32_t sh = 5u * (c.lane < n ? c.lane : 0u);
+    const fp_t a = c.s[(x >> sh) & 31u], b = c.s[(y >> sh) & 31u];
+    const fp_t r = a * b;
+    c.sync();
+    if (c.lane < n) c.s[(o >> sh) & 31u] = r;
+    c.sync();
+}
+
+// a = 2 a (dbl-2008-s-1, the products of xyzz_t::dbl in three levels)
+__device__ void coop_dbl(const coop_t &c, int a)
+{
+    fp_t *s = c.s;
+    if (s[a + 2].is_zero()) return;
+    enum { U = CO_TMP, V, XX, M, W, S, MM, D, T0, T1 };
+    {
+        const fp_t u = s[a + 1].dbl();
+        if (u.is_zero()) {
+            coop_set_inf(c, a);
+            return;
+        }
+        c.sync();
+        if (c.lane == 0) s[U] = u;
+        c.sync();
+    }
+    {
+        coop_level(c, 2, coop_pack({U, a}), coop_pack({U, a}), coop_pack({V, XX}));  // V = U^2, XX = X^2
+    }
+    if (c.lane == 0) s[M] = s[XX].dbl() + s[XX];
+    c.sync();
+    {
+        // W = U V, S = X V, ZZ3 = V ZZ, MM = M^2
+        coop_level(c, 4, coop_pack({U, a, V, M}), coop_pack({V, V, a + 2, M}), coop_pack({W, S, a + 2, MM}));
+    }
+    const fp_t X3 = s[MM] - s[S].dbl();
+    if (c.lane == 0) s[D] = s[S] - X3;
+    c.sync();
+    {
+        // M (S - X3), W Y, ZZZ3 = W ZZZ
+        coop_level(c, 3, coop_pack({M, W, W}), coop_pack({D, a + 1, a + 3}), coop_pack({T0, T1, a + 3}));
+    }
+    if (c.lane == 0) {
+        s[a] = X3;
+        s[a + 1] = s[T0] - s[T1];
+    }
+    c.sync();
+}
+
+// a += q (add-2008-s, the products of xyzz_t::add in four levels); q's
+// slots are left unchanged
+__device__ void coop_add(const coop_t &c, int a, int q)
+{
+    fp_t *s = c.s;
+    if (s[q + 2].is_zero()) return;
+    if (s[a + 2].is_zero()) {
+        coop_copy(c, s + a, s + q);
+        return;
+    }
+    enum { U1 = CO_TMP, U2, S1, S2, Z12, W12, P, R, PP, RR, PPP, QQ };
+    {
+        // U1 = X1 ZZ2, U2 = X2 ZZ1, S1 = Y1 ZZZ2, S2 = Y2 ZZZ1, ZZ1 ZZ2, ZZZ1 ZZZ2
+        coop_level(c, 6, coop_pack({a, q, a + 1, q + 1, a + 2, a + 3}), coop_pack({q + 2, a + 2, q + 3, a + 3, q + 2, q + 3}), coop_pack({U1, U2, S1, S2, Z12, W12}));
+    }
+    {
+        const fp_t p = s[U2] - s[U1];
+        const fp_t r = s[S2] - s[S1];
+        if (p.is_zero()) {
+            if (r.is_zero()) coop_dbl(c, a);
+            else coop_set_inf(c, a);
+            return;
+        }
+        c.sync();
+        if (c.lane == 0) s[P] = p;
+        if (c.lane == 1) s[R] = r;
+        c.sync();
+    }
+    {
+        coop_level(c, 2, coop_pack({P, R}), coop_pack({P, R}), coop_pack({PP, RR}));
+    }
+    {
+        // PPP = P PP, Q = U1 PP, ZZ3 = ZZ1 ZZ2 PP
+        coop_level(c, 3, coop_pack({P, U1, Z12}), coop_pack({PP, PP, PP}), coop_pack({PPP, QQ, a + 2}));
+    }
+    const fp_t X3 = s[RR] - s[PPP] - s[QQ].dbl();
+    if (c.lane == 0) s[U2] = s[QQ] - X3;  // U2 is free from here on
+    c.sync();
+    {
+        // R (Q - X3) -> S2, S1 PPP -> U1, ZZZ3 = ZZZ1 ZZZ2 PPP
+        coop_level(c, 3, coop_pack({R, S1, W12}), coop_pack({U2, PPP, PPP}), coop_pack({S2, U1, a + 3}));
+    }
+    if (c.lane == 0) {
+        s[a] = X3;
+        s[a + 1] = s[S2] - s[U1];
+    }
+    c.sync();
+}
+
+// the 16 groups of a block add their SUM slots into group 0's (4 levels)
+__device__ void coop_block_tree(fp_t *sh, const coop_t &c, uint32_t grp)
+{
+    for (uint32_t off = kCoopGroups / 2; off > 0; off >>= 1) {
+        __syncthreads();
+        if (grp < off) {
+            coop_copy(c, c.s + CO_OPD, sh + (size_t)(grp + off) * CO_SLOTS + CO_SUM);
+            coop_add(c, CO_SUM, CO_OPD);
+        }
+    }
+}
+
+// 8a'. msm_reduce_partial_kernel with one 8-lane group per (segment,
+//      sub-segment) and the block's 16 groups summed at the end: `partial`
+//      holds nseg * S / 16 points.  S is a power of two >= 16.
+__global__ void __launch_bounds__(128) msm_reduce_coop_kernel(const xyzz_t *__restrict__ buckets, uint32_t K,
+                                                              uint32_t S, xyzz_t *__restrict__ partial)
+{
+    __shared__ __align__(16) fp_t sh[kCoopGroups * CO_SLOTS];
+    const uint32_t grp = threadIdx.x / kCoopLanes;
+    const coop_t c{sh + (size_t)grp * CO_SLOTS, threadIdx.x % kCoopLanes, 0xffu << (threadIdx.x & 24u)};
+    const uint32_t gid = blockIdx.x * kCoopGroups + grp;
+    const uint32_t seg = gid / S, sub = gid % S, m = K / S, k0 = sub * m;
+    const xyzz_t *B = buckets + (size_t)seg * K;
+    coop_set_inf(c, CO_RUN);
+    coop_set_inf(c, CO_SUM);
+    for (uint32_t k = k0 + m; k-- > k0;) {
+        coop_load(c, CO_OPD, B + k);
+        coop_add(c, CO_RUN, CO_OPD);  // run += B[k]
+        coop_add(c, CO_SUM, CO_RUN);  // sum += run
+    }
+    if (k0) {
+        // sum += k0 * run, double-and-add from the top bit
+        coop_copy(c, c.s + CO_RES, c.s + CO_RUN);
+        int top = 31;
+        while (!((k0 >> top) & 1u)) top--;
+        for (int i = top - 1; i >= 0; i--) {
+            coop_dbl(c, CO_RES);
+            if ((k0 >> i) & 1u) coop_add(c, CO_RES, CO_RUN);
+        }
+        coop_add(c, CO_SUM, CO_RES);
+    }
+    coop_block_tree(sh, c, grp);
+    if (grp == 0) coop_store(c, CO_SUM, partial + blockIdx.x);
+}
+
+// 8b'. tree sum with groups: out[seg * gridDim.x + b] = sum of the 32-element
+//      slice b of in[seg * n .. seg * n + n)
+__global__ void __launch_bounds__(128) xyzz_tree_sum_coop_kernel(const xyzz_t *__restrict__ in, uint32_t n,
+                                                                 xyzz_t *__restrict__ out)
+{
+    __shared__ __align__(16) fp_t sh[kCoopGroups * CO_SLOTS];
+    const uint32_t grp = threadIdx.x / kCoopLanes;
+    const coop_t c{sh + (size_t)grp * CO_SLOTS, threadIdx.x % kCoopLanes, 0xffu << (threadIdx.x & 24u)};
+    const xyzz_t *src = in + (size_t)blockIdx.y * n;
+    const uint32_t i0 = blockIdx.x * 2 * kCoopGroups + grp, i1 = i0 + kCoopGroups;
+    if (i0 < n) coop_load(c, CO_SUM, src + i0);
+    else coop_set_inf(c, CO_SUM);
+    if (i1 < n) {
+        coop_load(c, CO_OPD, src + i1);
+        coop_add(c, CO_SUM, CO_OPD);
+    }
+    coop_block_tree(sh, c, grp);
+    if (grp == 0) coop_store(c, CO_SUM, out + (size_t)blockIdx.y * gridDim.x + blockIdx.x);
+}
+
 // 8c. per MSM: combine its window segments (Horner) and emit a Jacobian point
 __global__ void msm_combine_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t nitems, uint32_t segs_per_item,
                                    int c, jacobian_t *__restrict__ out)
@@ -475,6 +714,32 @@ __global__ void msm_combine_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t 
         acc.GB_ADD_LAT(ss[w]);
     }
     out[m] = acc.to_jacobian();
+}
+
+// 8c'. msm_combine_kernel with one 8-lane group per MSM (16 MSMs a block):
+//       the Horner chain of a plain MSM is (windows - 1) * c doublings long
+__global__ void __launch_bounds__(128) msm_combine_coop_kernel(const xyzz_t *__restrict__ seg_sum, uint32_t nitems,
+                                                               uint32_t segs_per_item, int c,
+                                                               jacobian_t *__restrict__ out)
+{
+    __shared__ __align__(16) fp_t sh[kCoopGroups * CO_SLOTS];
+    const uint32_t grp = threadIdx.x / kCoopLanes;
+    const coop_t cp{sh + (size_t)grp * CO_SLOTS, threadIdx.x % kCoopLanes, 0xffu << (threadIdx.x & 24u)};
+    const uint32_t m = blockIdx.x * kCoopGroups + grp;
+    if (m >= nitems) return;  // whole groups leave together; no block barrier follows
+    const xyzz_t *ss = seg_sum + (size_t)m * segs_per_item;
+    coop_set_inf(cp, CO_SUM);
+    for (int w = (int)segs_per_item - 1; w >= 0; w--) {
+        if (w != (int)segs_per_item - 1)
+            for (int k = 0; k < c; k++) coop_dbl(cp, CO_SUM);
+        coop_load(cp, CO_OPD, ss + w);
+        coop_add(cp, CO_SUM, CO_OPD);
+    }
+    if (cp.lane == 0) {
+        xyzz_t acc;
+        acc.x = cp.s[CO_SUM], acc.y = cp.s[CO_SUM + 1], acc.zz = cp.s[CO_SUM + 2], acc.zzz = cp.s[CO_SUM + 3];
+        out[m] = acc.to_jacobian();
+    }
 }
 
 // precompute: table[j * n + i] = 2^(c*j) P_i
@@ -588,6 +853,13 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     uint32_t S = 32;
     while (S < 8192 && (uint64_t)S * 2 * nseg <= 65536) S *= 2;
     S = std::min<uint32_t>(K, S);
+    // Few buckets in all (a single MSM or a small batch): the reduction is a
+    // latency-bound chain per sub-segment, run by cooperative 8-lane groups,
+    // ~8192 groups over the batch.  Many buckets (large batches): the
+    // one-thread-per-chain kernel keeps the multiply-add pipe busier.
+    const bool coop_reduce = (uint64_t)nseg * K <= kCoopMaxBuckets && K >= kCoopGroups;
+    uint32_t S_coop = kCoopGroups;
+    while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= 8192) S_coop *= 2;
     const uint64_t nchunks = std::max<uint64_t>(1, (digits_total + L - 1) / L);
     const int variant = default_acc_variant();
 
@@ -600,9 +872,10 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     dev_buf<uint32_t> digits(std::max<uint64_t>(digits_total, 1), s), sorted(std::max<uint64_t>(digits_total, 1), s);
     dev_buf<uint32_t> hist((size_t)nblocks * K, s), counts(G, s), starts((size_t)G + 1, s);
     dev_buf<xyzz_t> buckets(G, s), head(nchunks, s), tail(nchunks, s);
-    dev_buf<xyzz_t> partial((size_t)nseg * S, s), segsum(nseg, s);
+    dev_buf<xyzz_t> partial((size_t)nseg * (coop_reduce ? S_coop / kCoopGroups : S), s), segsum(nseg, s);
 
     int tok_all = timed_begin(s);
+    int tok_sort = timed_begin(s);
     if (points_total) {
         msm_recode_kernel<<<(unsigned)((points_total + 255) / 256), 256, 0, s>>>(d_items, nitems, points_total, c,
                                                                                  nwin, digits);
@@ -617,6 +890,7 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     msm_scatter_kernel<<<nblocks, 1024, smem, s>>>(digits, d_segs, d_blks, K, precomputed ? stride : 0, hist,
                                                    starts, sorted);
     GB_CHECK_LAUNCH();
+    timed_end(tok_sort, s, GB_SLOT_MSM_SORT);
     int tok = timed_begin(s);
     if (variant == 1) {
         msm_accumulate_kernel<256, 2><<<(unsigned)((nchunks + 255) / 256), 256, 0, s>>>(
@@ -630,6 +904,7 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     }
     GB_CHECK_LAUNCH();
     timed_end(tok, s, GB_SLOT_MSM_ACCUMULATE);
+    int tok_fix = timed_begin(s);
     {
         dev_buf<uint32_t> longs(G, s), nlong(1, s);
         GB_CUDA_OK(cudaMemsetAsync(nlong.get(), 0, sizeof(uint32_t), s));
@@ -640,6 +915,28 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
         msm_fixup_long_kernel<<<(unsigned)sms * 2, 256, 0, s>>>(starts, L, head, tail, longs, nlong, buckets);
         GB_CHECK_LAUNCH();
     }
+    timed_end(tok_fix, s, GB_SLOT_MSM_FIXUP);
+    int tok_red = timed_begin(s);
+    if (coop_reduce) {
+        // latency-bound: one 8-lane group per sub-segment, 16 groups a block
+        msm_reduce_coop_kernel<<<nseg * S_coop / kCoopGroups, 128, 0, s>>>(buckets, K, S_coop, partial);
+        GB_CHECK_LAUNCH();
+        const xyzz_t *src = partial;
+        uint32_t len = S_coop / kCoopGroups;
+        dev_buf<xyzz_t> tmp_a, tmp_b;
+        bool use_a = true;
+        while (len > 1) {
+            const uint32_t blocks = (len + 2 * kCoopGroups - 1) / (2 * kCoopGroups);
+            dev_buf<xyzz_t> &dst = use_a ? tmp_a : tmp_b;
+            dst = dev_buf<xyzz_t>((size_t)nseg * blocks, s);
+            xyzz_tree_sum_coop_kernel<<<dim3(blocks, nseg), 128, 0, s>>>(src, len, dst);
+            GB_CHECK_LAUNCH();
+            src = dst;
+            len = blocks;
+            use_a = !use_a;
+        }
+        GB_CUDA_OK(cudaMemcpyAsync(segsum, src, (size_t)nseg * sizeof(xyzz_t), cudaMemcpyDeviceToDevice, s));
+    } else {
     msm_reduce_partial_kernel<<<blocks_for((size_t)nseg * S, 128), 128, 0, s>>>(buckets, K, S, nseg, partial);
     GB_CHECK_LAUNCH();
     {
@@ -660,8 +957,16 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
         }
         GB_CUDA_OK(cudaMemcpyAsync(segsum, src, (size_t)nseg * sizeof(xyzz_t), cudaMemcpyDeviceToDevice, s));
     }
-    msm_combine_kernel<<<blocks_for(nitems, 32), 32, 0, s>>>(segsum, nitems, segs_per_item, c, d_out);
+    }
+    if (segs_per_item > 1) {
+        // plain MSMs: a Horner chain per MSM, cooperative groups
+        msm_combine_coop_kernel<<<(nitems + kCoopGroups - 1) / kCoopGroups, 128, 0, s>>>(segsum, nitems,
+                                                                                          segs_per_item, c, d_out);
+    } else {
+        msm_combine_kernel<<<blocks_for(nitems, 32), 32, 0, s>>>(segsum, nitems, segs_per_item, c, d_out);
+    }
     GB_CHECK_LAUNCH();
+    timed_end(tok_red, s, GB_SLOT_MSM_REDUCE);
     timed_end(tok_all, s, GB_SLOT_MSM_TOTAL);
 }
 

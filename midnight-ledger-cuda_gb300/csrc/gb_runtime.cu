@@ -293,7 +293,8 @@ void *gb_lane_stream(void)
 }
 
 // Per-kernel CUDA-event timing (slot 0: MSM bucket accumulation kernel,
-// slot 1: whole MSM, slot 2: NTT passes).
+// slot 1: whole MSM, slot 2: NTT passes, slots 3-5: the MSM's recode and
+// sort, bucket fix-up, and bucket reduction with window combination).
 void gb_profile_enable(int on)
 {
     g_prof.store(on != 0);

@@ -161,7 +161,8 @@ bool profiling_enabled();
 int timed_begin(cudaStream_t s);
 void timed_end(int token, cudaStream_t s, int slot);
 void timed_collect();
-enum { GB_SLOT_MSM_ACCUMULATE = 0, GB_SLOT_MSM_TOTAL = 1, GB_SLOT_NTT = 2, GB_SLOTS = 8 };
+enum { GB_SLOT_MSM_ACCUMULATE = 0, GB_SLOT_MSM_TOTAL = 1, GB_SLOT_NTT = 2, GB_SLOT_MSM_SORT = 3,
+       GB_SLOT_MSM_FIXUP = 4, GB_SLOT_MSM_REDUCE = 5, GB_SLOTS = 8 };
 
 // Autotuner: when enabled, an operation with several launch shapes (the MSM
 // window, the NTT pass variant) times its candidates the first time it meets

@@ -21,13 +21,16 @@ __all__ = [
     "bls12_381_fr_lookup_products_device", "bls12_381_fr_device_quotient_pieces",
     "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "imad_probe", "ntt_variant_set", "ntt_wait_timeouts", "transfer_counters",
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
-    "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "bls12_381_eval_numerator",
+    "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "PROFILE_MSM_SORT",
+    "PROFILE_MSM_FIXUP", "PROFILE_MSM_REDUCE", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
     "fr_lookup_permute_device", "autotune_set", "autotune_reset", "autotune_report",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
+# MSM phases: recode + sort, bucket fix-up, bucket reduction + window combination
+PROFILE_MSM_SORT, PROFILE_MSM_FIXUP, PROFILE_MSM_REDUCE = 3, 4, 5
 
 
 def _fr_arr(a):

@@ -50,6 +50,25 @@ def _chacha_blocks(key_words, counter0, nblocks, stream=0):
     return out
 
 
+def _chacha_block_int(key_words, counter, stream=0):
+    """One block with Python integers: far cheaper than the array form for
+    the few blocks a proof's host-side draws need."""
+    M = 0xFFFFFFFF
+    st = [0x61707865, 0x3320646E, 0x79622D32, 0x6B206574] + [int(k) for k in key_words] + [
+        counter & M, (counter >> 32) & M, stream & M, (stream >> 32) & M]
+    x = list(st)
+    for _ in range(10):
+        for a, b, c, d in ((0, 4, 8, 12), (1, 5, 9, 13), (2, 6, 10, 14), (3, 7, 11, 15),
+                           (0, 5, 10, 15), (1, 6, 11, 12), (2, 7, 8, 13), (3, 4, 9, 14)):
+            xa, xb, xc, xd = x[a], x[b], x[c], x[d]
+            xa = (xa + xb) & M; xd ^= xa; xd = ((xd << 16) | (xd >> 16)) & M
+            xc = (xc + xd) & M; xb ^= xc; xb = ((xb << 12) | (xb >> 20)) & M
+            xa = (xa + xb) & M; xd ^= xa; xd = ((xd << 8) | (xd >> 24)) & M
+            xc = (xc + xd) & M; xb ^= xc; xb = ((xb << 7) | (xb >> 25)) & M
+            x[a], x[b], x[c], x[d] = xa, xb, xc, xd
+    return np.array([(x[i] + st[i]) & M for i in range(16)], dtype=np.uint32)
+
+
 class ChaCha20Rng:
     def __init__(self, seed: bytes):
         if len(seed) != 32:
@@ -83,8 +102,13 @@ class ChaCha20Rng:
         have = len(self._buf) - self._pos
         if have < count:
             need = count - have
-            nblocks = max((need + 15) // 16, 256)
-            fresh = _chacha_blocks(self._key, self._block, nblocks).reshape(-1)
+            nblocks = (need + 15) // 16
+            if nblocks <= 4:
+                # a few words (blinding values): scalar blocks
+                fresh = np.concatenate([_chacha_block_int(self._key, self._block + b) for b in range(nblocks)])
+            else:
+                nblocks = max(nblocks, 256)
+                fresh = _chacha_blocks(self._key, self._block, nblocks).reshape(-1)
             self._block += nblocks
             self._buf = np.concatenate([self._buf[self._pos:], fresh])
             self._pos = 0
