@@ -214,10 +214,12 @@ def main():
     ap.add_argument("--log-n", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--case", default="msm", choices=["msm", "ntt", "ntt-queue"],
+    ap.add_argument("--case", default="msm", choices=["msm", "ntt", "ntt-queue", "proof"],
                     help="msm: the benchmark line; ntt / ntt-queue: only the resident NTT batch of --count "
-                         "transforms of 2^--log-n, or the 64-transform ragged batch in one launch (small "
-                         "cases for profilers; one JSON line of timings)")
+                         "transforms of 2^--log-n, or the 64-transform ragged batch in one launch; proof: "
+                         "--steps k=16 proofs after the key generation and --warmup proofs, with a "
+                         "peak_row_kernel launch just before the last proof as a marker (small cases for "
+                         "profilers; one JSON line of timings)")
     ap.add_argument("--count", type=int, default=16)
     args = ap.parse_args()
     args.n = 1 << args.log_n
@@ -226,6 +228,9 @@ def main():
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.case == "proof":
+        run_proof_case(args)
         return
     if args.case != "msm":
         run_ntt_case(args)
@@ -336,6 +341,7 @@ def main():
                          "threads (%.1f s)" % (args.n_ref.bit_length() - 1, dt)}
         if not args.no_extras:
             cpu["proof_k16_s"] = cpu_baseline_proof()
+            cpu["ntt_2p20_ms"] = cpu_baseline_ntt(20)
 
     del ctx, dv
     if rank == 0:
@@ -362,6 +368,35 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_proof_case(args):
+    """--case proof: the k = 16 synthetic proof, one at a time (wall time)."""
+    import torch
+    import gb_prover as gb
+    from gb_prover import plonk
+    from gb_prover.kzg import CircuitTranscript, ParamsKZG
+    from gb_prover.rng import ChaCha20Rng, ints_to_mont
+    torch.cuda.set_device(0)
+    gb.lib()
+    c = plonk.SyntheticCircuit(16, advice=3, degree=3, lookups=1, copies=1 << 14, table_log=12,
+                               label="full synthetic PLONK/KZG proof, k=16")
+    fixed, advice, copies = c.synthesize()
+    params = ParamsKZG.unsafe_setup(16, plonk.fr_mont(0x5EED0F7A0))
+    be = plonk.GpuBackend(params)
+    pk = plonk.keygen(params, c, be, fixed, copies)
+    adv = ints_to_mont([v for col in advice for v in col])
+    for i in range(args.warmup):
+        plonk.create_proof(params, pk, adv, be, CircuitTranscript(), ChaCha20Rng.from_label("warm%d" % i))
+    ms = []
+    for i in range(args.steps):
+        if i == args.steps - 1:
+            gb.imad_probe(1)
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plonk.create_proof(params, pk, adv, be, CircuitTranscript(), ChaCha20Rng.from_label("p%d" % i))
+        ms.append((time.perf_counter() - t0) * 1e3)
+    print(json.dumps({"case": "proof", "k": 16, "ms": ms, "best_ms": min(ms)}))
 
 
 def run_ntt_case(args):
@@ -590,6 +625,18 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, load=0.85):
         proofs[name] = [r.future.result() for r in done]
     out["serve_batched_equals_sequential"] = proofs["batched"] == proofs["sequential"]
     return out
+
+
+def cpu_baseline_ntt(log_n):
+    """One forward Fr NTT of 2^log_n uniform values, the oracle's radix-2
+    transform (the reference's best_fft semantics) on all host threads."""
+    from oracle import oracle as orc
+    v = fr_uniform(1 << log_n, np.random.default_rng(78))
+    threads = os.cpu_count() or 1
+    orc.fr_ntt(v[:1024], 10, False, threads=threads)
+    t0 = time.perf_counter()
+    orc.fr_ntt(v, log_n, False, threads=threads)
+    return (time.perf_counter() - t0) * 1e3
 
 
 def cpu_baseline_proof():
