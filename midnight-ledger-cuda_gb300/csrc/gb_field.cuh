@@ -20,6 +20,8 @@
 
 #include <stdint.h>
 
+#include <utility>
+
 #if defined(__CUDACC__)
 #define GB_HD __host__ __device__ __forceinline__
 #define GB_D __device__ __forceinline__
@@ -36,6 +38,8 @@
 #define GB_D inline
 #define GB_COLD inline
 #endif
+
+#include "gb_fp_sqr.cuh"
 
 namespace gb {
 
@@ -556,7 +560,16 @@ struct mont_t {
     static __device__ __noinline__ mont_t mul_by_value(mont_t a, mont_t b);
 #endif
     GB_HD mont_t &operator*=(const mont_t &o) { return *this = *this * o; }
-    GB_HD mont_t sqr() const { return *this * *this; }
+    GB_HD mont_t sqr() const
+    {
+#if defined(__CUDA_ARCH__) && !defined(GB_FP_MUL_INLINE) && !defined(GB_FP_SQR_OFF)
+        if constexpr (N == 12) return sqr_by_value(*this);
+#endif
+        return *this * *this;
+    }
+#if defined(__CUDA_ARCH__) && !defined(GB_FP_MUL_INLINE)
+    static __device__ __noinline__ mont_t sqr_by_value(mont_t a);
+#endif
 
     GB_HD static void mont_mul(uint32_t *out, const uint32_t *a, const uint32_t *b);
 
@@ -694,6 +707,77 @@ __device__ __noinline__ mont_t<Cfg> mont_t<Cfg>::mul_by_value(mont_t<Cfg> a, mon
 {
     mont_t<Cfg> r;
     mont_mul_device<Cfg>(r.v, a.v, b.v);
+    return r;
+}
+#endif
+
+#if defined(__CUDA_ARCH__)
+// Fp Montgomery squaring: CIOS whose step i adds a_i times (a_i at word i,
+// then the words of 2 * sum_{j>i} a_j 2^(32 j)), so every cross product
+// a_i a_j is computed once, doubled: the a*a rows take 84 products instead
+// of 144 (the Montgomery rows are unchanged), 234 multiply-adds in all
+// against 300.  A step's multiplicand is below 2a < 2p, so the running sum
+// stays below 3p < 2^384 and the result below 2p, as in the product (the
+// rows are restated word by word and checked against a^2 R^-1 mod p in
+// tests/test_fp_sqr_rows.py).  Measured on GB300: the 2^20 MSM's
+// accumulation 3 % faster.  GB_FP_SQR_OFF selects the product form.
+template <int I>
+GB_D void sqr_step_fp(uint32_t *even, uint32_t *odd, const uint32_t *a, const uint32_t *d)
+{
+    typedef FpCfg C;
+    constexpr int J0 = (I + 1) & ~1;  // first even word at or above I
+    // multiplicand word j of step I: 0 below I, a_I at I, 2 a_{I+1} (without
+    // a_I's top bit) at I + 1, the words of 2a above
+    auto y = [&](int j) -> uint32_t {
+        return j < I ? 0u : j == I ? a[I] : j == I + 1 ? (a[(I + 1) % 12] << 1) : d[j % 12];
+    };
+    uint32_t ye[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) ye[k] = J0 + 2 * k < 12 ? y(J0 + 2 * k) : 0u;
+    if constexpr (J0 < 12) sqr_row12<J0>(even, ye, a[I]);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const int j = 2 * k + 1;
+        const uint32_t yj = y(j);
+        odd[2 * k] = j < I ? 0u : yj * a[I];
+        odd[2 * k + 1] = j < I ? 0u : __umulhi(yj, a[I]);
+    }
+    odd[12] = 0;
+    const uint32_t m = even[0] * C::INV;
+    row_mac_mod<C>(even, 0, m);
+    row_mac_mod<C>(odd, 1, m);
+    fold<12>(even, odd);
+}
+
+template <int... I>
+GB_D void sqr_steps_fp(uint32_t *even, uint32_t *odd, const uint32_t *a, const uint32_t *d,
+                       std::integer_sequence<int, I...>)
+{
+    (sqr_step_fp<I>(even, odd, a, d), ...);
+}
+
+GB_D void mont_sqr_fp_device(uint32_t *out, const uint32_t *a)
+{
+    uint32_t d[12], even[13], odd[13];
+    d[0] = a[0] << 1;
+#pragma unroll
+    for (int j = 1; j < 12; j++) d[j] = (a[j] << 1) | (a[j - 1] >> 31);
+#pragma unroll
+    for (int i = 0; i < 13; i++) even[i] = 0;
+    sqr_steps_fp(even, odd, a, d, std::make_integer_sequence<int, 12>{});
+    mont_t<FpCfg>::reduce_once(even, even[12]);
+#pragma unroll
+    for (int i = 0; i < 12; i++) out[i] = even[i];
+}
+#endif
+
+#if defined(__CUDA_ARCH__) && !defined(GB_FP_MUL_INLINE)
+template <class Cfg>
+__device__ __noinline__ mont_t<Cfg> mont_t<Cfg>::sqr_by_value(mont_t<Cfg> a)
+{
+    mont_t<Cfg> r;
+    if constexpr (Cfg::N == 12) mont_sqr_fp_device(r.v, a.v);
+    else mont_mul_device<Cfg>(r.v, a.v, a.v);
     return r;
 }
 #endif
