@@ -290,6 +290,13 @@ GB_API RustError gb_fr_lookup_permute_device(void **out, const void *compressed_
                                              const RawFr *table_blinds);
 
 /* ---- blinding draws ---------------------------------------------------------- */
+/* nblocks ChaCha20 keystream blocks (RFC 8439 block function, 64-bit block
+ * counter in words 12-13 and stream id in words 14-15, as rand_chacha's
+ * ChaCha20Rng) from block `counter`, 16 words each, computed on the host: the
+ * prover's host-side draws.  No reference counterpart (rand_chacha 0.3.1 on
+ * the Rust side). */
+GB_API RustError gb_chacha20_blocks(const uint32_t *key, uint64_t counter, uint64_t stream, size_t nblocks,
+                                    uint32_t *out);
 /* n values by Fq::random's rejection rule (fq.rs:373-387) from the
  * ChaCha20Rng stream with this 32-byte seed, starting at keystream word
  * word_offset, into a new device vector in Montgomery form;

@@ -108,7 +108,51 @@ static fr_t host_r2()
 
 using namespace gb;
 
+// The same block function on the host (the prover's own draws: blinding
+// values, challenges' seeds); plain C, no device involved.
+static inline uint32_t host_rotl32(uint32_t x, int n) { return (x << n) | (x >> (32 - n)); }
+
+static void host_chacha20_block(const uint32_t *key, uint64_t counter, uint64_t stream, uint32_t *out)
+{
+    uint32_t st[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, key[0], key[1], key[2], key[3],
+                       key[4], key[5], key[6], key[7], (uint32_t)counter, (uint32_t)(counter >> 32),
+                       (uint32_t)stream, (uint32_t)(stream >> 32)};
+    uint32_t x[16];
+    for (int i = 0; i < 16; i++) x[i] = st[i];
+    auto qr = [&x](int a, int b, int c, int d) {
+        x[a] += x[b];
+        x[d] = host_rotl32(x[d] ^ x[a], 16);
+        x[c] += x[d];
+        x[b] = host_rotl32(x[b] ^ x[c], 12);
+        x[a] += x[b];
+        x[d] = host_rotl32(x[d] ^ x[a], 8);
+        x[c] += x[d];
+        x[b] = host_rotl32(x[b] ^ x[c], 7);
+    };
+    for (int r = 0; r < 10; r++) {
+        qr(0, 4, 8, 12);
+        qr(1, 5, 9, 13);
+        qr(2, 6, 10, 14);
+        qr(3, 7, 11, 15);
+        qr(0, 5, 10, 15);
+        qr(1, 6, 11, 12);
+        qr(2, 7, 8, 13);
+        qr(3, 4, 9, 14);
+    }
+    for (int i = 0; i < 16; i++) out[i] = x[i] + st[i];
+}
+
 extern "C" {
+
+// nblocks consecutive keystream blocks (16 words each) of the ChaCha20 stream
+// with this key (8 little-endian words) and stream id, from block `counter`.
+// Host only: no device memory or stream is touched.
+RustError gb_chacha20_blocks(const uint32_t *key, uint64_t counter, uint64_t stream, size_t nblocks, uint32_t *out)
+{
+    if (nblocks && (!key || !out)) return make_error((int)cudaErrorInvalidValue, "invalid ChaCha20 arguments");
+    for (size_t b = 0; b < nblocks; b++) host_chacha20_block(key, counter + b, stream, out + 16 * b);
+    return ok();
+}
 
 // n values by Fq::random's rejection rule from the ChaCha20Rng stream with
 // this 32-byte seed, starting at keystream word `word_offset`, into a new

@@ -138,6 +138,7 @@ def _declare(L):
             vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, vp, sz, RawGraph, vp, vp]),
         "gb_fr_permutation_products_device": (E, [vp, vp, vp, sz, sz, sz, fr, fr, fr, vp, vp, sz]),
         "gb_fr_random_chacha20": (E, [vp, vp, ctypes.c_uint64, sz, vp]),
+        "gb_chacha20_blocks": (E, [vp, ctypes.c_uint64, ctypes.c_uint64, sz, vp]),
         "gb_fr_lookup_permute_device": (E, [vp, vp, sz, sz, sz, vp, vp]),
         "gb_autotune_set": (None, [ctypes.c_int]),
         "gb_ntt_variant_set": (None, [ctypes.c_int]),

@@ -50,6 +50,32 @@ def affine_from_projective(jac):
     return np.array(_limbs(ax * _FP_R % P_MOD, 6) + _limbs(ay * _FP_R % P_MOD, 6), dtype=np.uint64)
 
 
+def affine_from_projective_batch(jacs):
+    """affine_from_projective over a batch with one field inversion
+    (Montgomery's trick): (m, 18) Jacobian rows -> (m, 12) affine rows."""
+    jacs = np.asarray(jacs, dtype=np.uint64).reshape(-1, 18)
+    zs = [_int(j[12:18]) * _FP_RINV % P_MOD for j in jacs]
+    prefix, acc = [], 1
+    for z in zs:
+        prefix.append(acc)
+        if z:
+            acc = acc * z % P_MOD
+    inv = pow(acc, -1, P_MOD)
+    out = np.zeros((len(zs), 12), dtype=np.uint64)
+    for i in range(len(zs) - 1, -1, -1):
+        z = zs[i]
+        if z == 0:
+            continue
+        zi = inv * prefix[i] % P_MOD
+        inv = inv * z % P_MOD
+        x = _int(jacs[i, 0:6]) * _FP_RINV % P_MOD
+        y = _int(jacs[i, 6:12]) * _FP_RINV % P_MOD
+        zi2 = zi * zi % P_MOD
+        ax, ay = x * zi2 % P_MOD, y * zi2 * zi % P_MOD
+        out[i] = _limbs(ax * _FP_R % P_MOD, 6) + _limbs(ay * _FP_R % P_MOD, 6)
+    return out
+
+
 def compress(affine):
     """zcash 48-byte compressed encoding of an affine point (g1.rs:1179-1211)."""
     a = np.asarray(affine, dtype=np.uint64).reshape(12)

@@ -45,7 +45,7 @@ import numpy as np
 from . import api
 from .graph import (ADD, BETA, CONSTANT, DOUBLE, FIXED, ADVICE, INSTANCE, GAMMA, HORNER, INTERMEDIATE, MUL,
                     NEGATE, PREVIOUS, SQUARE, STORE, SUB, THETA, Y, Graph)
-from .kzg import CircuitTranscript, ParamsKZG, affine_from_projective, compress, fr_to_repr
+from .kzg import CircuitTranscript, ParamsKZG, affine_from_projective_batch, compress, fr_to_repr
 from .rng import R2_LIMBS, ChaCha20Rng, fr_random, fr_random_raw, ints_to_mont, mont_to_ints
 
 R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
@@ -881,7 +881,7 @@ class GpuBackend:
     def _commit(self, h, n, count, lagrange):
         ctx = self.params.context(lagrange)
         res = ctx.device_batch(h, 0, n, count)
-        return [affine_from_projective(r) for r in res]
+        return list(affine_from_projective_batch(res))
 
     def commit_lagrange(self, h, n, count):
         return self._commit(h, n, count, True)

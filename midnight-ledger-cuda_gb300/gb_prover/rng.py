@@ -69,6 +69,24 @@ def _chacha_block_int(key_words, counter, stream=0):
     return np.array([(x[i] + st[i]) & M for i in range(16)], dtype=np.uint32)
 
 
+def _native_lib():
+    """The CUDA library once this process has loaded it (its host-side
+    gb_chacha20_blocks computes blocks in C), else None: the oracle-only
+    paths keep the restatements above."""
+    from . import _lib
+    return _lib._lib
+
+
+def _native_blocks(L, key_words, counter0, nblocks):
+    import ctypes
+    from ._lib import check
+    key = np.ascontiguousarray(key_words, dtype=np.uint32)
+    out = np.empty(16 * nblocks, dtype=np.uint32)
+    check(L.gb_chacha20_blocks(key.ctypes.data_as(ctypes.c_void_p), counter0, 0, nblocks,
+                               out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
 class ChaCha20Rng:
     def __init__(self, seed: bytes):
         if len(seed) != 32:
@@ -103,7 +121,11 @@ class ChaCha20Rng:
         if have < count:
             need = count - have
             nblocks = (need + 15) // 16
-            if nblocks <= 4:
+            L = _native_lib()
+            if L is not None:
+                nblocks = max(nblocks, 16)
+                fresh = _native_blocks(L, self._key, self._block, nblocks)
+            elif nblocks <= 4:
                 # a few words (blinding values): scalar blocks
                 fresh = np.concatenate([_chacha_block_int(self._key, self._block + b) for b in range(nblocks)])
             else:
@@ -176,10 +198,13 @@ def ints_to_mont(vals):
     return out
 
 
+_RINV = pow(1 << 256, -1, R_MOD)
+
+
 def mont_to_ints(arr):
     """(n, 4) u64 Montgomery limbs -> canonical integers"""
     arr = np.asarray(arr, dtype=np.uint64).reshape(-1, 4)
-    rinv = pow(1 << 256, -1, R_MOD)
+    rinv = _RINV
     out = []
     for row in arr:
         v = int(row[0]) | int(row[1]) << 64 | int(row[2]) << 128 | int(row[3]) << 192

@@ -116,3 +116,16 @@ def test_proof_on_the_reference_srs(gb, srs):
     gproof = plonk.create_proof(gp, gpk, advice, gbe, CircuitTranscript(), ChaCha20Rng.from_label("real-srs"))
     hproof = plonk.create_proof(hp, hpk, advice, hbe, CircuitTranscript(), ChaCha20Rng.from_label("real-srs"))
     assert gproof == hproof
+
+
+def test_native_chacha_blocks_match_restatement(gb):
+    """The library's host ChaCha20 blocks (used by ChaCha20Rng once the
+    library is loaded) equal the restatement, across the 32-bit counter
+    boundary."""
+    import numpy as np
+    from gb_prover import rng
+    key = np.arange(1, 9, dtype=np.uint32) * np.uint32(0x9E3779B9)
+    for counter, n in ((0, 1), (7, 3), ((1 << 32) - 2, 4), (1 << 40, 5)):
+        got = rng._native_blocks(gb.lib(), key, counter, n)
+        want = rng._chacha_blocks(key, counter, n).reshape(-1)
+        assert (got == want).all(), counter
