@@ -347,6 +347,13 @@ GB_API RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, R
 /* Kate quotients (f(X) - f(point)) / (X - point) of poly_count resident
  * polynomials (the division of the reference's multi-open kate scan,
  * bls12_381_g1_msm.cu:1923-1959), into a new device vector */
+/* several evaluations in one call: request r evaluates the counts[r]
+ * polynomials of poly_len coefficients in the device vector vecs[r] at
+ * points[r]; out gets sum(counts) values, request by request.  The batched
+ * form of bls12_381_g1_msm.cu:3985-4031 (one point per call there), for the
+ * evaluations a proof makes at x and its rotations. */
+GB_API RustError gb_fr_device_eval_many(RawFr *out, const void *const *vecs, const size_t *counts,
+                                        const RawFr *points, size_t requests, size_t poly_len);
 GB_API RustError gb_fr_device_kate_divide(void **out, const void *device_vec, size_t poly_len, size_t poly_count,
                                           RawFr point);
 /* Autotuner: when enabled, the plain MSM path times the window sizes

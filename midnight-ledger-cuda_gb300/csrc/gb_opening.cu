@@ -8,6 +8,8 @@
 // slice of c_i z^i, a second pass adds the slices.  Kate quotient: with
 // S_k = sum_{j >= k} f_j z^j (an additive suffix scan), q_i = S_{i+1} z^-(i+1)
 // for i < n-1 and q_{n-1} = 0; z = 0 is the shift q_i = f_{i+1}.
+#include <vector>
+
 #include "gb_vec.cuh"
 
 namespace gb {
@@ -54,6 +56,34 @@ void eval_polys(fr_t *d_out, const fr_t *polys, size_t len, size_t count, const 
     GB_CHECK_LAUNCH();
     sum_slices_kernel<<<blocks_for(count, 128), 128, 0, s>>>(partial, slices, count, d_out);
     GB_CHECK_LAUNCH();
+}
+
+// evaluations of a batch of (polynomial, point) pairs: pair p reads the
+// coefficients at polys[p] and the power row pw + row[p] * len
+struct eval_pair {
+    const fr_t *polys;
+    uint32_t row;
+};
+
+__global__ void __launch_bounds__(kEvalThreads) eval_slices_many_kernel(const eval_pair *__restrict__ pairs, size_t len,
+                                                                        const fr_t *__restrict__ pw, uint32_t slices,
+                                                                        fr_t *__restrict__ partial)
+{
+    __shared__ fr_t sh[kEvalThreads];
+    const size_t p = blockIdx.y, sl = blockIdx.x;
+    const eval_pair e = pairs[p];
+    const fr_t *c = e.polys;
+    const fr_t *z = pw + (size_t)e.row * len;
+    size_t lo = sl * kEvalSlice, hi = min(lo + kEvalSlice, len);
+    fr_t acc = fr_t::zero();
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) acc = acc + c[i] * z[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (unsigned off = blockDim.x / 2; off; off >>= 1) {
+        if (threadIdx.x < off) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[p * slices + sl] = sh[0];
 }
 
 // g[p][j] = f[p][j] * z^j
@@ -122,6 +152,45 @@ RustError midnight_sppark_bls12_381_fr_device_eval_polys(RawFr *out_raw, const v
     dev_buf<fr_t> d(poly_count, s);
     eval_polys(d, v->values, poly_len, poly_count, from_raw(point_raw), s);
     d2h(out_raw, d, poly_count * sizeof(fr_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+// Several evaluations in one call (no reference counterpart: the reference
+// makes one midnight_sppark_bls12_381_fr_device_eval_polys call per point).
+// Request r evaluates the counts[r] polynomials of poly_len coefficients held
+// by vecs[r] at points[r]; out receives the values request by request.
+RustError gb_fr_device_eval_many(RawFr *out_raw, const void *const *vecs, const size_t *counts,
+                                 const RawFr *points_raw, size_t requests, size_t poly_len)
+{
+    if (!out_raw || !vecs || !counts || !points_raw || requests == 0 || poly_len == 0 || requests > 65535)
+        return make_error((int)cudaErrorInvalidValue, "invalid batched evaluation arguments");
+    GB_ENTRY_BEGIN
+    std::vector<eval_pair> pairs;
+    for (size_t r = 0; r < requests; r++) {
+        auto *v = reinterpret_cast<const fr_device_vec *>(vecs[r]);
+        if (!v || counts[r] == 0 || counts[r] > SIZE_MAX / poly_len || v->len != counts[r] * poly_len)
+            return make_error((int)cudaErrorInvalidValue, "batched evaluation shape mismatch");
+        for (size_t p = 0; p < counts[r]; p++) pairs.push_back(eval_pair{v->values + p * poly_len, (uint32_t)r});
+    }
+    if (pairs.size() > 65535) return make_error((int)cudaErrorInvalidValue, "too many batched evaluations");
+    cudaStream_t s = lane_stream();
+    for (size_t r = 0; r < requests; r++) device_vec_wait(reinterpret_cast<const fr_device_vec *>(vecs[r]), s);
+    const size_t total = pairs.size();
+    dev_buf<fr_t> d_points(requests, s), pw(requests * poly_len, s), d_out(total, s);
+    dev_buf<eval_pair> d_pairs(total, s);
+    h2d(d_points, points_raw, requests * sizeof(fr_t), s);
+    h2d(d_pairs, pairs.data(), total * sizeof(eval_pair), s);
+    omega_powers_many(pw, d_points, requests, poly_len, s);
+    const uint32_t slices = (uint32_t)((poly_len + kEvalSlice - 1) / kEvalSlice);
+    dev_buf<fr_t> partial(total * slices, s);
+    eval_slices_many_kernel<<<dim3(slices, (unsigned)total), kEvalThreads, 0, s>>>(d_pairs, poly_len, pw, slices,
+                                                                                 partial);
+    GB_CHECK_LAUNCH();
+    sum_slices_kernel<<<blocks_for(total, 128), 128, 0, s>>>(partial, slices, total, d_out);
+    GB_CHECK_LAUNCH();
+    d2h(out_raw, d_out, total * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
     return ok();
     GB_ENTRY_END

@@ -279,6 +279,46 @@ __global__ void power_apply_kernel(const fr_t *__restrict__ tables, size_t n, fr
     d[i] = v;
 }
 
+// the tables of power_tables_kernel for several points: block q reads
+// points[q] and writes tables[q * 768 ..]
+__global__ void __launch_bounds__(256) power_tables_many_kernel(const fr_t *__restrict__ points,
+                                                                fr_t *__restrict__ tables)
+{
+    __shared__ fr_t sh[256];
+    fr_t base = points[blockIdx.x];
+    fr_t *t = tables + (size_t)blockIdx.x * 768;
+    for (int level = 0; level < 3; level++) {
+        block_scan_mul(base, sh);  // sh[t] = base^(t+1)
+        __syncthreads();
+        t[level * 256 + threadIdx.x] = threadIdx.x ? sh[threadIdx.x - 1] : fr_t::one();
+        base = sh[255];
+        __syncthreads();
+    }
+}
+
+// d[q * n + i] = tables_q-powers, i < n <= 2^24, one grid row per point
+__global__ void power_apply_many_kernel(const fr_t *__restrict__ tables, size_t n, fr_t *__restrict__ d)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const fr_t *t = tables + (size_t)blockIdx.y * 768;
+    fr_t v = t[i & 255];
+    if (i >> 8) v = v * t[256 + ((i >> 8) & 255)];
+    if (i >> 16) v = v * t[512 + (i >> 16)];
+    d[(size_t)blockIdx.y * n + i] = v;
+}
+
+void omega_powers_many(fr_t *d, const fr_t *d_points, size_t npoints, size_t n, cudaStream_t s)
+{
+    if (!n || !npoints) return;
+    if (n > ((size_t)1 << 24) || npoints > 65535) throw cuda_error((int)cudaErrorInvalidValue, "power table too large");
+    dev_buf<fr_t> tables(768 * npoints, s);
+    power_tables_many_kernel<<<(unsigned)npoints, 256, 0, s>>>(d_points, tables);
+    GB_CHECK_LAUNCH();
+    power_apply_many_kernel<<<dim3(blocks_for(n, 256), (unsigned)npoints), 256, 0, s>>>(tables, n, d);
+    GB_CHECK_LAUNCH();
+}
+
 void omega_powers(fr_t *d, const fr_t &w, size_t n, cudaStream_t s)
 {
     if (!n) return;

@@ -13,5 +13,8 @@ void batch_invert(fr_t *out, const fr_t *in, size_t n, const fr_t *mul, cudaStre
 void suffix_sum(fr_t *out, const fr_t *in, size_t n, cudaStream_t s);
 // d[i] = w^i for i < n
 void omega_powers(fr_t *d, const fr_t &w, size_t n, cudaStream_t s);
+// d[q * n + i] = points[q]^i for q < npoints, i < n <= 2^24 (points on the
+// device)
+void omega_powers_many(fr_t *d, const fr_t *d_points, size_t npoints, size_t n, cudaStream_t s);
 
 }  // namespace gb

@@ -116,6 +116,7 @@ def _declare(L):
         "gb_g1_to_lagrange": (E, [vp, vp, u32]),
         "midnight_sppark_bls12_381_fr_device_eval_polys": (E, [vp, vp, sz, sz, fr]),
         "gb_fr_device_kate_divide": (E, [vp, vp, sz, sz, fr]),
+        "gb_fr_device_eval_many": (E, [vp, vp, vp, vp, sz, sz]),
         "gb_kzg_setup": (E, [vp, vp, fr, u32]),
         "gb_transfer_counters": (None, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
         "gb_transfer_counters_reset": (None, []),

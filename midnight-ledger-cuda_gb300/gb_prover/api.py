@@ -23,7 +23,7 @@ __all__ = [
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "PROFILE_MSM_SORT",
     "PROFILE_MSM_FIXUP", "PROFILE_MSM_REDUCE", "bls12_381_eval_numerator",
-    "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_kate_divide",
+    "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_eval_many", "fr_device_kate_divide",
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
     "fr_lookup_permute_device", "autotune_set", "autotune_reset", "autotune_report",
 ]
@@ -506,6 +506,23 @@ def bls12_381_fr_device_eval_polys(devvec, poly_len, poly_count, point):
     check(lib().midnight_sppark_bls12_381_fr_device_eval_polys(_ptr(out), devvec.raw, poly_len, poly_count,
                                                                 _fr(point)))
     return out
+
+
+def fr_device_eval_many(requests, poly_len):
+    """Several evaluations in one call (gb_fr_device_eval_many): requests are
+    (device vector, polynomial count, point); returns one (count, 4) array
+    per request."""
+    vecs = (ctypes.c_void_p * len(requests))(*[r[0].raw for r in requests])
+    counts = np.array([r[1] for r in requests], dtype=np.uintp)
+    points = _fr_arr([r[2] for r in requests])
+    out = np.zeros((int(counts.sum()), 4), dtype=np.uint64)
+    check(lib().gb_fr_device_eval_many(_ptr(out), ctypes.cast(vecs, ctypes.c_void_p), _ptr(counts), _ptr(points),
+                                       len(requests), poly_len))
+    res, o = [], 0
+    for r in requests:
+        res.append(out[o:o + r[1]])
+        o += r[1]
+    return res
 
 
 def fr_device_kate_divide(devvec, poly_len, poly_count, point):

@@ -686,31 +686,41 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     x_next = dom.rotate_omega(x, 1)
     x_prev = dom.rotate_omega(x, -1)
     x_last = dom.rotate_omega(x, -(bf + 1))
-    for ev in _evals_at_rotations(backend, adv_c, n, m, dom, x, c.advice_queries):
-        transcript.write_scalar(w(ev))
-    for ev in _evals_at_rotations(backend, pk.fixed_coeffs, n, c.num_fixed, dom, x, c.fixed_queries):
-        transcript.write_scalar(w(ev))
+    # every evaluation at x and its rotations, in one batched call; written
+    # to the transcript in the reference's order below
+    adv_rots = list(dict.fromkeys(r for _, r in c.advice_queries))
+    fix_rots = list(dict.fromkeys(r for _, r in c.fixed_queries))
+    reqs = [(adv_c, m, w(dom.rotate_omega(x, rot))) for rot in adv_rots]
+    reqs += [(pk.fixed_coeffs, c.num_fixed, w(dom.rotate_omega(x, rot))) for rot in fix_rots]
+    reqs += [(random_poly, 1, w(x)), (pk.sigma_coeffs, m, w(x)), (zp_c, sets, w(x)), (zp_c, sets, w(x_next))]
+    if sets > 1:
+        reqs.append((zp_c, sets, w(x_last)))
+    if L:
+        reqs += [(zl_c, L, w(x)), (zl_c, L, w(x_next)), (perm_c, 2 * L, w(x)), (perm_c, 2 * L, w(x_prev))]
+    vals = [[fr_int(v) for v in arr] for arr in backend.eval_many(reqs, n)]
+    adv_at = dict(zip(adv_rots, vals[:len(adv_rots)]))
+    fix_at = dict(zip(fix_rots, vals[len(adv_rots):len(adv_rots) + len(fix_rots)]))
+    rest = iter(vals[len(adv_rots) + len(fix_rots):])
+    for col, rot in c.advice_queries:
+        transcript.write_scalar(w(adv_at[rot][col]))
+    for col, rot in c.fixed_queries:
+        transcript.write_scalar(w(fix_at[rot][col]))
     # vanishing.evaluate: the combined h polynomial and the random eval (vanishing/prover.rs:321-383)
     split = pow(x, n - 1, R)
     h_poly = backend.lincomb(h_pieces, n, pieces_n, ints_to_mont([pow(split, i, R) for i in range(pieces_n)]))
-    random_eval = fr_int(backend.eval_polys(random_poly, n, 1, w(x))[0])
+    random_eval = next(rest)[0]
     transcript.write_scalar(w(random_eval))
-    sig_ev = [fr_int(v) for v in backend.eval_polys(pk.sigma_coeffs, n, m, w(x))]
-    for v in sig_ev:
+    for v in next(rest):
         transcript.write_scalar(w(v))
-    zp_x = [fr_int(v) for v in backend.eval_polys(zp_c, n, sets, w(x))]
-    zp_xn = [fr_int(v) for v in backend.eval_polys(zp_c, n, sets, w(x_next))]
-    zp_xl = [fr_int(v) for v in backend.eval_polys(zp_c, n, sets, w(x_last))] if sets > 1 else []
+    zp_x, zp_xn = next(rest), next(rest)
+    zp_xl = next(rest) if sets > 1 else []
     for s in range(sets):
         transcript.write_scalar(w(zp_x[s]))
         transcript.write_scalar(w(zp_xn[s]))
         if s + 1 < sets:
             transcript.write_scalar(w(zp_xl[s]))
     if L:
-        zl_x = [fr_int(v) for v in backend.eval_polys(zl_c, n, L, w(x))]
-        zl_xn = [fr_int(v) for v in backend.eval_polys(zl_c, n, L, w(x_next))]
-        pp_x = [fr_int(v) for v in backend.eval_polys(perm_c, n, 2 * L, w(x))]
-        pp_xp = [fr_int(v) for v in backend.eval_polys(perm_c, n, 2 * L, w(x_prev))]
+        zl_x, zl_xn, pp_x, pp_xp = next(rest), next(rest), next(rest), next(rest)
         for li in range(L):
             for v in (zl_x[li], zl_xn[li], pp_x[2 * li], pp_xp[2 * li], pp_x[2 * li + 1]):
                 transcript.write_scalar(w(v))
@@ -731,14 +741,6 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     queries += [(P(h_poly, 0), x), (P(random_poly, 0), x)]
     multi_open(params, backend, n, queries, transcript)
     return transcript.finalize()
-
-
-def _evals_at_rotations(backend, h, n, count, dom, x, queries):
-    """evaluations of the queried columns, one batched evaluation per rotation"""
-    at = {}
-    for rot in dict.fromkeys(r for _, r in queries):
-        at[rot] = [fr_int(v) for v in backend.eval_polys(h, n, count, fr_mont(dom.rotate_omega(x, rot)))]
-    return [at[rot][col] for col, rot in queries]
 
 
 def construct_intermediate_sets(queries):
@@ -873,6 +875,9 @@ class GpuBackend:
 
     def eval_polys(self, h, n, count, point):
         return api.bls12_381_fr_device_eval_polys(h, n, count, point)
+
+    def eval_many(self, requests, n):
+        return api.fr_device_eval_many(requests, n)
 
     def kate_divide(self, h, n, count, point):
         return api.fr_device_kate_divide(h, n, count, point)

@@ -127,6 +127,9 @@ class OracleBackend:
     def eval_polys(self, h, n, count, point):
         return np.stack([orc.fr_eval_poly(h.a[i * n:(i + 1) * n], point) for i in range(count)])
 
+    def eval_many(self, requests, n):
+        return [self.eval_polys(h, n, count, point) for h, count, point in requests]
+
     def kate_divide(self, h, n, count, point):
         out = np.zeros((n * count, 4), dtype=np.uint64)
         for i in range(count):

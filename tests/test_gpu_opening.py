@@ -59,3 +59,21 @@ def test_device_random_draw_matches_host(gb, pre_words, n):
     assert (vec.download() == want).all()
     assert a.word_position() == b.word_position()
     vec.free()
+
+
+def test_eval_many_matches_single_evaluations(gb, orc):
+    """gb_fr_device_eval_many over requests of different vectors, counts and
+    points equals one evaluation call per request (itself pinned to the
+    oracle in this file)."""
+    import numpy as np
+    rng = np.random.default_rng(91)
+    n = 1 << 12
+    vecs = [gb.Bls12_381FrDeviceVec.upload(orc.fr_random(c * n, rng)) for c in (3, 1, 5)]
+    pts = orc.fr_random(6, rng)
+    reqs = [(vecs[0], 3, pts[0]), (vecs[1], 1, pts[1]), (vecs[2], 5, pts[2]), (vecs[0], 3, pts[3]),
+            (vecs[2], 5, pts[4]), (vecs[1], 1, orc.fr_from_ints([0])[0])]
+    got = gb.fr_device_eval_many(reqs, n)
+    for (v, c, p), g in zip(reqs, got):
+        assert (g == gb.bls12_381_fr_device_eval_polys(v, n, c, p)).all()
+    want0 = orc.fr_eval_poly(vecs[1].download()[:n], pts[1])
+    assert (got[1][0] == want0).all()
