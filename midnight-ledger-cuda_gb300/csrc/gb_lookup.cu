@@ -9,7 +9,9 @@
 //   values left after removing one copy of every distinct input, in sorted
 //   order, fill the remaining rows from the bottom up;
 //   rows u.. of A' and S' are the caller's blinds.
-// Sorting is a radix sort of canonical keys; every run start looks up the
+// Sorting is a radix sort of canonical keys (by their top 64-bit limb; by
+// the whole key only when two distinct values share a top limb, which a
+// check after the sort detects); every run start looks up the
 // first equal table entry by binary search (marking it used); two exclusive
 // scans give each leftover table value its rank and each repeated row its
 // rank from the bottom.  An input value missing from the table is the
@@ -30,6 +32,12 @@ struct ckey_decomposer {
     {
         return {k.l[3], k.l[2], k.l[1], k.l[0]};
     }
+};
+
+// the top limb alone: canonical order whenever no two distinct values
+// share it (equal values may sit in any order)
+struct ckey_top_decomposer {
+    __host__ __device__ ::cuda::std::tuple<uint64_t &> operator()(ckey &k) const { return {k.l[3]}; }
 };
 
 __device__ __forceinline__ int ckey_cmp(const ckey &a, const ckey &b)
@@ -87,6 +95,17 @@ __global__ void lk_match_kernel(const ckey *__restrict__ as, const ckey *__restr
     else atomicExch(missing, 1);
 }
 
+// after a sort by the top limb: flag two neighbours with the same top limb
+// but different values (the order among them is then not canonical)
+__global__ void lk_tie_kernel(const ckey *__restrict__ as, const ckey *__restrict__ ts, size_t u, int *tie)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 || i >= u) return;
+    if ((as[i].l[3] == as[i - 1].l[3] && ckey_cmp(as[i], as[i - 1]) != 0) ||
+        (ts[i].l[3] == ts[i - 1].l[3] && ckey_cmp(ts[i], ts[i - 1]) != 0))
+        atomicExch(tie, 1);
+}
+
 __global__ void lk_fill_kernel(uint32_t *keep, size_t u)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -130,8 +149,20 @@ static void exclusive_scan_u32(const uint32_t *in, uint32_t *out, size_t n, cuda
     GB_CUDA_OK(cub::DeviceScan::ExclusiveSum(t.get(), temp, in, out, (int)n, s));
 }
 
-// one lookup: a, t = compressed input / table (u rows read); outputs u rows
-static void permute_pair(const fr_t *a, const fr_t *t, size_t u, fr_t *a_out, fr_t *s_out, int *d_flags,
+template <class D>
+static void sort_ckeys(ckey *in_a, ckey *out_a, ckey *in_t, ckey *out_t, size_t u, int end_bit, cudaStream_t s)
+{
+    size_t temp = 0;
+    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(nullptr, temp, in_a, out_a, (int64_t)u, D{}, 0, end_bit, s));
+    dev_buf<uint8_t> tmp(temp, s);
+    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(tmp.get(), temp, in_a, out_a, (int64_t)u, D{}, 0, end_bit, s));
+    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(tmp.get(), temp, in_t, out_t, (int64_t)u, D{}, 0, end_bit, s));
+}
+
+// one lookup: a, t = compressed input / table (u rows read); outputs u rows.
+// full = false sorts by the top limb and raises d_flags[2] when that order
+// is not canonical (the caller then repeats with full = true).
+static void permute_pair(const fr_t *a, const fr_t *t, size_t u, fr_t *a_out, fr_t *s_out, int *d_flags, bool full,
                          cudaStream_t s)
 {
     dev_buf<ckey> ka(u, s), kt(u, s), sa(u, s), st(u, s), left(u, s);
@@ -139,14 +170,13 @@ static void permute_pair(const fr_t *a, const fr_t *t, size_t u, fr_t *a_out, fr
     const unsigned grid = blocks_for(u, 256);
     lk_keys_kernel<<<grid, 256, 0, s>>>(a, t, u, ka, kt);
     GB_CHECK_LAUNCH();
-    size_t temp = 0;
-    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(nullptr, temp, ka.get(), sa.get(), (int64_t)u, ckey_decomposer{}, 0,
-                                              256, s));
-    dev_buf<uint8_t> tmp(temp, s);
-    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(tmp.get(), temp, ka.get(), sa.get(), (int64_t)u, ckey_decomposer{}, 0,
-                                              256, s));
-    GB_CUDA_OK(cub::DeviceRadixSort::SortKeys(tmp.get(), temp, kt.get(), st.get(), (int64_t)u, ckey_decomposer{}, 0,
-                                              256, s));
+    if (full) {
+        sort_ckeys<ckey_decomposer>(ka, sa, kt, st, u, 256, s);
+    } else {
+        sort_ckeys<ckey_top_decomposer>(ka, sa, kt, st, u, 64, s);
+        lk_tie_kernel<<<grid, 256, 0, s>>>(sa, st, u, d_flags + 2);
+        GB_CHECK_LAUNCH();
+    }
     lk_fill_kernel<<<grid, 256, 0, s>>>(keep, u);
     GB_CHECK_LAUNCH();
     lk_match_kernel<<<grid, 256, 0, s>>>(sa, st, u, repeated, keep, d_flags);
@@ -184,20 +214,27 @@ RustError gb_fr_lookup_permute_device(void **out, const void *compressed_vec, si
     device_vec_wait(cv, s);
     const size_t nb = len - usable_rows;
     fr_device_vec *v = device_vec_new(2 * lookup_count * len, s);
-    int flags[2] = {0, 0};
+    int flags[3] = {0, 0, 0};
     try {
-        dev_buf<int> d_flags(2, s);
-        GB_CUDA_OK(cudaMemsetAsync(d_flags.get(), 0, 2 * sizeof(int), s));
-        for (size_t l = 0; l < lookup_count; l++) {
-            const fr_t *a = cv->values + 2 * l * len, *t = a + len;
-            fr_t *a_out = v->values + 2 * l * len, *s_out = a_out + len;
-            permute_pair(a, t, usable_rows, a_out, s_out, d_flags, s);
-            h2d(a_out + usable_rows, input_blinds + l * nb, nb * sizeof(fr_t), s);
-            h2d(s_out + usable_rows, table_blinds + l * nb, nb * sizeof(fr_t), s);
+        dev_buf<int> d_flags(3, s);
+        // sorted by the top limb first; on a tie of distinct values, again
+        // with the whole canonical key
+        for (int full = 0; full < 2; full++) {
+            GB_CUDA_OK(cudaMemsetAsync(d_flags.get(), 0, 3 * sizeof(int), s));
+            for (size_t l = 0; l < lookup_count; l++) {
+                const fr_t *a = cv->values + 2 * l * len, *t = a + len;
+                fr_t *a_out = v->values + 2 * l * len, *s_out = a_out + len;
+                permute_pair(a, t, usable_rows, a_out, s_out, d_flags, full != 0, s);
+                if (full == 0) {
+                    h2d(a_out + usable_rows, input_blinds + l * nb, nb * sizeof(fr_t), s);
+                    h2d(s_out + usable_rows, table_blinds + l * nb, nb * sizeof(fr_t), s);
+                }
+            }
+            d2h(flags, d_flags, 3 * sizeof(int), s);
+            GB_CUDA_OK(cudaStreamSynchronize(s));
+            if (!flags[2]) break;
         }
-        d2h(flags, d_flags, 2 * sizeof(int), s);
         device_vec_mark_ready(v, s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
     } catch (...) {
         device_vec_delete(v);
         throw;

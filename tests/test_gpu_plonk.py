@@ -129,3 +129,25 @@ def test_native_chacha_blocks_match_restatement(gb):
         got = rng._native_blocks(gb.lib(), key, counter, n)
         want = rng._chacha_blocks(key, counter, n).reshape(-1)
         assert (got == want).all(), counter
+
+
+def test_device_lookup_permutation_top_limb_ties(gb, orc):
+    """Distinct values that share their top 64-bit limb: the sort by the
+    top limb alone is then not canonical, and the device permutation must
+    fall back to the whole key (equal to the host permutation)."""
+    import numpy as np
+    from oracle.plonk_cpu import OracleBackend
+    rng = np.random.default_rng(1234)
+    n, u, tsize = 1024, 1018, 300
+    top = 0x1234567890ABCDEF << 192
+    ints = sorted({top + int(x) for x in rng.integers(0, 1 << 62, size=tsize)})
+    table_vals = orc.fr_from_ints(ints[:tsize])
+    tab = table_vals[rng.integers(0, len(table_vals), size=n)]
+    tab[:len(table_vals)] = table_vals
+    inp = table_vals[rng.integers(0, 40, size=n)]
+    comp = np.concatenate([inp, tab])
+    nb = n - u
+    ib, tb = orc.fr_random(nb, rng), orc.fr_random(nb, rng)
+    want = OracleBackend(None).permute_lookups(OracleBackend(None).put(comp), n, u, 1, ib, tb).a
+    got = gb.fr_lookup_permute_device(gb.Bls12_381FrDeviceVec.upload(comp), n, u, 1, ib, tb).download()
+    assert (got == want).all()
