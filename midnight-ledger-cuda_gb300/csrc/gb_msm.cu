@@ -476,6 +476,7 @@ __global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__rest
 static constexpr uint32_t kCoopLanes = 8;
 static constexpr uint32_t kCoopGroups = 16;  // groups per 128-thread block
 static constexpr uint64_t kCoopMaxBuckets = 8u << 15;  // cooperative reduction up to 8 x 2^15 buckets
+static constexpr uint64_t kCoopGroupBudget = 6144;     // groups of the cooperative reduction over a batch
 // slots of a group: RUN, SUM, OPD (operand), RES (4 each: X, Y, ZZ, ZZZ),
 // then 12 temporaries
 enum { CO_RUN = 0, CO_SUM = 4, CO_OPD = 8, CO_RES = 12, CO_TMP = 16, CO_SLOTS = 28 };
@@ -855,11 +856,14 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     S = std::min<uint32_t>(K, S);
     // Few buckets in all (a single MSM or a small batch): the reduction is a
     // latency-bound chain per sub-segment, run by cooperative 8-lane groups,
-    // ~8192 groups over the batch.  Many buckets (large batches): the
-    // one-thread-per-chain kernel keeps the multiply-add pipe busier.
+    // at most 6144 groups over the batch (more groups shorten the running
+    // sums but add a double-and-add each: measured best at 4096 groups for
+    // one MSM of 2^15 buckets, 6144 for three).  Many buckets (large
+    // batches): the one-thread-per-chain kernel keeps the multiply-add pipe
+    // busier.
     const bool coop_reduce = (uint64_t)nseg * K <= kCoopMaxBuckets && K >= kCoopGroups;
     uint32_t S_coop = kCoopGroups;
-    while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= 8192) S_coop *= 2;
+    while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= kCoopGroupBudget) S_coop *= 2;
     const uint64_t nchunks = std::max<uint64_t>(1, (digits_total + L - 1) / L);
     const int variant = default_acc_variant();
 
