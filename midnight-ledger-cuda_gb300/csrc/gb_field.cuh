@@ -601,6 +601,73 @@ struct mont_t {
         }
         return acc;
     }
+    // this^-1 by the binary extended Euclidean algorithm (Stein's binary
+    // GCD carrying the Bezout coefficient, Knuth TAOCP vol. 2, 4.5.2 and
+    // exercise 4.5.2-39); zero maps to zero.  With u = this, v = m and
+    // x1 a = u, x2 a = v (mod m) held throughout, halvings and subtractions
+    // bring u or v to 1 in at most 2 log2(m) steps.  The Montgomery form is
+    // restored by two products with R^2 (the plain inverse of aR is
+    // a^-1 R^-1).  Its dependent chain is short next to the 300-odd products
+    // of a Fermat inversion, so a single thread inverts much sooner; its
+    // data-dependent branches suit one inversion per tile, not one per
+    // thread of a warp.
+    GB_COLD mont_t inverse_binary() const
+    {
+        if (is_zero()) return *this;
+        uint32_t u[N], w[N], x1[N], x2[N], m[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            u[i] = v[i];
+            w[i] = m[i] = Cfg::mod(i);
+            x1[i] = x2[i] = 0;
+        }
+        x1[0] = 1;
+        auto is_one = [](const uint32_t *a) {
+            uint32_t x = a[0] ^ 1u;
+            for (int i = 1; i < N; i++) x |= a[i];
+            return x == 0;
+        };
+        // a /= 2 with an extra top bit
+        auto half = [](uint32_t *a, uint32_t top) {
+            for (int i = 0; i < N - 1; i++) a[i] = (a[i] >> 1) | (a[i + 1] << 31);
+            a[N - 1] = (a[N - 1] >> 1) | (top << 31);
+        };
+        // x / 2 mod m (m odd, x < m)
+        auto half_mod = [&](uint32_t *x) {
+            uint32_t top = 0;
+            if (x[0] & 1u) top = mp_add<N>(x, x, m);
+            half(x, top);
+        };
+        // x = x - y mod m (x, y < m)
+        auto sub_mod = [&](uint32_t *x, const uint32_t *y) {
+            if (mp_sub<N>(x, x, y)) mp_add<N>(x, x, m);
+        };
+        while (!is_one(u) && !is_one(w)) {
+            while (!(u[0] & 1u)) {
+                half(u, 0);
+                half_mod(x1);
+            }
+            while (!(w[0] & 1u)) {
+                half(w, 0);
+                half_mod(x2);
+            }
+            uint32_t d[N];
+            if (!mp_sub<N>(d, u, w)) {  // u >= w
+                for (int i = 0; i < N; i++) u[i] = d[i];
+                sub_mod(x1, x2);
+            } else {
+                mp_sub<N>(w, w, u);
+                sub_mod(x2, x1);
+            }
+        }
+        mont_t r, r2;
+        const uint32_t *res = is_one(u) ? x1 : x2;
+        for (int i = 0; i < N; i++) {
+            r.v[i] = res[i];
+            r2.v[i] = Cfg::r2(i);
+        }
+        return (r * r2) * r2;
+    }
     // this^e for a 64-bit exponent
     GB_COLD mont_t pow_u64(uint64_t e) const
     {

@@ -121,9 +121,18 @@ void kate_divide(fr_t *d_out, const fr_t *f, size_t len, size_t count, const fr_
         GB_CHECK_LAUNCH();
         return;
     }
-    dev_buf<fr_t> pw(len, s), ipw(len, s), g(total, s);
-    omega_powers(pw, z, len, s);
-    omega_powers(ipw, z.inverse(), len, s);
+    // powers of z and of 1/z (rows 0 and 1 of pws), in one launch pair up
+    // to 2^24 coefficients
+    dev_buf<fr_t> zs(2, s), pws(2 * len, s), g(total, s);
+    const fr_t hz[2] = {z, z.inverse()};
+    if (len <= ((size_t)1 << 24)) {
+        h2d(zs, hz, sizeof(hz), s);
+        omega_powers_many(pws, zs, 2, len, s);
+    } else {
+        omega_powers(pws, hz[0], len, s);
+        omega_powers(pws.get() + len, hz[1], len, s);
+    }
+    const fr_t *pw = pws.get(), *ipw = pws.get() + len;
     scale_by_powers_kernel<<<blocks_for(total, 256), 256, 0, s>>>(f, pw, len, total, g);
     GB_CHECK_LAUNCH();
     for (size_t p = 0; p < count; p++) suffix_sum(g.get() + p * len, g.get() + p * len, len, s);

@@ -194,7 +194,7 @@ void suffix_sum(fr_t *out, const fr_t *in, size_t n, cudaStream_t s)
 
 // ------------------------------------------------------------ batch inversion
 
-// Montgomery's trick per tile: one Fermat inversion per tile of 2048
+// Montgomery's trick per tile: one binary-GCD inversion per tile of 2048
 // elements; zeros stay zero (the field inverse the reference applies maps
 // 0 to 0).  out may alias in.  If `mul` is given, out[i] = mul[i] / in[i].
 __global__ void __launch_bounds__(kScanThreads) batch_invert_kernel(const fr_t *in, size_t n,
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kScanThreads) batch_invert_kernel(const fr_t *
     fr_t incl = block_scan_mul(p, sh);
     __syncthreads();
     fr_t excl = threadIdx.x ? sh[threadIdx.x - 1] : fr_t::one();
-    if (threadIdx.x == blockDim.x - 1) total_inv = incl.inverse();
+    if (threadIdx.x == blockDim.x - 1) total_inv = incl.inverse_binary();
     __syncthreads();
     fr_t suffix_incl = block_suffix_scan_mul(p, sh);
     __syncthreads();

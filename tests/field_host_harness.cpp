@@ -27,6 +27,23 @@ void h_fp_inv(uint64_t *out, const uint64_t *a)
     memcpy(out, &r, 48);
 }
 
+// the binary-GCD inverse (mont_t::inverse_binary) of Fp and Fr
+void h_fp_inv_binary(uint64_t *out, const uint64_t *a)
+{
+    fp_t x;
+    memcpy(&x, a, 48);
+    fp_t r = x.inverse_binary();
+    memcpy(out, &r, 48);
+}
+
+void h_fr_inv_binary(uint64_t *out, const uint64_t *a)
+{
+    fr_t x;
+    memcpy(&x, a, 32);
+    fr_t r = x.inverse_binary();
+    memcpy(out, &r, 32);
+}
+
 void h_fr_mul(uint64_t *out, const uint64_t *a, const uint64_t *b)
 {
     fr_t x, y;

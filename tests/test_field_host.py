@@ -89,3 +89,18 @@ def test_xyzz_formulas(hh, orc):
         hh.h_xyzz_mul_small(_p(out), _p(g), k)
         want = affine_of(orc, orc.g1_mul(g, orc.fr_from_ints([k])[0]))[0]
         assert (out == want).all(), k
+
+
+def test_binary_gcd_inverse(hh, orc):
+    """mont_t::inverse_binary (the batch inversion's tile inverse) against
+    pow(a, -1) for Fp and Fr, with the edge values 0, 1, 2 and m - 1."""
+    rng = np.random.default_rng(22)
+    P, R = orc.P_MOD, orc.R_MOD
+    for a in [0, 1, 2, P - 1, P - 2, (P + 1) // 2] + [int.from_bytes(rng.bytes(48), "little") % P for _ in range(150)]:
+        out = np.zeros(6, dtype=np.uint64)
+        hh.h_fp_inv_binary(_p(out), _p(orc.fp_from_int(a)))
+        assert orc.fp_to_int(out) == (pow(a, -1, P) if a else 0)
+    for a in [0, 1, 2, R - 1, R - 2, (R + 1) // 2] + [int.from_bytes(rng.bytes(32), "little") % R for _ in range(150)]:
+        out = np.zeros(4, dtype=np.uint64)
+        hh.h_fr_inv_binary(_p(out), _p(orc.fr_from_ints([a])[0]))
+        assert orc.fr_to_ints(out)[0] == (pow(a, -1, R) if a else 0)
