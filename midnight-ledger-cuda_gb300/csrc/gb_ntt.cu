@@ -878,6 +878,13 @@ void set_ntt_smem()
     });
 }
 
+static int sm_count()
+{
+    static int n = 0;
+    if (!n) GB_CUDA_OK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, current_device()));
+    return n;
+}
+
 // (s_hi, g) of each pass: ceil(log_n / 10) passes of near-equal size, the
 // larger ones first
 std::vector<std::pair<int, int>> pass_split(uint32_t log_n)
@@ -937,14 +944,20 @@ static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, cons
         const fr_t *tab = pass_twiddles(log_n, inverse, s_hi, g, tw, s);
         int q = kPassBits - g;
         size_t ctas;
+        auto ctas_for = [&](int qq) {
+            const size_t total = count << (log_n - g);
+            return s_lo > 0 ? total >> qq : (total + ((size_t)1 << qq) - 1) >> qq;
+        };
         if (s_lo > 0) {
             q = std::min(q, s_lo);
-            ctas = (count << (log_n - g)) >> q;
         } else {
             const size_t total = count << (log_n - g);
             while (q > 0 && ((size_t)1 << (q - 1)) >= total) q--;
-            ctas = (total + ((size_t)1 << q) - 1) >> q;
         }
+        // small transforms: fewer sub-blocks per CTA until there are two
+        // CTAs per SM (a single 2^16 transform is otherwise 64 CTAs)
+        while (q > 0 && ctas_for(q) < 2 * (size_t)sm_count()) q--;
+        ctas = ctas_for(q);
         const uint32_t nd = 1u << (g + q);
         const uint32_t tw_entries = s_lo > 0 ? nd : 1u << g;
         const size_t smem = ((size_t)nd + tw_entries) * sizeof(fr_t);
