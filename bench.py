@@ -42,7 +42,7 @@ METRIC = "G1 MSM Mpts/s at 2^20"
 FP_MULS_PER_MADD = 10    # XYZZ mixed addition: 8M + 2S
 FP_MULS_PER_ADD = 14     # XYZZ addition: 12M + 2S
 MADDS_PER_FP_MUL = 300   # 2 * 12^2 + 12 32x32->64 multiply-adds per Fp product
-ACC_DRAM_BYTES_PER_ENTRY = 784.65e6 / ((1 << 18) * 16)  # ncu, n = 2^18 launch (c = 16: 16 windows)
+ACC_DRAM_BYTES_PER_ENTRY = 801.33e6 / ((1 << 18) * 16)  # ncu, n = 2^18 launch (c = 16: 16 windows)
 
 
 def fr_uniform(n, rng):
@@ -326,7 +326,7 @@ def main():
                                   % (c_star, windows(c_star)),
         "avg_launch_ms": acc_avg_s * 1e3, "launches": acc_n,
         # DRAM bytes of one accumulate launch: the ncu capture of the n=2^18
-        # launch (dram__bytes_read.sum + dram__bytes_write.sum = 784.65 MB over
+        # launch (dram__bytes_read.sum + dram__bytes_write.sum = 801.33 MB over
         # 2^18 x 16 digit entries) scaled by this launch's n x W entries
         "traffic": ACC_DRAM_BYTES_PER_ENTRY * n * windows(c_star),
         "traffic_source": "ncu capture at n=2^18, scaled per digit entry",
