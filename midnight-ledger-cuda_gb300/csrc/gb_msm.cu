@@ -1164,6 +1164,20 @@ static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const st
     timed_collect();
 }
 
+// The device address of page-locked host memory (mapped into the unified
+// address space, so kernels read it over the host link), or null for
+// pageable or device memory.
+static const fr_t *pinned_device_view(const fr_t *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return reinterpret_cast<const fr_t *>(a.devicePointer);
+}
+
 static void context_run_device(msm_context_t *ctx, jacobian_t *out_host, const fr_t *d_scalars, size_t npoints,
                                size_t nmsms, cudaStream_t s)
 {
@@ -1272,6 +1286,13 @@ RustError midnight_sppark_bls12_381_g1_msm_context_batch(RawG1Projective *out_ra
     if (!out || (npoints && !scalars)) return make_error((int)cudaErrorInvalidValue, "invalid MSM batch arguments");
     if (npoints > ctx->npoints) return make_error((int)cudaErrorInvalidValue, "more scalars than context bases");
     cudaStream_t s = lane_stream();
+    // page-locked host scalars are read in place by the recode kernel over
+    // the host link, with no staging copy; pageable ones are staged
+    if (const fr_t *view = pinned_device_view(scalars)) {
+        count_transfer(true, npoints * nmsms * sizeof(fr_t));
+        context_run_device(ctx, out, view, npoints, nmsms, s);
+        return ok();
+    }
     dev_buf<fr_t> d_scalars(npoints * nmsms, s);
     h2d(d_scalars, scalars, npoints * nmsms * sizeof(fr_t), s);
     context_run_device(ctx, out, d_scalars, npoints, nmsms, s);

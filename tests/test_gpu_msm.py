@@ -279,3 +279,21 @@ def test_autotuned_paths_match_oracle(gb, orc):
         assert any(k.startswith("msm:") for k in rep) and any(k.startswith("ntt:") for k in rep)
     finally:
         gb.autotune_set(False)
+
+
+def test_context_batch_pinned_host_scalars(gb, orc):
+    """Page-locked host scalars are read in place by the device (no staging
+    copy): the results equal the pageable path's and the oracle's."""
+    import torch
+    rng = np.random.default_rng(77)
+    n, m = 1 << 12, 3
+    bases = gb.g1_generator_mul(orc.fr_random(n, rng))
+    scalars = orc.fr_random(n * m, rng).reshape(m, n, 4)
+    ctx = gb.Bls12_381G1MsmContext(bases)
+    pinned = torch.empty((m, n, 4), dtype=torch.int64, pin_memory=True)
+    view = pinned.numpy().view(np.uint64)
+    view[:] = scalars
+    got = ctx.batch(view)
+    want = ctx.batch(np.array(scalars))
+    assert (affine_of(orc, got) == affine_of(orc, want)).all()
+    assert (affine_of(orc, got[1:2]) == affine_of(orc, orc.g1_msm(bases, scalars[1])[None])).all()
