@@ -796,10 +796,10 @@ static void u32_exclusive_scan(const uint32_t *in, uint32_t n, uint32_t *out, cu
     GB_CUDA_OK(cudaMemcpyAsync(out + n, sums.get() + tiles, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
 }
 
-// Entries per accumulation thread: about half a bucket (8..64), then lowered
-// so that the chunks fill whole waves of resident accumulation blocks (a
-// 2^16 MSM's 65536 chunks of 16 fill 84 % of one wave on 152 SMs; chunks of
-// 14 fill 96 %).
+// Entries per accumulation thread: about half a bucket (8..64), then set so
+// that the chunks fill whole waves of resident accumulation blocks (a 2^16
+// MSM's 65536 chunks of 16 fill 84 % of one wave on 152 SMs; chunks of 14
+// fill 96 %; a 2^20 MSM's 3.4 waves of 64 become 3 of 72).
 static uint32_t chunk_length(uint64_t digits, double avg, int variant)
 {
     uint32_t L = (uint32_t)std::max(8.0, std::min(64.0, avg * 0.5));
@@ -815,9 +815,11 @@ static uint32_t chunk_length(uint64_t digits, double avg, int variant)
     }
     const uint64_t wave = (uint64_t)sms * (uint64_t)per_sm[v];  // chunks resident at once
     if (!wave || !digits) return L;
-    const uint64_t waves = (digits + (uint64_t)L * wave - 1) / ((uint64_t)L * wave);
+    // whole waves, rounded down (longer chunks: shorter fix-up chains) when
+    // there are several, up when there is less than one
+    const uint64_t waves = std::max<uint64_t>(1, digits / ((uint64_t)L * wave));
     const uint64_t L2 = (digits + waves * wave - 1) / (waves * wave);
-    return L2 >= 8 && L2 < L ? (uint32_t)L2 : L;
+    return L2 >= 8 && L2 <= 2 * (uint64_t)L ? (uint32_t)L2 : L;
 }
 
 // Run a batch of MSMs.  precomputed: `points` is a table of nwin rows of
