@@ -279,6 +279,58 @@ GB_API RustError gb_eval_numerator_device(
     size_t lookup_count, const void *trash_vec, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
     RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *trash_graphs);
 
+/* ---- numerator context (stateful resident quotient) -------------------------- */
+/* bls12_381_g1_msm.cu:5517-5660: the circuit's fixed data resident once.
+ * fixed [fixed_cols][len] extended cosets, fixed_lagrange [fixed_cols][input_len],
+ * l0 / l_last / l_active [len], permutation sigma cosets [pk_len][len] and
+ * Lagrange values [pk_len][input_len], trash selectors (fixed column indices),
+ * the graphs (copied into device memory), omega (extended domain), trace_omega
+ * (input domain), g_coset (the coset shift: delta_start = beta * g_coset). */
+GB_API RustError midnight_sppark_bls12_381_numerator_context_create(
+    void **out, size_t len, size_t input_len, const RawFr *fixed, const RawFr *fixed_lagrange, size_t fixed_cols,
+    const RawFr *l0, const RawFr *l_last, const RawFr *l_active, const RawColumnRef *permutation_columns,
+    size_t permutation_columns_len, const RawFr *permutation_pk_cosets, const RawFr *permutation_pk_lagrange,
+    size_t permutation_pk_cosets_len, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *lookup_input_graphs,
+    const RawGraph *lookup_table_graphs, size_t lookup_count, const RawGraph *trash_graphs, RawFr omega,
+    RawFr trace_omega, RawFr g_coset, RawFr delta_const, int32_t rot_scale, int32_t last_rotation,
+    uint32_t chunk_len);
+/* bls12_381_g1_msm.cu:5662-5665 (drains the device first) */
+GB_API void midnight_sppark_bls12_381_numerator_context_free(void *context);
+/* bls12_381_g1_msm.cu:5968-6162: the numerator over one resident column vector
+ * of total_columns x len values; each group (advice, instance, permutation
+ * products, lookup products / permuted inputs / permuted tables, trash) is a
+ * run of columns at its offset; out = a new device vector of len rows */
+GB_API RustError midnight_sppark_bls12_381_numerator_context_eval(
+    void **out, const void *context, const void *columns, size_t total_columns, size_t advice_offset,
+    size_t advice_cols, size_t instance_offset, size_t instance_cols, const RawFr *challenges, size_t challenge_len,
+    RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, size_t permutation_offset,
+    size_t permutation_sets, size_t lookup_product_offset, size_t lookup_input_offset, size_t lookup_table_offset,
+    size_t lookup_count, size_t trash_offset, size_t trash_count);
+/* bls12_381_g1_msm.cu:5667-5736: trash compressed expressions over the trace
+ * (input_len rows; advice / instance device vectors [cols][input_len]),
+ * out [trash_count][input_len] */
+GB_API RustError midnight_sppark_bls12_381_trace_context_trash(void **out, const void *context, const void *advice,
+                                                               size_t advice_cols, const void *instance,
+                                                               size_t instance_cols, const RawFr *challenges,
+                                                               size_t challenge_len, RawFr trash_challenge);
+/* bls12_381_g1_msm.cu:5738-5847: permutation products over the trace,
+ * out [sets][input_len], sets = ceil(permutation columns / chunk_len);
+ * delta_powers one per column, blind_values [sets][blinding_factors] */
+GB_API RustError midnight_sppark_bls12_381_trace_context_permutation(
+    void **out, const void *context, const void *advice, size_t advice_cols, const void *instance,
+    size_t instance_cols, RawFr beta, RawFr gamma, const RawFr *delta_powers, size_t delta_powers_len,
+    const RawFr *blind_values, size_t blind_values_len, size_t blinding_factors);
+/* bls12_381_g1_msm.cu:5849-5966: compressed lookup inputs and tables over the
+ * trace and their permutations, out [inputs | tables | permuted inputs |
+ * permuted tables], each [lookup_count][input_len] (the layout
+ * midnight_sppark_bls12_381_fr_lookup_products_device reads); blinds
+ * [lookup_count][blind_count], blind_count = input_len - usable_rows */
+GB_API RustError midnight_sppark_bls12_381_trace_context_lookup_permute(
+    void **out, const void *context, const void *advice, size_t advice_cols, const void *instance,
+    size_t instance_cols, const RawFr *challenges, size_t challenge_len, RawFr theta, size_t usable_rows,
+    const RawFr *input_blinds, const RawFr *table_blinds, size_t blind_count);
+
 /* permute_expression_pair (lookup/prover.rs:1573-1690) for lookup_count
  * lookups on the device: compressed_vec = per lookup its compressed input
  * then compressed table column (len rows each); out = a new device vector,

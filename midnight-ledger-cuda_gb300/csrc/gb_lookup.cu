@@ -189,6 +189,34 @@ static void permute_pair(const fr_t *a, const fr_t *t, size_t u, fr_t *a_out, fr
     GB_CHECK_LAUNCH();
 }
 
+const char *lookup_permute_core(const fr_t *inputs, const fr_t *tables, size_t in_stride, fr_t *a_out, fr_t *s_out,
+                                size_t out_stride, size_t len, size_t usable_rows, size_t lookup_count,
+                                const RawFr *input_blinds, const RawFr *table_blinds, cudaStream_t s)
+{
+    const size_t nb = len - usable_rows;
+    int flags[3] = {0, 0, 0};
+    dev_buf<int> d_flags(3, s);
+    // sorted by the top limb first; on a tie of distinct values, again with
+    // the whole canonical key
+    for (int full = 0; full < 2; full++) {
+        GB_CUDA_OK(cudaMemsetAsync(d_flags.get(), 0, 3 * sizeof(int), s));
+        for (size_t l = 0; l < lookup_count; l++) {
+            fr_t *ao = a_out + l * out_stride, *so = s_out + l * out_stride;
+            permute_pair(inputs + l * in_stride, tables + l * in_stride, usable_rows, ao, so, d_flags, full != 0, s);
+            if (full == 0 && nb) {
+                h2d(ao + usable_rows, input_blinds + l * nb, nb * sizeof(fr_t), s);
+                h2d(so + usable_rows, table_blinds + l * nb, nb * sizeof(fr_t), s);
+            }
+        }
+        d2h(flags, d_flags, 3 * sizeof(int), s);
+        GB_CUDA_OK(cudaStreamSynchronize(s));
+        if (!flags[2]) break;
+    }
+    if (flags[0]) return "lookup input value missing from the table";
+    if (flags[1]) return "lookup table/input multiset mismatch";
+    return nullptr;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -212,37 +240,19 @@ RustError gb_fr_lookup_permute_device(void **out, const void *compressed_vec, si
         return make_error((int)cudaErrorInvalidValue, "compressed lookup columns too short");
     cudaStream_t s = lane_stream();
     device_vec_wait(cv, s);
-    const size_t nb = len - usable_rows;
     fr_device_vec *v = device_vec_new(2 * lookup_count * len, s);
-    int flags[3] = {0, 0, 0};
+    const char *failed = nullptr;
     try {
-        dev_buf<int> d_flags(3, s);
-        // sorted by the top limb first; on a tie of distinct values, again
-        // with the whole canonical key
-        for (int full = 0; full < 2; full++) {
-            GB_CUDA_OK(cudaMemsetAsync(d_flags.get(), 0, 3 * sizeof(int), s));
-            for (size_t l = 0; l < lookup_count; l++) {
-                const fr_t *a = cv->values + 2 * l * len, *t = a + len;
-                fr_t *a_out = v->values + 2 * l * len, *s_out = a_out + len;
-                permute_pair(a, t, usable_rows, a_out, s_out, d_flags, full != 0, s);
-                if (full == 0) {
-                    h2d(a_out + usable_rows, input_blinds + l * nb, nb * sizeof(fr_t), s);
-                    h2d(s_out + usable_rows, table_blinds + l * nb, nb * sizeof(fr_t), s);
-                }
-            }
-            d2h(flags, d_flags, 3 * sizeof(int), s);
-            GB_CUDA_OK(cudaStreamSynchronize(s));
-            if (!flags[2]) break;
-        }
+        failed = lookup_permute_core(cv->values, cv->values + len, 2 * len, v->values, v->values + len, 2 * len, len,
+                                     usable_rows, lookup_count, input_blinds, table_blinds, s);
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
         throw;
     }
-    if (flags[0] || flags[1]) {
+    if (failed) {
         device_vec_delete(v);
-        return make_error((int)cudaErrorInvalidValue,
-                          flags[0] ? "lookup input value missing from the table" : "lookup table/input multiset mismatch");
+        return make_error((int)cudaErrorInvalidValue, failed);
     }
     *out = v;
     return ok();

@@ -9,6 +9,7 @@
 // list (uniform control flow, broadcast loads), with its intermediates in a
 // per-thread local array sized to the graph.
 #include <algorithm>
+#include <memory>
 #include <vector>
 
 #include "gb_vec.cuh"
@@ -309,6 +310,32 @@ static dev_buf<fr_t> upload_fr(const RawFr *h, size_t n, cudaStream_t s)
 }
 
 
+// one launch per graph, graph gi (device-resident, its descriptor on the
+// host) into d_out + gi * p.len; p carries the columns and challenges
+static void graph_batch_launch(fr_t *d_out, num_params p, const dgraph *graphs, size_t graph_count, cudaStream_t s)
+{
+    const unsigned grid = blocks_for(p.len, 128);
+    for (size_t gi = 0; gi < graph_count; gi++) {
+        p.custom = graphs[gi];
+        fr_t *o = d_out + gi * p.len;
+        launch_by_capacity(
+            capacity_for(graphs[gi].ninter), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
+            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
+        GB_CHECK_LAUNCH();
+    }
+}
+
+// the numerator kernel sized for max_inter intermediates per row
+static void numerator_launch(const num_params &p, uint32_t max_inter, cudaStream_t s)
+{
+    const unsigned grid = blocks_for(p.len, 128);
+    launch_by_capacity(
+        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
+        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
+    GB_CHECK_LAUNCH();
+}
+
 // graph_count graphs over device columns into d_out [graph_count][len];
 // challenges are a host array
 static void graph_batch_core(fr_t *d_out, size_t len, const fr_t *fixed, size_t fixed_cols, const fr_t *advice,
@@ -334,17 +361,12 @@ static void graph_batch_core(fr_t *d_out, size_t len, const fr_t *fixed, size_t 
     p.trash = from_raw(trash_challenge);
     p.y = from_raw(y);
     std::vector<graph_upload> up(graph_count);
-    const unsigned grid = blocks_for(len, 128);
+    std::vector<dgraph> dg(graph_count);
     for (size_t gi = 0; gi < graph_count; gi++) {
         upload_graph(up[gi], graphs[gi], s);
-        p.custom = up[gi].g;
-        fr_t *o = d_out + gi * len;
-        launch_by_capacity(
-            capacity_for(graphs[gi].num_intermediates), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
-        GB_CHECK_LAUNCH();
+        dg[gi] = up[gi].g;
     }
+    graph_batch_launch(d_out, p, dg.data(), graph_count, s);
 }
 
 // Device pointers of one numerator evaluation; graphs still in host memory.
@@ -438,13 +460,86 @@ static void numerator_core(fr_t *d_out, const numerator_inputs &in, RawFr beta, 
     p.trash_cosets = in.trash_cosets;
     p.trash_sel = d_tsel;
     p.trash_graphs = d_trg;
-    const unsigned grid = blocks_for(len, 128);
-    launch_by_capacity(
-        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
-        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
-    GB_CHECK_LAUNCH();
+    numerator_launch(p, max_inter, s);
     // the graph and column-reference buffers are released in stream order
     // after the launch; the caller's stream keeps the kernel ahead of them
+}
+
+// Resident numerator state of one circuit (numerator_context_t,
+// bls12_381_g1_msm.cu:1116 and :5517-5660): the fixed columns as extended
+// cosets and as Lagrange values, l0 / l_last / l_active, the permutation
+// columns with their sigma cosets and Lagrange values, omega^i over the
+// extended domain and every graph uploaded once.  Read-only once created, so
+// calls from several lanes may share it.
+struct numerator_context {
+    cudaStream_t owner = nullptr;
+    size_t len = 0, input_len = 0, fixed_cols = 0, perm_columns_len = 0, perm_pk_len = 0;
+    size_t lookup_count = 0, trash_count = 0;
+    int32_t rot_scale = 1, last_rotation = 0;
+    uint32_t chunk_len = 0, max_inter = 0;
+    fr_t g_coset, delta_const, trace_omega;
+    dev_buf<fr_t> fixed, fixed_lagrange, l0, l_last, l_active, pk_cosets, pk_lagrange, omega_pows;
+    std::vector<RawColumnRef> perm_columns;
+    dev_buf<RawColumnRef> d_perm_columns;
+    dev_buf<uint32_t> d_trash_sel;
+    graph_upload custom;
+    std::vector<graph_upload> lookup, lookup_input, lookup_table, trash;
+    std::vector<dgraph> lookup_input_g, lookup_table_g, trash_g;  // descriptors, host copies
+    dev_buf<dgraph> d_lookup, d_trash;
+};
+
+static void upload_graphs(std::vector<graph_upload> &up, std::vector<dgraph> &desc, const RawGraph *graphs, size_t n,
+                          cudaStream_t s)
+{
+    up = std::vector<graph_upload>(n);
+    desc.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        upload_graph(up[i], graphs[i], s);
+        desc[i] = up[i].g;
+    }
+}
+
+// the Lagrange-basis column a permutation column reference names, over the
+// context's input domain; nullptr when out of range
+static const fr_t *lagrange_column(const numerator_context &c, const RawColumnRef &ref, const fr_t *advice,
+                                   size_t advice_cols, const fr_t *instance, size_t instance_cols)
+{
+    const size_t n = c.input_len;
+    if (ref.kind == 0) return ref.index < c.fixed_cols ? c.fixed_lagrange.get() + (size_t)ref.index * n : nullptr;
+    if (ref.kind == 1) return ref.index < advice_cols ? advice + (size_t)ref.index * n : nullptr;
+    if (ref.kind == 2) return ref.index < instance_cols ? instance + (size_t)ref.index * n : nullptr;
+    return nullptr;
+}
+
+// advice / instance device vectors of at least cols * n values
+static const fr_t *trace_values(const void *v, size_t cols, size_t n, cudaStream_t s, const char *what)
+{
+    if (!cols) return nullptr;
+    auto *dv = reinterpret_cast<const fr_device_vec *>(v);
+    if (!dv || dv->len < cols * n) throw cuda_error((int)cudaErrorInvalidValue, what);
+    device_vec_wait(dv, s);
+    return dv->values;
+}
+
+// num_params over the context's Lagrange-basis fixed columns and the trace's
+// advice / instance values (input_len rows, rotations unscaled), with every
+// challenge but the named ones zero
+static num_params trace_params(const numerator_context &c, const fr_t *advice, size_t advice_cols,
+                               const fr_t *instance, size_t instance_cols, const fr_t *d_chal, size_t challenge_len)
+{
+    num_params p{};
+    p.len = c.input_len;
+    p.rot_scale = 1;
+    p.fixed = c.fixed_lagrange;
+    p.fixed_cols = c.fixed_cols;
+    p.advice = advice;
+    p.advice_cols = advice_cols;
+    p.instance = instance;
+    p.instance_cols = instance_cols;
+    p.challenges = d_chal;
+    p.challenge_len = challenge_len;
+    p.beta = p.gamma = p.theta = p.trash = p.y = fr_t::zero();
+    return p;
 }
 
 static const fr_t *vec_values(const void *v, size_t need, const char *what)
@@ -613,6 +708,312 @@ RustError gb_eval_numerator_device(
     } catch (...) {
         device_vec_delete(v);
         throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:5517-5660: the circuit's fixed data resident once,
+// for numerator evaluations and the trace-context calls below.
+RustError midnight_sppark_bls12_381_numerator_context_create(
+    void **out, size_t len, size_t input_len, const RawFr *fixed, const RawFr *fixed_lagrange, size_t fixed_cols,
+    const RawFr *l0, const RawFr *l_last, const RawFr *l_active, const RawColumnRef *permutation_columns,
+    size_t permutation_columns_len, const RawFr *permutation_pk_cosets, const RawFr *permutation_pk_lagrange,
+    size_t permutation_pk_cosets_len, const uint32_t *trash_selector_fixed_indices, size_t trash_count,
+    RawGraph custom_graph, const RawGraph *lookup_graphs, const RawGraph *lookup_input_graphs,
+    const RawGraph *lookup_table_graphs, size_t lookup_count, const RawGraph *trash_graphs, RawFr omega,
+    RawFr trace_omega, RawFr g_coset, RawFr delta_const, int32_t rot_scale, int32_t last_rotation,
+    uint32_t chunk_len)
+{
+    if (!out || len == 0 || input_len == 0 || !l0 || !l_last || !l_active)
+        return make_error((int)cudaErrorInvalidValue, "invalid numerator context arguments");
+    if ((fixed_cols && (!fixed || !fixed_lagrange)) || (permutation_columns_len && !permutation_columns) ||
+        (permutation_pk_cosets_len && (!permutation_pk_cosets || !permutation_pk_lagrange)) ||
+        (lookup_count && (!lookup_graphs || !lookup_input_graphs || !lookup_table_graphs)) ||
+        (trash_count && (!trash_graphs || !trash_selector_fixed_indices)))
+        return make_error((int)cudaErrorInvalidValue, "missing numerator context data");
+    *out = nullptr;
+    if (permutation_pk_cosets_len < permutation_columns_len)
+        return make_error((int)cudaErrorInvalidValue, "fewer permutation cosets than permutation columns");
+    for (size_t i = 0; i < trash_count; i++)
+        if (trash_selector_fixed_indices[i] >= fixed_cols)
+            return make_error((int)cudaErrorInvalidValue, "trash selector is not a fixed column");
+    if (fixed_cols > SIZE_MAX / len || permutation_pk_cosets_len > SIZE_MAX / len)
+        return make_error((int)cudaErrorInvalidValue, "numerator context size overflow");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    auto c = std::make_unique<numerator_context>();
+    c->owner = s;
+    c->len = len;
+    c->input_len = input_len;
+    c->fixed_cols = fixed_cols;
+    c->perm_columns_len = permutation_columns_len;
+    c->perm_pk_len = permutation_pk_cosets_len;
+    c->lookup_count = lookup_count;
+    c->trash_count = trash_count;
+    c->rot_scale = rot_scale;
+    c->last_rotation = last_rotation;
+    c->chunk_len = chunk_len;
+    c->g_coset = from_raw(g_coset);
+    c->delta_const = from_raw(delta_const);
+    c->trace_omega = from_raw(trace_omega);
+    c->fixed = upload_fr(fixed, fixed_cols * len, s);
+    c->fixed_lagrange = upload_fr(fixed_lagrange, fixed_cols * input_len, s);
+    c->l0 = upload_fr(l0, len, s);
+    c->l_last = upload_fr(l_last, len, s);
+    c->l_active = upload_fr(l_active, len, s);
+    c->pk_cosets = upload_fr(permutation_pk_cosets, permutation_pk_cosets_len * len, s);
+    c->pk_lagrange = upload_fr(permutation_pk_lagrange, permutation_pk_cosets_len * input_len, s);
+    c->perm_columns.assign(permutation_columns, permutation_columns + permutation_columns_len);
+    c->d_perm_columns = dev_buf<RawColumnRef>(permutation_columns_len, s);
+    h2d(c->d_perm_columns, permutation_columns, permutation_columns_len * sizeof(RawColumnRef), s);
+    c->d_trash_sel = dev_buf<uint32_t>(trash_count, s);
+    h2d(c->d_trash_sel, trash_selector_fixed_indices, trash_count * sizeof(uint32_t), s);
+    c->omega_pows = dev_buf<fr_t>(len, s);
+    omega_powers(c->omega_pows, from_raw(omega), len, s);
+    upload_graph(c->custom, custom_graph, s);
+    c->max_inter = custom_graph.num_intermediates;
+    std::vector<dgraph> lookup_g;
+    upload_graphs(c->lookup, lookup_g, lookup_graphs, lookup_count, s);
+    upload_graphs(c->lookup_input, c->lookup_input_g, lookup_input_graphs, lookup_count, s);
+    upload_graphs(c->lookup_table, c->lookup_table_g, lookup_table_graphs, lookup_count, s);
+    upload_graphs(c->trash, c->trash_g, trash_graphs, trash_count, s);
+    for (const dgraph &g : lookup_g) c->max_inter = std::max(c->max_inter, g.ninter);
+    for (const dgraph &g : c->trash_g) c->max_inter = std::max(c->max_inter, g.ninter);
+    if (!capacity_for(c->max_inter))
+        return make_error((int)cudaErrorInvalidValue, "graph needs more than 256 intermediates");
+    c->d_lookup = dev_buf<dgraph>(lookup_count, s);
+    h2d(c->d_lookup, lookup_g.data(), lookup_count * sizeof(dgraph), s);
+    c->d_trash = dev_buf<dgraph>(trash_count, s);
+    h2d(c->d_trash, c->trash_g.data(), trash_count * sizeof(dgraph), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    *out = c.release();
+    return ok();
+    GB_ENTRY_END
+}
+
+// Evaluations issued on any lane may still read the context: the whole
+// device is drained before its buffers go.
+void midnight_sppark_bls12_381_numerator_context_free(void *context)
+{
+    auto *c = reinterpret_cast<numerator_context *>(context);
+    if (!c) return;
+    cudaDeviceSynchronize();
+    delete c;
+}
+
+// bls12_381_g1_msm.cu:5968-6162: the numerator over one resident column
+// vector (each group of columns a run of len-row columns at its offset),
+// into a new device vector of len rows.
+RustError midnight_sppark_bls12_381_numerator_context_eval(
+    void **out, const void *raw_context, const void *raw_columns, size_t total_columns, size_t advice_offset,
+    size_t advice_cols, size_t instance_offset, size_t instance_cols, const RawFr *challenges, size_t challenge_len,
+    RawFr beta, RawFr gamma, RawFr theta, RawFr trash_challenge, RawFr y, size_t permutation_offset,
+    size_t permutation_sets, size_t lookup_product_offset, size_t lookup_input_offset, size_t lookup_table_offset,
+    size_t lookup_count, size_t trash_offset, size_t trash_count)
+{
+    if (!out || !raw_context || (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid numerator evaluation arguments");
+    *out = nullptr;
+    const auto *c = reinterpret_cast<const numerator_context *>(raw_context);
+    const auto *cols = reinterpret_cast<const fr_device_vec *>(raw_columns);
+    const size_t len = c->len;
+    auto in_bounds = [total_columns](size_t offset, size_t count) {
+        return offset <= total_columns && count <= total_columns - offset;
+    };
+    if (lookup_count != c->lookup_count || trash_count != c->trash_count || total_columns > SIZE_MAX / len ||
+        !cols || cols->len < total_columns * len || !in_bounds(advice_offset, advice_cols) ||
+        !in_bounds(instance_offset, instance_cols) || !in_bounds(permutation_offset, permutation_sets) ||
+        !in_bounds(lookup_product_offset, lookup_count) || !in_bounds(lookup_input_offset, lookup_count) ||
+        !in_bounds(lookup_table_offset, lookup_count) || !in_bounds(trash_offset, trash_count))
+        return make_error((int)cudaErrorInvalidValue, "resident numerator vector length mismatch");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    device_vec_wait(cols, s);
+    auto view = [cols, len](size_t offset, size_t count) -> const fr_t * {
+        return count ? cols->values + offset * len : nullptr;
+    };
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    num_params p{};
+    p.len = len;
+    p.rot_scale = c->rot_scale;
+    p.fixed = c->fixed;
+    p.fixed_cols = c->fixed_cols;
+    p.advice = view(advice_offset, advice_cols);
+    p.advice_cols = advice_cols;
+    p.instance = view(instance_offset, instance_cols);
+    p.instance_cols = instance_cols;
+    p.challenges = d_chal;
+    p.challenge_len = challenge_len;
+    p.beta = from_raw(beta);
+    p.gamma = from_raw(gamma);
+    p.theta = from_raw(theta);
+    p.trash = from_raw(trash_challenge);
+    p.y = from_raw(y);
+    p.run_custom = 1;
+    p.custom = c->custom.g;
+    p.l0 = c->l0;
+    p.l_last = c->l_last;
+    p.l_active = c->l_active;
+    p.perm_sets = permutation_sets;
+    p.perm_products = view(permutation_offset, permutation_sets);
+    p.perm_columns = c->d_perm_columns;
+    p.perm_columns_len = c->perm_columns_len;
+    p.perm_pk_cosets = c->pk_cosets;
+    p.omega_powers = c->omega_pows;
+    p.delta_start = p.beta * c->g_coset;
+    p.delta_const = c->delta_const;
+    p.last_rotation = c->last_rotation;
+    p.chunk_len = c->chunk_len;
+    p.lookup_count = lookup_count;
+    p.lk_product = view(lookup_product_offset, lookup_count);
+    p.lk_input = view(lookup_input_offset, lookup_count);
+    p.lk_table = view(lookup_table_offset, lookup_count);
+    p.lk_stride = len;
+    p.lookup_graphs = c->d_lookup;
+    p.trash_count = trash_count;
+    p.trash_cosets = view(trash_offset, trash_count);
+    p.trash_sel = c->d_trash_sel;
+    p.trash_graphs = c->d_trash;
+    fr_device_vec *v = device_vec_new(len, s);
+    try {
+        p.out = v->values;
+        numerator_launch(p, c->max_inter, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:5667-5736: every trash argument's compressed
+// expression over the trace (input_len rows), out [trash_count][input_len]
+RustError midnight_sppark_bls12_381_trace_context_trash(void **out, const void *raw_context, const void *raw_advice,
+                                                        size_t advice_cols, const void *raw_instance,
+                                                        size_t instance_cols, const RawFr *challenges,
+                                                        size_t challenge_len, RawFr trash_challenge)
+{
+    if (!out || !raw_context || (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid resident trash arguments");
+    *out = nullptr;
+    const auto *c = reinterpret_cast<const numerator_context *>(raw_context);
+    const size_t n = c->input_len;
+    if (c->trash_count == 0) return make_error((int)cudaErrorInvalidValue, "resident trash vector length mismatch");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    const fr_t *advice = trace_values(raw_advice, advice_cols, n, s, "resident trash vector length mismatch");
+    const fr_t *instance = trace_values(raw_instance, instance_cols, n, s, "resident trash vector length mismatch");
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    num_params p = trace_params(*c, advice, advice_cols, instance, instance_cols, d_chal, challenge_len);
+    p.trash = from_raw(trash_challenge);
+    fr_device_vec *v = device_vec_new(c->trash_count * n, s);
+    try {
+        graph_batch_launch(v->values, p, c->trash_g.data(), c->trash_count, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:5738-5847: z of every permutation set over the trace,
+// out [sets][input_len]; the columns are the context's permutation column
+// references into its fixed Lagrange values and the given advice / instance
+RustError midnight_sppark_bls12_381_trace_context_permutation(
+    void **out, const void *raw_context, const void *raw_advice, size_t advice_cols, const void *raw_instance,
+    size_t instance_cols, RawFr beta, RawFr gamma, const RawFr *delta_powers, size_t delta_powers_len,
+    const RawFr *blind_values, size_t blind_values_len, size_t blinding_factors)
+{
+    if (!out || !raw_context || !delta_powers)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident permutation arguments");
+    *out = nullptr;
+    const auto *c = reinterpret_cast<const numerator_context *>(raw_context);
+    const size_t n = c->input_len, cc = c->perm_columns_len, chunk = c->chunk_len;
+    if (cc == 0 || chunk == 0 || delta_powers_len != cc)
+        return make_error((int)cudaErrorInvalidValue, "resident permutation vector length mismatch");
+    const size_t sets = (cc + chunk - 1) / chunk;
+    if (blinding_factors >= n || blind_values_len != sets * blinding_factors || (blind_values_len && !blind_values))
+        return make_error((int)cudaErrorInvalidValue, "resident permutation blind mismatch");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    const char *what = "resident permutation vector length mismatch";
+    const fr_t *advice = trace_values(raw_advice, advice_cols, n, s, what);
+    const fr_t *instance = trace_values(raw_instance, instance_cols, n, s, what);
+    std::vector<const fr_t *> ptrs(cc);
+    for (size_t i = 0; i < cc; i++) {
+        ptrs[i] = lagrange_column(*c, c->perm_columns[i], advice, advice_cols, instance, instance_cols);
+        if (!ptrs[i]) return make_error((int)cudaErrorInvalidValue, "permutation column out of range");
+    }
+    dev_buf<const fr_t *> d_ptrs(cc, s);
+    h2d(d_ptrs, ptrs.data(), cc * sizeof(const fr_t *), s);
+    auto dd = upload_fr(delta_powers, cc, s);
+    auto db = upload_fr(blind_values, blind_values_len, s);
+    fr_device_vec *v = device_vec_new(sets * n, s);
+    try {
+        permutation_products(v->values, nullptr, d_ptrs, c->pk_lagrange, n, cc, chunk, from_raw(beta),
+                             from_raw(gamma), c->trace_omega, dd, db, blinding_factors, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:5849-5966: every lookup's compressed input and table
+// expressions over the trace and their permutations, one device vector
+// [inputs | tables | permuted inputs | permuted tables], each
+// [lookup_count][input_len]; rows usable_rows.. of the permuted columns from
+// the blinds ([lookup_count][blind_count] each)
+RustError midnight_sppark_bls12_381_trace_context_lookup_permute(
+    void **out, const void *raw_context, const void *raw_advice, size_t advice_cols, const void *raw_instance,
+    size_t instance_cols, const RawFr *challenges, size_t challenge_len, RawFr theta, size_t usable_rows,
+    const RawFr *input_blinds, const RawFr *table_blinds, size_t blind_count)
+{
+    if (!out || !raw_context || (challenge_len && !challenges))
+        return make_error((int)cudaErrorInvalidValue, "invalid resident lookup permutation arguments");
+    *out = nullptr;
+    const auto *c = reinterpret_cast<const numerator_context *>(raw_context);
+    const size_t n = c->input_len, lc = c->lookup_count;
+    if (lc == 0 || usable_rows == 0 || usable_rows > n || blind_count != n - usable_rows ||
+        (blind_count && (!input_blinds || !table_blinds)))
+        return make_error((int)cudaErrorInvalidValue, "resident lookup permutation shape mismatch");
+    if (n > ((size_t)1 << 31) || lc > SIZE_MAX / n || lc * n > SIZE_MAX / 4)
+        return make_error((int)cudaErrorInvalidValue, "resident lookup permutation size overflow");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    const char *what = "resident lookup permutation shape mismatch";
+    const fr_t *advice = trace_values(raw_advice, advice_cols, n, s, what);
+    const fr_t *instance = trace_values(raw_instance, instance_cols, n, s, what);
+    auto d_chal = upload_fr(challenges, challenge_len, s);
+    num_params p = trace_params(*c, advice, advice_cols, instance, instance_cols, d_chal, challenge_len);
+    p.theta = from_raw(theta);
+    const size_t group = lc * n;
+    fr_device_vec *v = device_vec_new(4 * group, s);
+    const char *failed = nullptr;
+    try {
+        fr_t *t = v->values;
+        graph_batch_launch(t, p, c->lookup_input_g.data(), lc, s);
+        graph_batch_launch(t + group, p, c->lookup_table_g.data(), lc, s);
+        failed = lookup_permute_core(t, t + group, n, t + 2 * group, t + 3 * group, n, n, usable_rows, lc,
+                                     input_blinds, table_blinds, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    if (failed) {
+        device_vec_delete(v);
+        return make_error((int)cudaErrorInvalidValue, failed);
     }
     *out = v;
     return ok();

@@ -358,11 +358,12 @@ __global__ void copy_one_kernel(fr_t *dst, const fr_t *src) { *dst = *src; }
 __global__ void set_scalar_kernel(fr_t *dst, fr_t v) { *dst = v; }
 
 // Permutation fraction numerator / denominator per row (prover.rs:392-460):
-// num = prod_j (v_j + delta^j w^i beta + gamma), den = prod_j (v_j + beta s_j + gamma)
-__global__ void perm_num_den_kernel(const fr_t *__restrict__ columns, const fr_t *__restrict__ perms,
-                                    const fr_t *__restrict__ delta_powers, fr_t omega, fr_t beta, fr_t gamma,
-                                    size_t len, size_t c0, size_t ncols, fr_t *__restrict__ num,
-                                    fr_t *__restrict__ den)
+// num = prod_j (v_j + delta^j w^i beta + gamma), den = prod_j (v_j + beta s_j + gamma).
+// Column c is columns[c * len ..] or, with a pointer table, col_ptrs[c][..].
+__global__ void perm_num_den_kernel(const fr_t *__restrict__ columns, const fr_t *const *__restrict__ col_ptrs,
+                                    const fr_t *__restrict__ perms, const fr_t *__restrict__ delta_powers,
+                                    fr_t omega, fr_t beta, fr_t gamma, size_t len, size_t c0, size_t ncols,
+                                    fr_t *__restrict__ num, fr_t *__restrict__ den)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= len) return;
@@ -371,7 +372,7 @@ __global__ void perm_num_den_kernel(const fr_t *__restrict__ columns, const fr_t
     fr_t nn = fr_t::one(), dd = fr_t::one();
     for (size_t j = 0; j < ncols; j++) {
         size_t c = c0 + j;
-        fr_t v = columns[c * len + i];
+        fr_t v = col_ptrs ? col_ptrs[c][i] : columns[c * len + i];
         nn = nn * (v + delta_powers[c] * bw + gamma);
         dd = dd * (v + beta * perms[c * len + i] + gamma);
     }
@@ -402,9 +403,9 @@ static void grand_product(fr_t *out, fr_t *num, fr_t *den, size_t len, const fr_
     GB_CHECK_LAUNCH();
 }
 
-void permutation_products(fr_t *out, const fr_t *d_columns, const fr_t *d_perms, size_t len, size_t column_count,
-                          size_t chunk_len, const fr_t &beta, const fr_t &gamma, const fr_t &omega,
-                          const fr_t *d_delta, const fr_t *d_blinds, size_t bf, cudaStream_t s)
+void permutation_products(fr_t *out, const fr_t *d_columns, const fr_t *const *d_col_ptrs, const fr_t *d_perms,
+                          size_t len, size_t column_count, size_t chunk_len, const fr_t &beta, const fr_t &gamma,
+                          const fr_t &omega, const fr_t *d_delta, const fr_t *d_blinds, size_t bf, cudaStream_t s)
 {
     const size_t sets = (column_count + chunk_len - 1) / chunk_len;
     dev_buf<fr_t> num(len, s), den(len, s), scratch(len, s), init(1, s);
@@ -414,8 +415,8 @@ void permutation_products(fr_t *out, const fr_t *d_columns, const fr_t *d_perms,
         size_t c0 = set * chunk_len;
         size_t nc = std::min(chunk_len, column_count - c0);
         fr_t *z = out + set * len;
-        perm_num_den_kernel<<<blocks_for(len, 256), 256, 0, s>>>(d_columns, d_perms, d_delta, omega, beta, gamma,
-                                                                 len, c0, nc, num, den);
+        perm_num_den_kernel<<<blocks_for(len, 256), 256, 0, s>>>(d_columns, d_col_ptrs, d_perms, d_delta, omega, beta,
+                                                                 gamma, len, c0, nc, num, den);
         GB_CHECK_LAUNCH();
         grand_product(z, num, den, len, init, scratch, s);
         // next set starts from this set's last unblinded value
@@ -693,7 +694,7 @@ RustError midnight_sppark_bls12_381_fr_permutation_products(void **out, const Ra
     auto db = upload(blind_values, sets * blinding_factors, s);
     fr_device_vec *v = device_vec_new(sets * len, s);
     try {
-        permutation_products(v->values, dc, dp, len, column_count, chunk_len, beta, gamma, omega, dd, db,
+        permutation_products(v->values, dc, nullptr, dp, len, column_count, chunk_len, beta, gamma, omega, dd, db,
                              blinding_factors, s);
         device_vec_mark_ready(v, s);
         GB_CUDA_OK(cudaStreamSynchronize(s));
@@ -734,8 +735,9 @@ RustError gb_fr_permutation_products_device(void **out, const void *columns_vec,
     auto db = upload(blind_values, sets * blinding_factors, s);
     fr_device_vec *v = device_vec_new(sets * len, s);
     try {
-        permutation_products(v->values, cv->values, pv->values, len, column_count, chunk_len, gb::from_raw(beta_raw),
-                             gb::from_raw(gamma_raw), gb::from_raw(omega_raw), dd, db, blinding_factors, s);
+        permutation_products(v->values, cv->values, nullptr, pv->values, len, column_count, chunk_len,
+                             gb::from_raw(beta_raw), gb::from_raw(gamma_raw), gb::from_raw(omega_raw), dd, db,
+                             blinding_factors, s);
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);

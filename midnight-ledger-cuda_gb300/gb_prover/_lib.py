@@ -141,6 +141,17 @@ def _declare(L):
         "gb_fr_random_chacha20": (E, [vp, vp, ctypes.c_uint64, sz, vp]),
         "gb_chacha20_blocks": (E, [vp, ctypes.c_uint64, ctypes.c_uint64, sz, vp]),
         "gb_fr_lookup_permute_device": (E, [vp, vp, sz, sz, sz, vp, vp]),
+        "midnight_sppark_bls12_381_numerator_context_create": (E, [
+            vp, sz, sz, vp, vp, sz, vp, vp, vp, vp, sz, vp, vp, sz, vp, sz, RawGraph, vp, vp, vp, sz, vp,
+            fr, fr, fr, fr, i32, i32, u32]),
+        "midnight_sppark_bls12_381_numerator_context_free": (None, [vp]),
+        "midnight_sppark_bls12_381_numerator_context_eval": (E, [
+            vp, vp, vp, sz, sz, sz, sz, sz, vp, sz, fr, fr, fr, fr, fr, sz, sz, sz, sz, sz, sz, sz, sz]),
+        "midnight_sppark_bls12_381_trace_context_trash": (E, [vp, vp, vp, sz, vp, sz, vp, sz, fr]),
+        "midnight_sppark_bls12_381_trace_context_permutation": (E, [
+            vp, vp, vp, sz, vp, sz, fr, fr, vp, sz, vp, sz, sz]),
+        "midnight_sppark_bls12_381_trace_context_lookup_permute": (E, [
+            vp, vp, vp, sz, vp, sz, vp, sz, fr, sz, vp, vp, sz]),
         "gb_autotune_set": (None, [ctypes.c_int]),
         "gb_ntt_variant_set": (None, [ctypes.c_int]),
         "gb_ntt_wait_timeouts": (E, [ctypes.POINTER(ctypes.c_uint32)]),

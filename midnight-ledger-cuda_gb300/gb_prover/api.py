@@ -25,7 +25,7 @@ __all__ = [
     "PROFILE_MSM_FIXUP", "PROFILE_MSM_REDUCE", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_eval_many", "fr_device_kate_divide",
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
-    "fr_lookup_permute_device", "autotune_set", "autotune_reset", "autotune_report",
+    "fr_lookup_permute_device", "NumeratorContext", "autotune_set", "autotune_reset", "autotune_report",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -611,6 +611,98 @@ def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, inpu
     check(lib().gb_fr_lookup_permute_device(ctypes.byref(h), compressed.raw, length, usable_rows, lookup_count,
                                             _ptr(ib), _ptr(tb)))
     return Bls12_381FrDeviceVec(h)
+
+
+class NumeratorContext:
+    """midnight_sppark_bls12_381_numerator_context_{create,eval,free} and the
+    trace-context calls on it (bls12_381_g1_msm.cu:5517-6162).  Host arrays
+    are Montgomery Fr rows ([rows][4] uint64), column groups laid out
+    [column][rows]: extended-coset data has `length` rows, Lagrange-basis
+    (trace) data `input_len` rows.  The graphs are copied into device memory
+    at creation."""
+
+    def __init__(self, length, input_len, custom_graph, fixed=None, fixed_lagrange=None, fixed_cols=0, l0=None,
+                 l_last=None, l_active=None, permutation_columns=(), permutation_pk_cosets=None,
+                 permutation_pk_lagrange=None, permutation_pk_count=0, trash_selectors=(), lookup_graphs=(),
+                 lookup_input_graphs=(), lookup_table_graphs=(), trash_graphs=(), omega=None, trace_omega=None,
+                 g_coset=None, delta_const=None, rot_scale=1, last_rotation=-1, chunk_len=1):
+        from .graph import column_refs, graph_array
+        z = np.zeros(4, dtype=np.uint64)
+        arr = lambda v: None if v is None else _fr_arr(v)  # noqa: E731
+        f = lambda v: _fr(z if v is None else v)  # noqa: E731
+        fx, fl, pk, pl = arr(fixed), arr(fixed_lagrange), arr(permutation_pk_cosets), arr(permutation_pk_lagrange)
+        lag = [arr(x) for x in (l0, l_last, l_active)]
+        pcols = column_refs(list(permutation_columns))
+        tr_s = np.array(list(trash_selectors) or [0], dtype=np.uint32)
+        lk, lki, lkt, tr = (graph_array(list(g)) for g in (lookup_graphs, lookup_input_graphs, lookup_table_graphs,
+                                                            trash_graphs))
+        self.length, self.input_len = length, input_len
+        self._h = ctypes.c_void_p()
+        vp = lambda a: ctypes.cast(a, ctypes.c_void_p)  # noqa: E731
+        check(lib().midnight_sppark_bls12_381_numerator_context_create(
+            ctypes.byref(self._h), length, input_len, _ptr(fx), _ptr(fl), fixed_cols, _ptr(lag[0]), _ptr(lag[1]),
+            _ptr(lag[2]), vp(pcols), len(permutation_columns), _ptr(pk), _ptr(pl), permutation_pk_count,
+            _ptr(tr_s) if len(trash_selectors) else None, len(trash_selectors), custom_graph.raw(), vp(lk), vp(lki),
+            vp(lkt), len(lookup_graphs), vp(tr), f(omega), f(trace_omega), f(g_coset), f(delta_const), rot_scale,
+            last_rotation, chunk_len))
+
+    def eval(self, columns, total_columns, advice_offset=0, advice_cols=0, instance_offset=0, instance_cols=0,
+             challenges=None, beta=None, gamma=None, theta=None, trash_challenge=None, y=None, permutation_offset=0,
+             permutation_sets=0, lookup_product_offset=0, lookup_input_offset=0, lookup_table_offset=0,
+             lookup_count=0, trash_offset=0, trash_count=0):
+        """The numerator over one Bls12_381FrDeviceVec of total_columns x length
+        values; a new device vector of length rows."""
+        z = np.zeros(4, dtype=np.uint64)
+        f = lambda v: _fr(z if v is None else v)  # noqa: E731
+        ch = None if challenges is None else _fr_arr(challenges)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_numerator_context_eval(
+            ctypes.byref(h), self._h, columns.raw, total_columns, advice_offset, advice_cols, instance_offset,
+            instance_cols, _ptr(ch), 0 if ch is None else len(ch), f(beta), f(gamma), f(theta), f(trash_challenge),
+            f(y), permutation_offset, permutation_sets, lookup_product_offset, lookup_input_offset,
+            lookup_table_offset, lookup_count, trash_offset, trash_count))
+        return Bls12_381FrDeviceVec(h)
+
+    def trace_trash(self, advice, advice_cols, instance, instance_cols, challenges, trash_challenge):
+        ch = None if challenges is None else _fr_arr(challenges)
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_trace_context_trash(
+            ctypes.byref(h), self._h, _raw(advice), advice_cols, _raw(instance), instance_cols, _ptr(ch),
+            0 if ch is None else len(ch), _fr(trash_challenge)))
+        return Bls12_381FrDeviceVec(h)
+
+    def trace_permutation(self, advice, advice_cols, instance, instance_cols, beta, gamma, delta_powers,
+                          blind_values, blinding_factors):
+        d = _fr_arr(delta_powers)
+        b = _fr_arr(blind_values) if blind_values is not None and len(blind_values) else None
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_trace_context_permutation(
+            ctypes.byref(h), self._h, _raw(advice), advice_cols, _raw(instance), instance_cols, _fr(beta),
+            _fr(gamma), _ptr(d), len(d), _ptr(b), 0 if b is None else len(b), blinding_factors))
+        return Bls12_381FrDeviceVec(h)
+
+    def trace_lookup_permute(self, advice, advice_cols, instance, instance_cols, challenges, theta, usable_rows,
+                             input_blinds, table_blinds):
+        ch = None if challenges is None else _fr_arr(challenges)
+        nb = self.input_len - usable_rows
+        ib = _fr_arr(input_blinds) if nb else None
+        tb = _fr_arr(table_blinds) if nb else None
+        h = ctypes.c_void_p()
+        check(lib().midnight_sppark_bls12_381_trace_context_lookup_permute(
+            ctypes.byref(h), self._h, _raw(advice), advice_cols, _raw(instance), instance_cols, _ptr(ch),
+            0 if ch is None else len(ch), _fr(theta), usable_rows, _ptr(ib), _ptr(tb), nb))
+        return Bls12_381FrDeviceVec(h)
+
+    def close(self):
+        if self._h:
+            lib().midnight_sppark_bls12_381_numerator_context_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------- autotuner
