@@ -104,6 +104,9 @@ typedef struct {
 } RawGraph;
 /* permutation column: kind 0 fixed, 1 advice, 2 instance (lib.rs:81-86) */
 typedef struct { uint32_t kind; uint32_t index; } RawColumnRef;
+/* resident polynomial: source 0 dynamic, 1 fixed, 2 extra device vector,
+ * index-th polynomial in it (bls12_381_g1_msm.cu:383-386) */
+typedef struct { uint32_t source; uint32_t index; } RawDevicePolyRef;
 
 /* ---- lanes ---------------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:134-146: 0 = shared lane, 1..8 private lanes */
@@ -362,6 +365,42 @@ GB_API RustError gb_fr_random_chacha20(void **out, const uint8_t *key32, uint64_
  * poly_count resident polynomials of poly_len coefficients */
 GB_API RustError midnight_sppark_bls12_381_fr_device_eval_polys(RawFr *out, const void *device_vec, size_t poly_len,
                                                                 size_t poly_count, RawFr point);
+
+/* bls12_381_g1_msm.cu:3600-3721: multi-open preparation over host
+ * polynomials [poly_count][poly_len]: q_out [q_count][poly_len], q k = sum of
+ * q_coefficients[t] * polys[q_poly_indices[t]] for q_offsets[k] <= t <
+ * q_offsets[k+1] (q_count = q_offsets_len - 1); eval_out[r] = polynomial
+ * query_poly_indices[r] at points[query_point_indices[r]] */
+GB_API RustError midnight_sppark_bls12_381_fr_multiopen_prepare(
+    RawFr *q_out, RawFr *eval_out, const RawFr *polys, size_t poly_len, size_t poly_count, const uint32_t *q_offsets,
+    size_t q_offsets_len, const uint32_t *q_poly_indices, const RawFr *q_coefficients, size_t q_items_len,
+    const RawFr *points, size_t point_count, const uint32_t *query_poly_indices, const uint32_t *query_point_indices,
+    size_t query_count);
+/* bls12_381_g1_msm.cu:3723-3871: the same over resident polynomials named by
+ * poly_refs; q_out (host) and *q_device_out (new device vector) optional,
+ * not both absent */
+GB_API RustError midnight_sppark_bls12_381_fr_multiopen_prepare_device(
+    RawFr *q_out, void **q_device_out, RawFr *eval_out, const void *dynamic_source, const void *fixed_source,
+    const void *extra_source, size_t poly_len, const RawDevicePolyRef *poly_refs, size_t poly_count,
+    const uint32_t *q_offsets, size_t q_offsets_len, const uint32_t *q_poly_indices, const RawFr *q_coefficients,
+    size_t q_items_len, const RawFr *points, size_t point_count, const uint32_t *query_poly_indices,
+    const uint32_t *query_point_indices, size_t query_count);
+/* bls12_381_g1_msm.cu:3873-3983: f = sum_k combination_scalars[k] * q_k /
+ * prod (X - points[j]) over q k's points (point_offsets, remainders
+ * dropped); a new device vector of poly_len coefficients */
+GB_API RustError midnight_sppark_bls12_381_fr_multiopen_f_poly_device(void **out, const void *q_device_vec,
+                                                                      size_t poly_len, const uint32_t *point_offsets,
+                                                                      size_t point_offsets_len, const RawFr *points,
+                                                                      size_t point_count,
+                                                                      const RawFr *combination_scalars,
+                                                                      size_t scalar_count);
+/* bls12_381_g1_msm.cu:4025-4118: pi = (sum_k scalars[k] q_k + scalars[last] f)
+ * / (X - point), remainder dropped; a new device vector of poly_len - 1
+ * coefficients */
+GB_API RustError midnight_sppark_bls12_381_fr_multiopen_pi_device(void **out, const void *q_device_vec,
+                                                                  const void *f_device_vec, size_t poly_len,
+                                                                  const RawFr *combination_scalars,
+                                                                  size_t scalar_count, RawFr point);
 
 /* ---- device vectors --------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:2741-3442 */

@@ -8,6 +8,7 @@
 // slice of c_i z^i, a second pass adds the slices.  Kate quotient: with
 // S_k = sum_{j >= k} f_j z^j (an additive suffix scan), q_i = S_{i+1} z^-(i+1)
 // for i < n-1 and q_{n-1} = 0; z = 0 is the shift q_i = f_{i+1}.
+#include <algorithm>
 #include <vector>
 
 #include "gb_vec.cuh"
@@ -86,6 +87,36 @@ __global__ void __launch_bounds__(kEvalThreads) eval_slices_many_kernel(const ev
     if (threadIdx.x == 0) partial[p * slices + sl] = sh[0];
 }
 
+// evaluations of pairs (pair p: coefficients at pairs[p].polys of len
+// values, at the host point points[pairs[p].row]) into d_out; the powers of
+// every point tabulated once
+static void eval_pairs(fr_t *d_out, const std::vector<eval_pair> &pairs, const RawFr *points, size_t npoints,
+                       size_t len, cudaStream_t s)
+{
+    const size_t total = pairs.size();
+    if (!total) return;
+    dev_buf<fr_t> d_points(npoints, s), pw(npoints * len, s);
+    dev_buf<eval_pair> d_pairs(total, s);
+    h2d(d_points, points, npoints * sizeof(fr_t), s);
+    h2d(d_pairs, pairs.data(), total * sizeof(eval_pair), s);
+    if (len <= ((size_t)1 << 24)) {
+        omega_powers_many(pw, d_points, npoints, len, s);
+    } else {
+        for (size_t q = 0; q < npoints; q++) omega_powers(pw.get() + q * len, from_raw(points[q]), len, s);
+    }
+    const uint32_t slices = (uint32_t)((len + kEvalSlice - 1) / kEvalSlice);
+    const size_t chunk = 65535;  // grid.y limit
+    dev_buf<fr_t> partial(std::min(total, chunk) * slices, s);
+    for (size_t b = 0; b < total; b += chunk) {
+        const size_t m = std::min(chunk, total - b);
+        eval_slices_many_kernel<<<dim3(slices, (unsigned)m), kEvalThreads, 0, s>>>(d_pairs.get() + b, len, pw, slices,
+                                                                                   partial);
+        GB_CHECK_LAUNCH();
+        sum_slices_kernel<<<blocks_for(m, 128), 128, 0, s>>>(partial, slices, m, d_out + b);
+        GB_CHECK_LAUNCH();
+    }
+}
+
 // g[p][j] = f[p][j] * z^j
 __global__ void scale_by_powers_kernel(const fr_t *__restrict__ f, const fr_t *__restrict__ pw, size_t len,
                                        size_t total, fr_t *__restrict__ g)
@@ -140,6 +171,74 @@ void kate_divide(fr_t *d_out, const fr_t *f, size_t len, size_t count, const fr_
     GB_CHECK_LAUNCH();
 }
 
+// q[k][i] = sum over the items t of q k (q_offsets[k] <= t < q_offsets[k+1])
+// of coeffs[t] * poly(item_polys[t])[i]; polynomials through a pointer table
+__global__ void multiopen_q_kernel(fr_t *__restrict__ out, const fr_t *const *__restrict__ polys,
+                                   const uint32_t *__restrict__ q_offsets, const uint32_t *__restrict__ item_polys,
+                                   const fr_t *__restrict__ coeffs, size_t len, size_t q_count)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= len * q_count) return;
+    const size_t k = t / len, i = t - k * len;
+    fr_t acc = fr_t::zero();
+    for (uint32_t it = q_offsets[k]; it < q_offsets[k + 1]; it++) acc = acc + polys[item_polys[it]][i] * coeffs[it];
+    out[t] = acc;
+}
+
+// out[i] = sum_p k[p] * polys[p][i], polynomials through a pointer table
+__global__ void lincomb_table_kernel(fr_t *__restrict__ out, const fr_t *const *__restrict__ polys,
+                                     const fr_t *__restrict__ k, size_t len, size_t count)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    fr_t acc = fr_t::zero();
+    for (size_t p = 0; p < count; p++) acc = acc + polys[p][i] * k[p];
+    out[i] = acc;
+}
+
+// checks of the q description shared by both preparation entry points
+static const char *check_q_layout(const uint32_t *q_offsets, size_t q_offsets_len, const uint32_t *q_poly_indices,
+                                  size_t q_items_len, size_t poly_count, const uint32_t *query_poly_indices,
+                                  const uint32_t *query_point_indices, size_t query_count, size_t point_count)
+{
+    const size_t q_count = q_offsets_len - 1;
+    if (q_offsets[0] != 0 || q_offsets[q_count] != q_items_len) return "invalid multi-open q offsets";
+    for (size_t k = 0; k < q_count; k++)
+        if (q_offsets[k] > q_offsets[k + 1]) return "non-monotonic multi-open q offsets";
+    for (size_t t = 0; t < q_items_len; t++)
+        if (q_poly_indices[t] >= poly_count) return "multi-open q polynomial index out of range";
+    for (size_t r = 0; r < query_count; r++)
+        if (query_poly_indices[r] >= poly_count || query_point_indices[r] >= point_count)
+            return "multi-open query index out of range";
+    return nullptr;
+}
+
+// the q polynomials into d_q and the query evaluations into d_eval, the
+// polynomials named by a host table of device pointers
+static void multiopen_prepare_core(fr_t *d_q, fr_t *d_eval, const std::vector<const fr_t *> &polys, size_t len,
+                                   const uint32_t *q_offsets, size_t q_offsets_len, const uint32_t *q_poly_indices,
+                                   const RawFr *q_coefficients, size_t q_items_len, const RawFr *points,
+                                   size_t point_count, const uint32_t *query_poly_indices,
+                                   const uint32_t *query_point_indices, size_t query_count, cudaStream_t s)
+{
+    const size_t q_count = q_offsets_len - 1;
+    dev_buf<const fr_t *> d_polys(polys.size(), s);
+    dev_buf<uint32_t> d_offsets(q_offsets_len, s), d_items(q_items_len, s);
+    dev_buf<fr_t> d_coeffs(q_items_len, s);
+    h2d(d_polys, polys.data(), polys.size() * sizeof(const fr_t *), s);
+    h2d(d_offsets, q_offsets, q_offsets_len * sizeof(uint32_t), s);
+    h2d(d_items, q_poly_indices, q_items_len * sizeof(uint32_t), s);
+    h2d(d_coeffs, q_coefficients, q_items_len * sizeof(fr_t), s);
+    if (q_count) {
+        multiopen_q_kernel<<<blocks_for(len * q_count, 256), 256, 0, s>>>(d_q, d_polys, d_offsets, d_items, d_coeffs,
+                                                                           len, q_count);
+        GB_CHECK_LAUNCH();
+    }
+    std::vector<eval_pair> pairs(query_count);
+    for (size_t r = 0; r < query_count; r++) pairs[r] = eval_pair{polys[query_poly_indices[r]], query_point_indices[r]};
+    eval_pairs(d_eval, pairs, points, point_count, len, s);
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -183,22 +282,11 @@ RustError gb_fr_device_eval_many(RawFr *out_raw, const void *const *vecs, const 
             return make_error((int)cudaErrorInvalidValue, "batched evaluation shape mismatch");
         for (size_t p = 0; p < counts[r]; p++) pairs.push_back(eval_pair{v->values + p * poly_len, (uint32_t)r});
     }
-    if (pairs.size() > 65535) return make_error((int)cudaErrorInvalidValue, "too many batched evaluations");
     cudaStream_t s = lane_stream();
     for (size_t r = 0; r < requests; r++) device_vec_wait(reinterpret_cast<const fr_device_vec *>(vecs[r]), s);
     const size_t total = pairs.size();
-    dev_buf<fr_t> d_points(requests, s), pw(requests * poly_len, s), d_out(total, s);
-    dev_buf<eval_pair> d_pairs(total, s);
-    h2d(d_points, points_raw, requests * sizeof(fr_t), s);
-    h2d(d_pairs, pairs.data(), total * sizeof(eval_pair), s);
-    omega_powers_many(pw, d_points, requests, poly_len, s);
-    const uint32_t slices = (uint32_t)((poly_len + kEvalSlice - 1) / kEvalSlice);
-    dev_buf<fr_t> partial(total * slices, s);
-    eval_slices_many_kernel<<<dim3(slices, (unsigned)total), kEvalThreads, 0, s>>>(d_pairs, poly_len, pw, slices,
-                                                                                 partial);
-    GB_CHECK_LAUNCH();
-    sum_slices_kernel<<<blocks_for(total, 128), 128, 0, s>>>(partial, slices, total, d_out);
-    GB_CHECK_LAUNCH();
+    dev_buf<fr_t> d_out(total, s);
+    eval_pairs(d_out, pairs, points_raw, requests, poly_len, s);
     d2h(out_raw, d_out, total * sizeof(fr_t), s);
     GB_CUDA_OK(cudaStreamSynchronize(s));
     return ok();
@@ -228,6 +316,199 @@ RustError gb_fr_device_kate_divide(void **out, const void *device_vec, size_t po
         throw;
     }
     *out = r;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:3600-3721: host polynomials [poly_count][poly_len];
+// q_out [q_count][poly_len] (q k = the sum of its items' coefficient times
+// polynomial), eval_out[r] = polynomial query_poly_indices[r] at
+// points[query_point_indices[r]]
+RustError midnight_sppark_bls12_381_fr_multiopen_prepare(
+    RawFr *q_out, RawFr *eval_out, const RawFr *polys, size_t poly_len, size_t poly_count, const uint32_t *q_offsets,
+    size_t q_offsets_len, const uint32_t *q_poly_indices, const RawFr *q_coefficients, size_t q_items_len,
+    const RawFr *points, size_t point_count, const uint32_t *query_poly_indices, const uint32_t *query_point_indices,
+    size_t query_count)
+{
+    if (poly_len == 0 || poly_count == 0 || q_offsets_len < 2 || !q_out || !eval_out || !polys || !q_offsets ||
+        !q_poly_indices || !q_coefficients || !points || point_count == 0 || !query_poly_indices ||
+        !query_point_indices)
+        return make_error((int)cudaErrorInvalidValue, "invalid multi-open preparation arguments");
+    if (const char *bad = check_q_layout(q_offsets, q_offsets_len, q_poly_indices, q_items_len, poly_count,
+                                         query_poly_indices, query_point_indices, query_count, point_count))
+        return make_error((int)cudaErrorInvalidValue, bad);
+    const size_t q_count = q_offsets_len - 1;
+    if (poly_count > SIZE_MAX / poly_len || q_count > SIZE_MAX / poly_len || point_count > SIZE_MAX / poly_len)
+        return make_error((int)cudaErrorInvalidValue, "multi-open preparation size overflow");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    dev_buf<fr_t> d_polys(poly_len * poly_count, s), d_q(poly_len * q_count, s), d_eval(query_count, s);
+    h2d(d_polys, polys, poly_len * poly_count * sizeof(fr_t), s);
+    std::vector<const fr_t *> table(poly_count);
+    for (size_t p = 0; p < poly_count; p++) table[p] = d_polys.get() + p * poly_len;
+    multiopen_prepare_core(d_q, d_eval, table, poly_len, q_offsets, q_offsets_len, q_poly_indices, q_coefficients,
+                           q_items_len, points, point_count, query_poly_indices, query_point_indices, query_count, s);
+    d2h(q_out, d_q, poly_len * q_count * sizeof(fr_t), s);
+    d2h(eval_out, d_eval, query_count * sizeof(fr_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:3723-3871: the same over resident polynomials; poly
+// reference p names polynomial index of source 0 (dynamic), 1 (fixed) or 2
+// (extra), each a device vector of whole polynomials.  q_out (host) and
+// q_device_out (a new device vector) are each optional, not both absent.
+RustError midnight_sppark_bls12_381_fr_multiopen_prepare_device(
+    RawFr *q_out, void **q_device_out, RawFr *eval_out, const void *dynamic_source, const void *fixed_source,
+    const void *extra_source, size_t poly_len, const RawDevicePolyRef *poly_refs, size_t poly_count,
+    const uint32_t *q_offsets, size_t q_offsets_len, const uint32_t *q_poly_indices, const RawFr *q_coefficients,
+    size_t q_items_len, const RawFr *points, size_t point_count, const uint32_t *query_poly_indices,
+    const uint32_t *query_point_indices, size_t query_count)
+{
+    if (poly_len == 0 || poly_count == 0 || q_offsets_len < 2 || (!q_out && !q_device_out) || !eval_out ||
+        !dynamic_source || !fixed_source || !extra_source || !poly_refs || !q_offsets || !q_poly_indices ||
+        !q_coefficients || !points || point_count == 0 || !query_poly_indices || !query_point_indices)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident multi-open arguments");
+    if (q_device_out) *q_device_out = nullptr;
+    const fr_device_vec *src[3] = {reinterpret_cast<const fr_device_vec *>(dynamic_source),
+                                   reinterpret_cast<const fr_device_vec *>(fixed_source),
+                                   reinterpret_cast<const fr_device_vec *>(extra_source)};
+    std::vector<const fr_t *> table(poly_count);
+    for (size_t p = 0; p < poly_count; p++) {
+        const RawDevicePolyRef r = poly_refs[p];
+        if (r.source > 2 || (size_t)r.index >= src[r.source]->len / poly_len)
+            return make_error((int)cudaErrorInvalidValue, "resident polynomial reference out of range");
+        table[p] = src[r.source]->values + (size_t)r.index * poly_len;
+    }
+    if (const char *bad = check_q_layout(q_offsets, q_offsets_len, q_poly_indices, q_items_len, poly_count,
+                                         query_poly_indices, query_point_indices, query_count, point_count))
+        return make_error((int)cudaErrorInvalidValue, bad);
+    const size_t q_count = q_offsets_len - 1;
+    if (q_count > SIZE_MAX / poly_len || point_count > SIZE_MAX / poly_len)
+        return make_error((int)cudaErrorInvalidValue, "multi-open preparation size overflow");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    for (const fr_device_vec *v : src) device_vec_wait(v, s);
+    fr_device_vec *q = device_vec_new(poly_len * q_count, s);
+    try {
+        dev_buf<fr_t> d_eval(query_count, s);
+        multiopen_prepare_core(q->values, d_eval, table, poly_len, q_offsets, q_offsets_len, q_poly_indices,
+                               q_coefficients, q_items_len, points, point_count, query_poly_indices,
+                               query_point_indices, query_count, s);
+        device_vec_mark_ready(q, s);
+        if (q_out) d2h(q_out, q->values, poly_len * q_count * sizeof(fr_t), s);
+        d2h(eval_out, d_eval, query_count * sizeof(fr_t), s);
+        GB_CUDA_OK(cudaStreamSynchronize(s));
+    } catch (...) {
+        device_vec_delete(q);
+        throw;
+    }
+    if (q_device_out) *q_device_out = q;
+    else device_vec_delete(q);
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:3873-3983: f = sum_k scalars[k] * floor(q_k / prod_j
+// (X - points[j])) over q k's points (point_offsets[k] <= j <
+// point_offsets[k+1]), one Kate division per point; a new device vector of
+// poly_len coefficients
+RustError midnight_sppark_bls12_381_fr_multiopen_f_poly_device(void **out, const void *q_device_vec, size_t poly_len,
+                                                               const uint32_t *point_offsets,
+                                                               size_t point_offsets_len, const RawFr *points,
+                                                               size_t point_count, const RawFr *combination_scalars,
+                                                               size_t scalar_count)
+{
+    if (!out || !q_device_vec || poly_len < 2 || !point_offsets || point_offsets_len < 2 || !points ||
+        !combination_scalars)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident f-polynomial arguments");
+    *out = nullptr;
+    const size_t q_count = point_offsets_len - 1;
+    auto *qv = reinterpret_cast<const fr_device_vec *>(q_device_vec);
+    if (q_count != scalar_count || q_count > SIZE_MAX / poly_len || qv->len != q_count * poly_len ||
+        point_offsets[0] != 0 || point_offsets[q_count] != point_count)
+        return make_error((int)cudaErrorInvalidValue, "resident f-polynomial shape mismatch");
+    for (size_t k = 0; k < q_count; k++)
+        if (point_offsets[k] > point_offsets[k + 1])
+            return make_error((int)cudaErrorInvalidValue, "non-monotonic f-polynomial point offsets");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    device_vec_wait(qv, s);
+    dev_buf<fr_t> divided(q_count * poly_len, s), work(2 * poly_len, s);
+    std::vector<const fr_t *> table(q_count);
+    for (size_t k = 0; k < q_count; k++) {
+        const fr_t *cur = qv->values + k * poly_len;
+        const uint32_t p0 = point_offsets[k], p1 = point_offsets[k + 1];
+        for (uint32_t j = p0; j < p1; j++) {
+            fr_t *dst = j + 1 == p1 ? divided.get() + k * poly_len : work.get() + ((j - p0) & 1) * poly_len;
+            kate_divide(dst, cur, poly_len, 1, from_raw(points[j]), s);
+            cur = dst;
+        }
+        table[k] = cur;
+    }
+    dev_buf<const fr_t *> d_table(q_count, s);
+    h2d(d_table, table.data(), q_count * sizeof(const fr_t *), s);
+    dev_buf<fr_t> d_scalars(scalar_count, s);
+    h2d(d_scalars, combination_scalars, scalar_count * sizeof(fr_t), s);
+    fr_device_vec *v = device_vec_new(poly_len, s);
+    try {
+        lincomb_table_kernel<<<blocks_for(poly_len, 256), 256, 0, s>>>(v->values, d_table, d_scalars, poly_len,
+                                                                       q_count);
+        GB_CHECK_LAUNCH();
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:4025-4118: pi = floor((sum_k scalars[k] q_k +
+// scalars[q_count] f) / (X - point)), a new device vector of poly_len - 1
+// coefficients (q_count = scalar_count - 1)
+RustError midnight_sppark_bls12_381_fr_multiopen_pi_device(void **out, const void *q_device_vec,
+                                                           const void *f_device_vec, size_t poly_len,
+                                                           const RawFr *combination_scalars, size_t scalar_count,
+                                                           RawFr point)
+{
+    if (!out || !q_device_vec || !f_device_vec || poly_len < 2 || !combination_scalars || scalar_count < 2)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident pi-polynomial arguments");
+    *out = nullptr;
+    const size_t q_count = scalar_count - 1;
+    auto *qv = reinterpret_cast<const fr_device_vec *>(q_device_vec);
+    auto *fv = reinterpret_cast<const fr_device_vec *>(f_device_vec);
+    if (q_count > SIZE_MAX / poly_len || qv->len != q_count * poly_len || fv->len != poly_len)
+        return make_error((int)cudaErrorInvalidValue, "resident pi-polynomial shape mismatch");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    device_vec_wait(qv, s);
+    device_vec_wait(fv, s);
+    std::vector<const fr_t *> table(scalar_count);
+    for (size_t k = 0; k < q_count; k++) table[k] = qv->values + k * poly_len;
+    table[q_count] = fv->values;
+    dev_buf<const fr_t *> d_table(scalar_count, s);
+    h2d(d_table, table.data(), scalar_count * sizeof(const fr_t *), s);
+    dev_buf<fr_t> d_scalars(scalar_count, s), combined(poly_len, s), quotient(poly_len, s);
+    h2d(d_scalars, combination_scalars, scalar_count * sizeof(fr_t), s);
+    lincomb_table_kernel<<<blocks_for(poly_len, 256), 256, 0, s>>>(combined, d_table, d_scalars, poly_len,
+                                                                   scalar_count);
+    GB_CHECK_LAUNCH();
+    // the quotient ignores the constant term, so subtracting the value at
+    // the point (as the reference does first) changes nothing
+    kate_divide(quotient, combined, poly_len, 1, from_raw(point), s);
+    fr_device_vec *v = device_vec_new(poly_len - 1, s);
+    try {
+        GB_CUDA_OK(cudaMemcpyAsync(v->values, quotient.get(), (poly_len - 1) * sizeof(fr_t), cudaMemcpyDeviceToDevice,
+                                   s));
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
     return ok();
     GB_ENTRY_END
 }

@@ -49,6 +49,11 @@ class RawFr(ctypes.Structure):
     _fields_ = [("limbs", ctypes.c_uint64 * 4)]
 
 
+class RawDevicePolyRef(ctypes.Structure):
+    """source 0 dynamic, 1 fixed, 2 extra device vector; index-th polynomial"""
+    _fields_ = [("source", ctypes.c_uint32), ("index", ctypes.c_uint32)]
+
+
 _lib = None
 _libc = ctypes.CDLL(None)
 _libc.free.argtypes = [ctypes.c_void_p]
@@ -145,6 +150,12 @@ def _declare(L):
             vp, sz, sz, vp, vp, sz, vp, vp, vp, vp, sz, vp, vp, sz, vp, sz, RawGraph, vp, vp, vp, sz, vp,
             fr, fr, fr, fr, i32, i32, u32]),
         "midnight_sppark_bls12_381_numerator_context_free": (None, [vp]),
+        "midnight_sppark_bls12_381_fr_multiopen_prepare": (E, [
+            vp, vp, vp, sz, sz, vp, sz, vp, vp, sz, vp, sz, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_multiopen_prepare_device": (E, [
+            vp, vp, vp, vp, vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, sz, vp, vp, sz]),
+        "midnight_sppark_bls12_381_fr_multiopen_f_poly_device": (E, [vp, vp, sz, vp, sz, vp, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_multiopen_pi_device": (E, [vp, vp, vp, sz, vp, sz, fr]),
         "midnight_sppark_bls12_381_numerator_context_eval": (E, [
             vp, vp, vp, sz, sz, sz, sz, sz, vp, sz, fr, fr, fr, fr, fr, sz, sz, sz, sz, sz, sz, sz, sz]),
         "midnight_sppark_bls12_381_trace_context_trash": (E, [vp, vp, vp, sz, vp, sz, vp, sz, fr]),

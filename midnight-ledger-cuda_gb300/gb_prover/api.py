@@ -25,7 +25,9 @@ __all__ = [
     "PROFILE_MSM_FIXUP", "PROFILE_MSM_REDUCE", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_eval_many", "fr_device_kate_divide",
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
-    "fr_lookup_permute_device", "NumeratorContext", "autotune_set", "autotune_reset", "autotune_report",
+    "fr_lookup_permute_device", "NumeratorContext", "bls12_381_fr_multiopen_prepare",
+    "bls12_381_fr_multiopen_prepare_device", "bls12_381_fr_multiopen_f_poly_device",
+    "bls12_381_fr_multiopen_pi_device", "autotune_set", "autotune_reset", "autotune_report",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -610,6 +612,63 @@ def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, inpu
     h = ctypes.c_void_p()
     check(lib().gb_fr_lookup_permute_device(ctypes.byref(h), compressed.raw, length, usable_rows, lookup_count,
                                             _ptr(ib), _ptr(tb)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def bls12_381_fr_multiopen_prepare(polys, poly_len, q_offsets, q_poly_indices, q_coefficients, points,
+                                   query_poly_indices, query_point_indices):
+    """midnight_sppark_bls12_381_fr_multiopen_prepare: host polynomials
+    [poly_count][poly_len]; returns (q [q_count * poly_len], evaluations
+    [query_count])."""
+    p = _fr_arr(polys)
+    qo, qi, qc = _u32(q_offsets), _u32(q_poly_indices), _fr_arr(q_coefficients)
+    pts, rp, rq = _fr_arr(points), _u32(query_poly_indices), _u32(query_point_indices)
+    q = np.zeros(((len(qo) - 1) * poly_len, 4), dtype=np.uint64)
+    ev = np.zeros((max(len(rp), 1), 4), dtype=np.uint64)
+    check(lib().midnight_sppark_bls12_381_fr_multiopen_prepare(
+        _ptr(q), _ptr(ev), _ptr(p), poly_len, len(p) // poly_len, _ptr(qo), len(qo), _ptr(qi), _ptr(qc), len(qi),
+        _ptr(pts), len(pts), _ptr(rp), _ptr(rq), len(rp)))
+    return q, ev[:len(rp)]
+
+
+def bls12_381_fr_multiopen_prepare_device(sources, poly_len, poly_refs, q_offsets, q_poly_indices, q_coefficients,
+                                          points, query_poly_indices, query_point_indices, q_host=True):
+    """..._multiopen_prepare_device: sources = (dynamic, fixed, extra)
+    Bls12_381FrDeviceVec, poly_refs = [(source, index)]; returns (q on the
+    host or None, q as a new device vector, evaluations)."""
+    from ._lib import RawDevicePolyRef
+    refs = (RawDevicePolyRef * max(len(poly_refs), 1))()
+    for i, (src, idx) in enumerate(poly_refs):
+        refs[i] = RawDevicePolyRef(src, idx)
+    qo, qi, qc = _u32(q_offsets), _u32(q_poly_indices), _fr_arr(q_coefficients)
+    pts, rp, rq = _fr_arr(points), _u32(query_poly_indices), _u32(query_point_indices)
+    q = np.zeros(((len(qo) - 1) * poly_len, 4), dtype=np.uint64) if q_host else None
+    ev = np.zeros((max(len(rp), 1), 4), dtype=np.uint64)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_multiopen_prepare_device(
+        _ptr(q), ctypes.byref(h), _ptr(ev), sources[0].raw, sources[1].raw, sources[2].raw, poly_len,
+        ctypes.cast(refs, ctypes.c_void_p), len(poly_refs), _ptr(qo), len(qo), _ptr(qi), _ptr(qc), len(qi),
+        _ptr(pts), len(pts), _ptr(rp), _ptr(rq), len(rp)))
+    return q, Bls12_381FrDeviceVec(h), ev[:len(rp)]
+
+
+def bls12_381_fr_multiopen_f_poly_device(q_vec, poly_len, point_offsets, points, combination_scalars):
+    po, pts, sc = _u32(point_offsets), _fr_arr(points), _fr_arr(combination_scalars)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_multiopen_f_poly_device(
+        ctypes.byref(h), q_vec.raw, poly_len, _ptr(po), len(po), _ptr(pts), len(pts), _ptr(sc), len(sc)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_multiopen_pi_device(q_vec, f_vec, poly_len, combination_scalars, point):
+    sc = _fr_arr(combination_scalars)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_multiopen_pi_device(
+        ctypes.byref(h), q_vec.raw, f_vec.raw, poly_len, _ptr(sc), len(sc), _fr(point)))
     return Bls12_381FrDeviceVec(h)
 
 
