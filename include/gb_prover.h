@@ -334,6 +334,15 @@ GB_API RustError midnight_sppark_bls12_381_trace_context_lookup_permute(
     size_t instance_cols, const RawFr *challenges, size_t challenge_len, RawFr theta, size_t usable_rows,
     const RawFr *input_blinds, const RawFr *table_blinds, size_t blind_count);
 
+/* bls12_381_g1_msm.cu:5139-5194: lookup permutation from host compressed
+ * inputs / tables ([lookup_count][len] each); out = a new device vector
+ * [inputs | tables | permuted inputs | permuted tables], blinds
+ * [lookup_count][blind_count], blind_count = len - usable_rows */
+GB_API RustError midnight_sppark_bls12_381_fr_lookup_permute_batch(void **out, const RawFr *compressed_inputs,
+                                                                   const RawFr *compressed_tables, size_t len,
+                                                                   size_t lookup_count, size_t usable_rows,
+                                                                   const RawFr *input_blinds,
+                                                                   const RawFr *table_blinds, size_t blind_count);
 /* permute_expression_pair (lookup/prover.rs:1573-1690) for lookup_count
  * lookups on the device: compressed_vec = per lookup its compressed input
  * then compressed table column (len rows each); out = a new device vector,
@@ -420,6 +429,22 @@ GB_API RustError midnight_sppark_bls12_381_fr_device_vec_gather_polys(void **out
                                                                       size_t poly_len, const uint32_t *indices,
                                                                       size_t index_count);
 GB_API void midnight_sppark_bls12_381_fr_device_vec_free(void *device_vec);
+/* bls12_381_g1_msm.cu:3101-3179: for count polynomials of poly_len values at
+ * scalar_offset: starts[p] = first nonzero coefficient (poly_len if none),
+ * nonzero_counts[p] (optional) = nonzero coefficients, out = the suffixes
+ * from starts[p] on, packed; *out_len = packed length.  out == NULL with
+ * out_capacity == 0 asks for *out_len only. */
+GB_API RustError midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes(
+    RawFr *out, size_t out_capacity, size_t *out_len, size_t *starts, size_t *nonzero_counts, const void *device_vec,
+    size_t scalar_offset, size_t poly_len, size_t count);
+
+/* ---- test hooks (bls12_381_g1_msm.cu:6379-6423) ---------------------------- */
+/* the next scrambled batches on this thread zero their masked scalars and
+ * hold the stream back delay_ms before the mask is added */
+GB_API void midnight_sppark_test_mask_delay(uint32_t delay_ms);
+/* device_vec *= scale on this lane after holding the lane back delay_ms; the
+ * vector is ready for other lanes only after the scaling */
+GB_API RustError midnight_sppark_test_delayed_scale(void *device_vec, RawFr scale, uint32_t delay_ms);
 
 /* ---- library additions (no reference counterpart) ---------------------------- */
 /* number of Fr elements held by a device vector */

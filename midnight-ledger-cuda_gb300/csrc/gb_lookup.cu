@@ -259,4 +259,47 @@ RustError gb_fr_lookup_permute_device(void **out, const void *compressed_vec, si
     GB_ENTRY_END
 }
 
+// bls12_381_g1_msm.cu:5139-5194: host compressed inputs and tables
+// ([lookup_count][len] each) in, one device vector [inputs | tables |
+// permuted inputs | permuted tables] out (the layout
+// midnight_sppark_bls12_381_fr_lookup_products_device reads); blinds
+// [lookup_count][blind_count], blind_count = len - usable_rows
+RustError midnight_sppark_bls12_381_fr_lookup_permute_batch(void **out, const RawFr *compressed_inputs,
+                                                            const RawFr *compressed_tables, size_t len,
+                                                            size_t lookup_count, size_t usable_rows,
+                                                            const RawFr *input_blinds, const RawFr *table_blinds,
+                                                            size_t blind_count)
+{
+    if (!out || !compressed_inputs || !compressed_tables || !input_blinds || !table_blinds || len == 0 ||
+        lookup_count == 0 || usable_rows == 0 || usable_rows > len || blind_count != len - usable_rows ||
+        usable_rows > UINT32_MAX || lookup_count > SIZE_MAX / len)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident lookup permutation arguments");
+    *out = nullptr;
+    const size_t group = lookup_count * len;
+    if (group > SIZE_MAX / 4 || len > ((size_t)1 << 31))
+        return make_error((int)cudaErrorInvalidValue, "resident lookup permutation size overflow");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    fr_device_vec *v = device_vec_new(4 * group, s);
+    const char *failed = nullptr;
+    try {
+        fr_t *t = v->values;
+        h2d(t, compressed_inputs, group * sizeof(fr_t), s);
+        h2d(t + group, compressed_tables, group * sizeof(fr_t), s);
+        failed = lookup_permute_core(t, t + group, len, t + 2 * group, t + 3 * group, len, len, usable_rows,
+                                     lookup_count, input_blinds, table_blinds, s);
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    if (failed) {
+        device_vec_delete(v);
+        return make_error((int)cudaErrorInvalidValue, failed);
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
 }  // extern "C"

@@ -1351,6 +1351,17 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_ragged(RawG1Projective
     GB_ENTRY_END
 }
 
+// bls12_381_g1_msm.cu:6379-6404 (test hooks): a delay for the next
+// scrambled batches' mask producer on this thread; the masked scalars are
+// zeroed and the stream held back before the mask is added, so that an MSM
+// that did not wait for them would read zeros
+static thread_local uint32_t t_mask_delay_ms = 0;
+
+void midnight_sppark_test_mask_delay(uint32_t delay_ms)
+{
+    t_mask_delay_ms = delay_ms;
+}
+
 // bls12_381_g1_msm.cu:6426-6486: MSM of (scalars + mask) for each batch
 // entry; the caller subtracts its precomputed MSM(mask, bases)
 // (midnight-sppark-msm/src/lib.rs:3302-3354).
@@ -1378,6 +1389,11 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch(RawG1P
     device_vec_wait(dv, s);
     device_vec_wait(mv, s);
     dev_buf<fr_t> masked(count, s);
+    if (t_mask_delay_ms) {
+        GB_CUDA_OK(cudaMemsetAsync(masked.get(), 0, count * sizeof(fr_t), s));
+        GB_CUDA_OK(cudaStreamSynchronize(s));
+        stream_host_delay(s, t_mask_delay_ms);
+    }
     add_mask_kernel<<<blocks_for(count, 256), 256, 0, s>>>(masked, dv->values + scalar_offset, mv->values, npoints,
                                                            count);
     GB_CHECK_LAUNCH();

@@ -1,6 +1,9 @@
 // Host runtime: lanes, stream-ordered memory, device vectors, transfer
 // counters and the lane / device-vector entry points of the C ABI.
 #include <atomic>
+#include <chrono>
+#include <cstdint>
+#include <thread>
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -93,6 +96,16 @@ void device_vec_mark_ready(fr_device_vec *v, cudaStream_t s)
 void device_vec_wait(const fr_device_vec *v, cudaStream_t s)
 {
     if (v->ready && v->owner != s) GB_CUDA_OK(cudaStreamWaitEvent(s, v->ready, 0));
+}
+
+static void CUDART_CB host_sleep(void *ms)
+{
+    std::this_thread::sleep_for(std::chrono::milliseconds((uintptr_t)ms));
+}
+
+void stream_host_delay(cudaStream_t s, uint32_t ms)
+{
+    if (ms) GB_CUDA_OK(cudaLaunchHostFunc(s, host_sleep, (void *)(uintptr_t)ms));
 }
 
 void device_vec_delete(fr_device_vec *v)

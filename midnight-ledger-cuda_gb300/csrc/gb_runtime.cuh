@@ -146,6 +146,10 @@ void device_vec_mark_ready(fr_device_vec *v, cudaStream_t s);
 void device_vec_wait(const fr_device_vec *v, cudaStream_t s);
 void device_vec_delete(fr_device_vec *v);
 
+// holds stream s back on the host for ms milliseconds (a host function on
+// the stream; the test hooks' stand-in for a slow producer)
+void stream_host_delay(cudaStream_t s, uint32_t ms);
+
 // host<->device copies on the lane stream (pageable or pinned host memory)
 void h2d(void *dst, const void *src, size_t bytes, cudaStream_t s);
 void d2h(void *dst, const void *src, size_t bytes, cudaStream_t s);

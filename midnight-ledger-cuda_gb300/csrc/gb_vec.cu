@@ -5,6 +5,7 @@
 // 2741-3442 device vectors, 3558-4634 vector ops and products).
 #include <cub/device/device_radix_sort.cuh>
 
+#include <algorithm>
 #include <vector>
 
 #include "gb_ntt.cuh"
@@ -542,6 +543,53 @@ static dev_buf<fr_t> upload(const fr_t *host, size_t n, cudaStream_t s)
 
 }  // namespace gb
 
+namespace gb {
+
+static constexpr size_t kSuffixSlice = 8192;
+
+__global__ void nonzero_init_kernel(unsigned long long *stats, size_t count, size_t len)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) {
+        stats[i] = len;        // first nonzero (len: none)
+        stats[count + i] = 0;  // nonzero count
+    }
+}
+
+// block (slice, poly): the slice's first nonzero index and nonzero count,
+// merged into the polynomial's by atomics
+__global__ void nonzero_stats_kernel(unsigned long long *first, unsigned long long *live,
+                                     const fr_t *__restrict__ values, size_t len)
+{
+    __shared__ unsigned long long f_sh[256], c_sh[256];
+    const size_t p = blockIdx.y;
+    const fr_t *poly = values + p * len;
+    const size_t lo = (size_t)blockIdx.x * kSuffixSlice, hi = min(lo + kSuffixSlice, len);
+    unsigned long long f = len, c = 0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        if (!poly[i].is_zero()) {
+            f = min(f, (unsigned long long)i);
+            c++;
+        }
+    }
+    f_sh[threadIdx.x] = f;
+    c_sh[threadIdx.x] = c;
+    __syncthreads();
+    for (unsigned off = blockDim.x / 2; off; off >>= 1) {
+        if (threadIdx.x < off) {
+            f_sh[threadIdx.x] = min(f_sh[threadIdx.x], f_sh[threadIdx.x + off]);
+            c_sh[threadIdx.x] += c_sh[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (f_sh[0] < len) atomicMin(first + p, f_sh[0]);
+        if (c_sh[0]) atomicAdd(live + p, c_sh[0]);
+    }
+}
+
+}  // namespace gb
+
 using namespace gb;
 
 extern "C" {
@@ -1071,6 +1119,85 @@ RustError midnight_sppark_bls12_381_fr_device_vec_gather_polys(void **out, const
         throw;
     }
     *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:3101-3179: per polynomial the first nonzero
+// coefficient (starts) and the nonzero count, then the suffixes from the
+// first nonzero coefficient on, packed polynomial after polynomial.  With
+// out == NULL and out_capacity == 0 only *out_len (the packed length) is
+// returned.
+RustError midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes(RawFr *out, size_t out_capacity,
+                                                                           size_t *out_len, size_t *starts,
+                                                                           size_t *nonzero_counts,
+                                                                           const void *device_vec,
+                                                                           size_t scalar_offset, size_t poly_len,
+                                                                           size_t count)
+{
+    if (!out_len || !starts || !device_vec || poly_len == 0 || count == 0 || count > SIZE_MAX / poly_len ||
+        (out_capacity != 0 && !out))
+        return make_error((int)cudaErrorInvalidValue, "invalid nonzero suffix download arguments");
+    *out_len = 0;
+    auto *v = reinterpret_cast<const fr_device_vec *>(device_vec);
+    const size_t required = poly_len * count;
+    if (scalar_offset > v->len || required > v->len - scalar_offset)
+        return make_error((int)cudaErrorInvalidValue, "nonzero suffix range exceeds device vector");
+    GB_ENTRY_BEGIN
+    cudaStream_t s = lane_stream();
+    device_vec_wait(v, s);
+    const fr_t *base = v->values + scalar_offset;
+    dev_buf<unsigned long long> d_stats(2 * count, s);
+    const uint32_t slices = (uint32_t)((poly_len + kSuffixSlice - 1) / kSuffixSlice);
+    nonzero_init_kernel<<<blocks_for(count, 256), 256, 0, s>>>(d_stats, count, poly_len);
+    GB_CHECK_LAUNCH();
+    for (size_t c0 = 0; c0 < count; c0 += 65535) {
+        const unsigned m = (unsigned)std::min<size_t>(65535, count - c0);
+        nonzero_stats_kernel<<<dim3(slices, m), 256, 0, s>>>(d_stats.get() + c0, d_stats.get() + count + c0,
+                                                             base + c0 * poly_len, poly_len);
+        GB_CHECK_LAUNCH();
+    }
+    std::vector<unsigned long long> h(2 * count);
+    d2h(h.data(), d_stats, 2 * count * sizeof(unsigned long long), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    size_t total = 0;
+    for (size_t p = 0; p < count; p++) {
+        starts[p] = (size_t)h[p];
+        if (nonzero_counts) nonzero_counts[p] = (size_t)h[count + p];
+        total += poly_len - starts[p];
+    }
+    if (!out && out_capacity == 0) {
+        *out_len = total;
+        return ok();
+    }
+    if (total > out_capacity) return make_error((int)cudaErrorInvalidValue, "nonzero suffix output is too small");
+    size_t cursor = 0;
+    for (size_t p = 0; p < count; p++) {
+        const size_t n = poly_len - starts[p];
+        if (n) d2h(out + cursor, base + p * poly_len + starts[p], n * sizeof(fr_t), s);
+        cursor += n;
+    }
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    *out_len = total;
+    return ok();
+    GB_ENTRY_END
+}
+
+// bls12_381_g1_msm.cu:6406-6423 (test hooks): scales a resident vector in
+// place on this lane after holding the lane's stream back for delay_ms; the
+// vector's ready event moves past the scaling, so a reader on another lane
+// waits for it
+RustError midnight_sppark_test_delayed_scale(void *device_vec, RawFr scale, uint32_t delay_ms)
+{
+    if (!device_vec) return make_error((int)cudaErrorInvalidValue, "null device vector");
+    GB_ENTRY_BEGIN
+    auto *v = reinterpret_cast<fr_device_vec *>(device_vec);
+    cudaStream_t s = lane_stream();
+    device_vec_wait(v, s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    stream_host_delay(s, delay_ms);
+    if (v->len) launch_mul_assign(v->values, gb::from_raw(scale), v->len, s);
+    device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
 }

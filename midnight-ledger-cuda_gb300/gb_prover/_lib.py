@@ -156,6 +156,11 @@ def _declare(L):
             vp, vp, vp, vp, vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, sz, vp, vp, sz]),
         "midnight_sppark_bls12_381_fr_multiopen_f_poly_device": (E, [vp, vp, sz, vp, sz, vp, sz, vp, sz]),
         "midnight_sppark_bls12_381_fr_multiopen_pi_device": (E, [vp, vp, vp, sz, vp, sz, fr]),
+        "midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes": (E, [
+            vp, sz, vp, vp, vp, vp, sz, sz, sz]),
+        "midnight_sppark_bls12_381_fr_lookup_permute_batch": (E, [vp, vp, vp, sz, sz, sz, vp, vp, sz]),
+        "midnight_sppark_test_mask_delay": (None, [u32]),
+        "midnight_sppark_test_delayed_scale": (E, [vp, fr, u32]),
         "midnight_sppark_bls12_381_numerator_context_eval": (E, [
             vp, vp, vp, sz, sz, sz, sz, sz, vp, sz, fr, fr, fr, fr, fr, sz, sz, sz, sz, sz, sz, sz, sz]),
         "midnight_sppark_bls12_381_trace_context_trash": (E, [vp, vp, vp, sz, vp, sz, vp, sz, fr]),

@@ -27,7 +27,8 @@ __all__ = [
     "eval_graph_batch_device", "eval_numerator_device", "fr_permutation_products_device", "fr_random_chacha20",
     "fr_lookup_permute_device", "NumeratorContext", "bls12_381_fr_multiopen_prepare",
     "bls12_381_fr_multiopen_prepare_device", "bls12_381_fr_multiopen_f_poly_device",
-    "bls12_381_fr_multiopen_pi_device", "autotune_set", "autotune_reset", "autotune_report",
+    "bls12_381_fr_multiopen_pi_device", "bls12_381_fr_lookup_permute_batch", "hook_mask_delay",
+    "hook_delayed_scale", "autotune_set", "autotune_reset", "autotune_report",
 ]
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
@@ -193,6 +194,19 @@ class Bls12_381FrDeviceVec:
         check(lib().midnight_sppark_bls12_381_fr_device_vec_gather_polys(ctypes.byref(h), self.raw, poly_len,
                                                                          _ptr(idx), len(idx)))
         return Bls12_381FrDeviceVec(h)
+
+    def download_nonzero_suffixes(self, scalar_offset, poly_len, count):
+        """(packed suffixes, starts, nonzero counts): each polynomial from its
+        first nonzero coefficient on (lib.rs:2035-2160)."""
+        n_out = ctypes.c_size_t()
+        starts = np.zeros(count, dtype=np.uint64)
+        live = np.zeros(count, dtype=np.uint64)
+        f = lib().midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes
+        check(f(None, 0, ctypes.byref(n_out), _ptr(starts), _ptr(live), self.raw, scalar_offset, poly_len, count))
+        out = np.zeros((max(n_out.value, 1), 4), dtype=np.uint64)
+        check(f(_ptr(out), n_out.value, ctypes.byref(n_out), _ptr(starts), _ptr(live), self.raw, scalar_offset,
+                poly_len, count))
+        return out[:n_out.value], starts, live
 
     def ntt_zeta(self, log_n, inverse, scale, first, second):
         check(lib().midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(self.raw, log_n, inverse, _fr(scale),
@@ -613,6 +627,31 @@ def fr_lookup_permute_device(compressed, length, usable_rows, lookup_count, inpu
     check(lib().gb_fr_lookup_permute_device(ctypes.byref(h), compressed.raw, length, usable_rows, lookup_count,
                                             _ptr(ib), _ptr(tb)))
     return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_lookup_permute_batch(compressed_inputs, compressed_tables, length, lookup_count, usable_rows,
+                                      input_blinds, table_blinds):
+    """midnight_sppark_bls12_381_fr_lookup_permute_batch: a device vector
+    [inputs | tables | permuted inputs | permuted tables]."""
+    ci, ct = _fr_arr(compressed_inputs), _fr_arr(compressed_tables)
+    nb = length - usable_rows
+    ib = _fr_arr(input_blinds) if nb else np.zeros((1, 4), dtype=np.uint64)
+    tb = _fr_arr(table_blinds) if nb else np.zeros((1, 4), dtype=np.uint64)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_lookup_permute_batch(
+        ctypes.byref(h), _ptr(ci), _ptr(ct), length, lookup_count, usable_rows, ib.ctypes.data_as(ctypes.c_void_p),
+        tb.ctypes.data_as(ctypes.c_void_p), nb))
+    return Bls12_381FrDeviceVec(h)
+
+
+def hook_mask_delay(delay_ms):
+    """test hook: delay the next scrambled batches' mask producer"""
+    lib().midnight_sppark_test_mask_delay(int(delay_ms))
+
+
+def hook_delayed_scale(vec, scale, delay_ms):
+    """test hook: vec *= scale on this lane after holding it back delay_ms"""
+    check(lib().midnight_sppark_test_delayed_scale(vec.raw, _fr(scale), int(delay_ms)))
 
 
 def _u32(a):
