@@ -58,3 +58,32 @@ def test_argument_validation_without_gpu(gb):
     err = lib.midnight_sppark_execution_lane_set(99)
     assert err.code == 1
     gb.api.check(lib.midnight_sppark_execution_lane_set(0))
+
+
+def test_context_and_multiopen_validation_without_gpu(gb):
+    """The numerator context, multi-open and lookup batch entry points check
+    their arguments before any device work, with the reference's messages
+    (bls12_381_g1_msm.cu:3617-3642, 5548-5561, 5150-5155)."""
+    lib = gb.lib()
+    z = gb.api._fr(np.zeros(4, dtype=np.uint64))
+    h = ctypes.c_void_p()
+    # create without l0 / l_last / l_active
+    err = lib.midnight_sppark_bls12_381_numerator_context_create(
+        ctypes.byref(h), 16, 4, None, None, 0, None, None, None, None, 0, None, None, 0, None, 0,
+        gb.graph.RawGraph(), None, None, None, 0, None, z, z, z, z, 1, -1, 1)
+    with pytest.raises(gb.MsmError, match="invalid numerator context arguments"):
+        gb.api.check(err)
+    # non-monotonic q offsets
+    polys = np.zeros((8, 4), dtype=np.uint64)
+    with pytest.raises(gb.MsmError, match="non-monotonic multi-open q offsets"):
+        gb.bls12_381_fr_multiopen_prepare(polys, 4, [0, 2, 1, 3], [0, 1, 1], np.zeros((3, 4), np.uint64),
+                                          np.zeros((1, 4), np.uint64), [0], [0])
+    # a query point out of range
+    with pytest.raises(gb.MsmError, match="multi-open query index out of range"):
+        gb.bls12_381_fr_multiopen_prepare(polys, 4, [0, 1], [0], np.zeros((1, 4), np.uint64),
+                                          np.zeros((1, 4), np.uint64), [0], [1])
+    # blind count that does not match len - usable_rows
+    err = lib.midnight_sppark_bls12_381_fr_lookup_permute_batch(
+        ctypes.byref(h), gb.api._ptr(polys), gb.api._ptr(polys), 8, 1, 6, gb.api._ptr(polys), gb.api._ptr(polys), 1)
+    with pytest.raises(gb.MsmError, match="invalid resident lookup permutation arguments"):
+        gb.api.check(err)
