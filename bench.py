@@ -84,24 +84,31 @@ def f_msm(n):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms.  The
+    sampler is running before the timed region starts (its first row has
+    arrived), each row carries its arrival time, and the summary keeps the
+    rows that arrived inside the region set by window()."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, interval_ms=20):
         self.index = index
+        self.interval_ms = interval_ms
         self.rows = []
         self.proc = None
+        self.span = None
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            self.first.wait(timeout=5.0)
         except OSError:
             self.proc = None
         return self
@@ -110,10 +117,16 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) == 7:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
+                self.first.set()
+
+    def window(self, t0, t1):
+        """the timed region, in time.perf_counter() seconds"""
+        self.span = (t0, t1)
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(2 * self.interval_ms / 1e3)  # the row covering the region's end
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -121,14 +134,16 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        rows = [r for t, r in self.rows if self.span is None or self.span[0] <= t <= self.span[1] +
+                self.interval_ms / 1e3]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "interval_ms": self.interval_ms}
 
 
 def dist_setup():
@@ -282,6 +297,7 @@ def main():
         e1.record(stream)
         e1.synchronize()
         wall = time.perf_counter() - t0
+        clk.window(t0, t0 + wall)
     torch.cuda.synchronize()
     barrier(world)
     launches = gb.launch_counter() - launches0
