@@ -129,6 +129,9 @@ GB_API RustError midnight_sppark_bls12_381_g1_msm_context_create_with_config(voi
                                                                              RawMsmConfig config);
 /* bls12_381_g1_msm.cu:6283-6286 */
 GB_API void midnight_sppark_bls12_381_g1_msm_context_free(void *context);
+/* device bytes held by a context (its nwin x npoints table of affine
+ * points); no reference counterpart, for HBM budgeting */
+GB_API size_t gb_g1_msm_context_device_bytes(const void *context);
 /* bls12_381_g1_msm.cu:6288-6308: host scalars [nmsms][npoints] */
 GB_API RustError midnight_sppark_bls12_381_g1_msm_context_batch(RawG1Projective *out, void *context,
                                                                 const RawFr *scalars, size_t npoints,
@@ -453,6 +456,11 @@ GB_API size_t gb_fr_device_vec_len(const void *device_vec);
 GB_API RustError gb_g1_generator_mul(RawG1Affine *out, const RawFr *scalars, size_t n);
 /* same with device pointers; queued on the calling lane's stream */
 GB_API RustError gb_g1_generator_mul_device(RawG1Affine *d_out, const RawFr *d_scalars, size_t n);
+/* one MSM over n bases and n scalars already in device memory (caller's
+ * pointers), result to the host: the plain engine (Horner over windows),
+ * no precomputed table (a context keeps nwin x n x 96 bytes) */
+GB_API RustError gb_g1_msm_device(RawG1Projective *out, const RawG1Affine *d_points, const RawFr *d_scalars,
+                                  size_t n);
 /* KZG SRS (no FFI counterpart; the reference does these in Rust on the CPU):
  * g_lagrange = iFFT(g) * n^-1 over G1 for 2^k points (arithmetic.rs:34-50,
  * params.rs:60-77 downsize), and the seeded-tau setup of params.rs:79-129
@@ -482,10 +490,41 @@ GB_API void gb_autotune_set(int enabled);
  * in shared memory by a bulk copy; 0 restores the default (4) or the
  * autotuned choice */
 GB_API void gb_ntt_variant_set(int variant);
-/* staged NTT passes whose twiddle copy did not complete within the spin
- * limit, plus work-queue waits that ran out, since the last call (their
- * output is invalid); resets the count */
+/* bounded waits of NTT calls (staged-pass twiddle copies, work-queue waits)
+ * that ran out since the last read, process-wide; every call that saw one
+ * returned cudaErrorLaunchTimeout and its output is invalid.  Resets the
+ * count.  Each call counts its own waits in a status word it owns. */
 GB_API RustError gb_ntt_wait_timeouts(uint32_t *out);
+/* test hook: poll limit of the first twiddle-copy wait of staged NTT passes
+ * launched from now on, process-wide (negative = default; 0 = the wait gives
+ * up at once and the call returns cudaErrorLaunchTimeout, while the copy
+ * still lands in a second, longer wait before the CTA moves on) */
+GB_API void gb_ntt_wait_limit_set(int64_t spins);
+/* ---- coset by the powers of a shift: sppark's coset NTT and LDE form
+ * (vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:78-97,196-209,283-342; kernels.cu
+ * LDE_distribute_powers / LDE_spread_distribute_powers), which the
+ * reference's vendored sppark uses with the multiplicative generator 7
+ * (parameters/bls12_381.h:11, fq.rs:31-33 GENERATOR).  The reference's
+ * midnight_sppark_* FFI exports only the ZETA coset; these are the
+ * generator-coset counterparts. */
+/* coefficients -> evaluations on shift * <w_ext>: out[p][j] = sum_i
+ * inputs[p][i] (shift w_ext^j)^i for count polynomials of input_len values,
+ * out count x 2^extended_log_n; host buffers */
+GB_API RustError gb_fr_coeff_to_extended_coset_batch(RawFr *out, const RawFr *inputs, size_t input_len,
+                                                     size_t count, uint32_t extended_log_n, RawFr shift);
+/* the same from resident coefficients into a new device vector */
+GB_API RustError gb_fr_device_coeff_to_extended_coset_batch(void **out, const void *source, size_t input_len,
+                                                            size_t count, uint32_t extended_log_n, RawFr shift);
+/* coset NTT in place on count resident polynomials of 2^log_n values
+ * (NTT::Base with Type::coset, natural order): forward NTT(a_i shift^i),
+ * inverse iNTT(a)_i shift^-i with the iNTT's 1/n */
+GB_API RustError gb_fr_device_vec_ntt_coset_batch(void *device_vec, uint32_t log_n, size_t count, bool inverse,
+                                                  RawFr shift);
+/* the same on one host polynomial */
+GB_API RustError gb_fr_ntt_coset(RawFr *values, uint32_t log_n, bool inverse, RawFr shift);
+/* NTT::LDE: 2^lg_domain_size evaluations -> 2^(lg_domain_size + lg_blowup)
+ * evaluations of the same polynomial on the coset of the generator 7 */
+GB_API RustError gb_fr_lde_coset(RawFr *out, const RawFr *in, uint32_t lg_domain_size, uint32_t lg_blowup);
 /* NTTs of `count` polynomials of different sizes held in one device vector,
  * in one persistent launch fed by a device work queue: polynomial j is the
  * 2^log_ns[j] values at element offset offsets[j] (ranges inside the vector,

@@ -1208,6 +1208,31 @@ RustError midnight_sppark_bls12_381_g1_msm(RawG1Projective *out_raw, const RawG1
     GB_ENTRY_END
 }
 
+// One MSM over bases and scalars already in device memory (the caller's
+// pointers, e.g. a resident SRS and a polynomial): the plain engine with
+// windows combined by Horner's rule, no precomputed table, so it needs n x
+// 96 bytes of bases instead of a context's nwin x n x 96.  No reference
+// counterpart: the reference's resident MSMs all go through a context.
+RustError gb_g1_msm_device(RawG1Projective *out_raw, const RawG1Affine *d_points_raw, const RawFr *d_scalars_raw,
+                           size_t n)
+{
+    jacobian_t *out = reinterpret_cast<jacobian_t *>(out_raw);
+    const affine_t *d_points = reinterpret_cast<const affine_t *>(d_points_raw);
+    const fr_t *d_scalars = reinterpret_cast<const fr_t *>(d_scalars_raw);
+    GB_ENTRY_BEGIN
+    if (!out || (n && (!d_points || !d_scalars)))
+        return make_error((int)cudaErrorInvalidValue, "invalid device MSM arguments");
+    cudaStream_t s = lane_stream();
+    dev_buf<jacobian_t> d_out(1, s);
+    std::vector<msm_item> items{msm_item{d_scalars, n, 0}};
+    msm_run_batch(items, tuned_window(items, d_points, 0, s), false, d_points, 0, d_out, s);
+    d2h(out, d_out, sizeof(jacobian_t), s);
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    timed_collect();
+    return ok();
+    GB_ENTRY_END
+}
+
 // bls12_381_g1_msm.cu:6202-6245; scalars laid out [nmsms][npoints]
 RustError midnight_sppark_bls12_381_g1_msm_batch(RawG1Projective *out_raw, const RawG1Affine *points_raw, const RawFr *scalars_raw, size_t npoints, size_t nmsms)
 {
@@ -1265,6 +1290,14 @@ RustError midnight_sppark_bls12_381_g1_msm_context_create(void **out, const RawG
 {
     return midnight_sppark_bls12_381_g1_msm_context_create_with_config(out, points_raw, npoints,
                                                                        default_config(npoints));
+}
+
+// Device bytes a context holds: its table of nwin x npoints affine points
+// (the bases shifted by each window).  No reference counterpart.
+size_t gb_g1_msm_context_device_bytes(const void *context)
+{
+    auto *ctx = reinterpret_cast<const msm_context_t *>(context);
+    return ctx ? ctx->npoints * (size_t)ctx->nwin * sizeof(affine_t) : 0;
 }
 
 void midnight_sppark_bls12_381_g1_msm_context_free(void *context)

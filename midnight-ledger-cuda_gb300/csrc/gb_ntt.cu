@@ -11,8 +11,10 @@
 // Within a pass, either each thread runs one radix-2 butterfly per stage
 // (a barrier per stage), or each thread holds 4 or 8 elements and runs 2 or 3
 // stages in registers between exchanges through shared memory.
+#include <atomic>
 #include <cstdlib>
 #include <map>
+#include <string>
 #include <mutex>
 #include <algorithm>
 #include <tuple>
@@ -394,13 +396,22 @@ __device__ __forceinline__ void ntt_tw_group(uint4 *sd, const uint4 *stw, uint32
     for (int k = 0; k < E; k++) ntt_st_c(sd, base ^ off[k], x[k]);
 }
 
+// Spin limits of the twiddle copy's waits.  The first wait gives up after
+// the launch's `spins` polls (kWaitSpins unless a test lowers it), counts a
+// timeout in the call's status word and skips the butterflies; the CTA then
+// waits again, up to kDrainSpins polls, for the copy still in flight, so
+// that it does not leave while the copy can still write its shared memory.
+// The copy's source lies inside the pass's twiddle table and its size is
+// that of the CTA's chunk (at most 2^10 entries of 32 bytes), so in a
+// working GPU it lands within microseconds.
 static constexpr unsigned kWaitSpins = 1u << 24;
+static constexpr unsigned kDrainSpins = 1u << 26;
 
 // bounded wait on the phase of an mbarrier with the given parity; true when
 // the phase completed
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, unsigned spins)
 {
-    for (unsigned i = 0; i < kWaitSpins; i++) {
+    for (unsigned i = 0; i < spins; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -414,13 +425,41 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
     return false;
 }
 
-__device__ unsigned int g_ntt_wait_timeouts;
-
-// output factors of the last pass: natural index i of a transform is
-// multiplied by f[i mod 3] (the ZETA coset distribution times the scale)
+// Factors by position i (natural order) of a transform, applied by the last
+// pass to its outputs or by a fused first pass to its inputs:
+//   on == 1: f[i mod 3] (the ZETA coset distribution times a scale);
+//   on == 2: pw_hi[i >> lo_bits] * pw_lo[i mod 2^lo_bits] (powers of a
+//            coset shift from two tables, any scale folded into pw_hi);
+//   on == 0: none.
 struct ntt_factors {
     fr_t f[3];
     int on;
+    const fr_t *pw_lo = nullptr, *pw_hi = nullptr;
+    uint32_t lo_bits = 0;
+};
+
+__device__ __forceinline__ fr_t ntt_factor(const ntt_factors &fac, size_t i)
+{
+    fr_t f;
+    if (fac.on == 2) {
+        const fr_t lo = fac.pw_lo[i & (((size_t)1 << fac.lo_bits) - 1)];
+        const fr_t hi = fac.pw_hi[i >> fac.lo_bits];
+        f = hi * lo;
+    } else {
+        const uint32_t c = (uint32_t)(i % 3);
+#pragma unroll
+        for (int w = 0; w < 8; w++) f.v[w] = c == 0 ? fac.f[0].v[w] : c == 1 ? fac.f[1].v[w] : fac.f[2].v[w];
+    }
+    return f;
+}
+
+// The input of a fused first pass: `count` polynomials of in_len values
+// each at src (values past in_len read as zero: the zero padding of a coset
+// LDE), each value multiplied by fac's factor of its position when fac.on.
+struct ntt_input {
+    const fr_t *src;
+    size_t in_len;
+    ntt_factors fac;
 };
 
 __device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bits ? __brev(x) >> (32 - bits) : 0u; }
@@ -444,10 +483,15 @@ __device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bit
 // the block may be wider than the piece (the extra threads sit out the
 // butterfly groups), the sources are read through L2 because other CTAs of
 // the same launch wrote them, and the mbarrier completes one phase per piece.
-template <int EL, bool LAST, bool QUEUE>
+// LOADF selects the fused first pass of a coset LDE or coset transform: the
+// sub-blocks are gathered from `in` (see ntt_input) instead of src; it needs
+// s_lo > 0, i.e. a transform of two or more passes.  A twiddle copy that
+// does not land within `spins` polls is counted in *status.
+template <int EL, bool LAST, bool QUEUE, bool LOADF = false>
 __device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q,
                                              size_t count, const fr_t *__restrict__ twt, const ntt_factors &fac,
-                                             size_t cta, uint4 *smem, uint32_t mbar, uint32_t parity, int &copy_ok)
+                                             size_t cta, uint4 *smem, uint32_t mbar, uint32_t parity, int &copy_ok,
+                                             uint32_t *status, unsigned spins, const ntt_input &in = ntt_input{})
 {
     const int s_lo = s_hi - g + 1;
     const uint32_t sub = 1u << g, Q = 1u << q, nd = Q << g;
@@ -505,7 +549,14 @@ __device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_
             }
         }
         fr_t v = fr_t::zero();
-        if (valid) {
+        if (LOADF) {
+            // first pass: s_hi = log_n - 1, so the position is addr - poly * n
+            const size_t i = addr - poly * n;
+            if (i < in.in_len) {
+                v = in.src[poly * in.in_len + i];
+                if (in.fac.on) v = v * ntt_factor(in.fac, i);
+            }
+        } else if (valid) {
             if (QUEUE) {
                 const uint4 *p = reinterpret_cast<const uint4 *>(src + addr);
                 const uint4 lo = __ldcg(p), hi = __ldcg(p + 1);
@@ -518,10 +569,10 @@ __device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_
         ntt_st(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u), v);
     }
     if (threadIdx.x == 0) {
-        bool ok = mbar_wait(mbar, parity);
+        bool ok = mbar_wait(mbar, parity, spins);
         if (!ok) {
-            atomicAdd(&g_ntt_wait_timeouts, 1u);
-            mbar_wait(mbar, parity);  // let the copy in flight land before the CTA exits
+            if (status) atomicAdd(status, 1u);
+            mbar_wait(mbar, parity, kDrainSpins);  // let the copy in flight land before the CTA goes on
         }
         copy_ok = ok;
     }
@@ -588,13 +639,7 @@ __device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_
             fr_t v = ntt_ld(sd + 2 * (size_t)qq * sub, t, ntt_twist(qq & 7u));
             // x * f with x < 2r, f < r is fully reduced by the product
             if (!fac.on) v = bfly_out(v);
-            if (fac.on) {
-                const uint32_t c = (uint32_t)(i_nat % 3);
-                fr_t f;
-#pragma unroll
-                for (int w = 0; w < 8; w++) f.v[w] = c == 0 ? fac.f[0].v[w] : c == 1 ? fac.f[1].v[w] : fac.f[2].v[w];
-                v = v * f;
-            }
+            else v = v * ntt_factor(fac, i_nat);
             dst[addr] = v;
             continue;
         }
@@ -603,10 +648,11 @@ __device__ __forceinline__ bool ntt_tw_piece(const fr_t *src, fr_t *dst, uint32_
     return true;
 }
 
-template <int EL, bool LAST>
+template <int EL, bool LAST, bool LOADF = false>
 __global__ void __launch_bounds__(1024 >> EL, 3)
     ntt_dif_pass_tw_kernel(const fr_t *src, fr_t *dst, uint32_t log_n, int s_hi, int g, int q, size_t count,
-                           const fr_t *__restrict__ twt, ntt_factors fac)
+                           const fr_t *__restrict__ twt, ntt_factors fac, ntt_input in, uint32_t *status,
+                           unsigned spins)
 {
     extern __shared__ uint4 smem[];
     __shared__ uint64_t mbar_store;
@@ -617,7 +663,8 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    ntt_tw_piece<EL, LAST, false>(src, dst, log_n, s_hi, g, q, count, twt, fac, blockIdx.x, smem, mbar, 0, copy_ok);
+    ntt_tw_piece<EL, LAST, false, LOADF>(src, dst, log_n, s_hi, g, q, count, twt, fac, blockIdx.x, smem, mbar, 0,
+                                         copy_ok, status, spins, in);
 }
 
 // ---------------------------------------------------------------- work queue
@@ -652,8 +699,6 @@ enum { NTT_Q_NEXT = 0, NTT_Q_ABORT = 1, NTT_Q_COUNTERS = 2 };
 static constexpr unsigned kQueueSpins = 1u << 22;
 static constexpr uint32_t kQueuePieceBits = 24;
 
-__device__ unsigned int g_ntt_queue_timeouts;
-
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
 {
     uint32_t v;
@@ -664,7 +709,7 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
 template <int EL>
 __global__ void __launch_bounds__(1024 >> EL, 3)
     ntt_queue_kernel(const ntt_qjob *__restrict__ jobs, const uint2 *__restrict__ items, uint32_t n_items,
-                     uint32_t *ctl)
+                     uint32_t *ctl, uint32_t *status, unsigned spins)
 {
     extern __shared__ uint4 smem[];
     __shared__ uint64_t mbar_store;
@@ -698,7 +743,7 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
                         __nanosleep(64);
                     }
                     if (i == kQueueSpins) {
-                        atomicAdd(&g_ntt_queue_timeouts, 1u);
+                        atomicAdd(&status[1], 1u);
                         atomicExch(&ctl[NTT_Q_ABORT], 1u);
                         ok = 0;
                     }
@@ -716,11 +761,11 @@ __global__ void __launch_bounds__(1024 >> EL, 3)
         bool ok;
         if (pass + 1 == J.npass) {
             ok = ntt_tw_piece<EL, true, true>(P.src, P.dst, J.log_n, P.s_hi, P.g, P.q, 1, P.tw, J.fac, piece, smem,
-                                              mbar, parity, copy_ok);
+                                              mbar, parity, copy_ok, status, spins);
         } else {
             const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
             ok = ntt_tw_piece<EL, false, true>(P.src, P.dst, J.log_n, P.s_hi, P.g, P.q, 1, P.tw, none, piece, smem,
-                                               mbar, parity, copy_ok);
+                                               mbar, parity, copy_ok, status, spins);
         }
         parity ^= 1u;
         __syncthreads();  // every store of the piece is issued
@@ -836,7 +881,79 @@ __global__ void c2e_prepare_kernel(fr_t *out, const fr_t *__restrict__ in, fr_t 
     out[f] = v;
 }
 
+// d[i] *= fac's factor of position i mod period_len (mode 1 or 2)
+__global__ void mul_factors_kernel(fr_t *d, ntt_factors fac, size_t len, size_t period_len)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    d[i] = d[i] * ntt_factor(fac, i % period_len);
+}
+
+// out[p][i] = i < in_len ? in[p][i] * factor(i) : 0 for count polynomials of
+// out_len values (the padded input of an unfused coset LDE); in may equal out
+// when in_len == out_len
+__global__ void c2e_factors_kernel(fr_t *out, const fr_t *in, ntt_factors fac, size_t input_len, size_t output_len,
+                                   size_t count)
+{
+    const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= output_len * count) return;
+    const size_t li = f % output_len, p = f / output_len;
+    fr_t v = fr_t::zero();
+    if (li < input_len) {
+        v = in[p * input_len + li];
+        if (fac.on) v = v * ntt_factor(fac, li);
+    }
+    out[f] = v;
+}
+
+// out[j] = scale * base^j
+__global__ void powers_table_kernel(fr_t *out, fr_t base, fr_t scale, size_t len)
+{
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < len) out[j] = scale * base.pow_u64(j);
+}
+
 // ---------------------------------------------------------------- host side
+
+// The first twiddle wait's poll limit for every launch; a test lowers it
+// through gb_ntt_wait_limit_set to make the wait run out on purpose (the
+// copy then still lands within the drain wait, see kDrainSpins).
+static std::atomic<long long> g_wait_spins_override{-1};
+static unsigned wait_spins()
+{
+    const long long v = g_wait_spins_override.load(std::memory_order_relaxed);
+    return v < 0 ? kWaitSpins : (unsigned)v;
+}
+
+// Bounded waits that ran out in NTT calls since the last gb_ntt_wait_timeouts
+// (each such call also returned an error).
+static std::atomic<unsigned long long> g_timeouts_seen{0};
+
+// The status words of one NTT call on stream s, in memory the call owns:
+// [0] staged-pass CTAs whose twiddle copy did not land within the wait
+// limit, [1] work-queue waits that ran out.  check() waits for the call's
+// work and throws cudaErrorLaunchTimeout when either is non-zero (the
+// transform is then not valid).
+struct ntt_status {
+    dev_buf<uint32_t> w;
+    cudaStream_t s;
+    explicit ntt_status(cudaStream_t st) : w(2, st), s(st)
+    {
+        GB_CUDA_OK(cudaMemsetAsync(w.get(), 0, 2 * sizeof(uint32_t), s));
+    }
+    uint32_t *ptr() const { return w.get(); }
+    void check()
+    {
+        uint32_t h[2] = {0, 0};
+        GB_CUDA_OK(cudaMemcpyAsync(h, w.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+        GB_CUDA_OK(cudaStreamSynchronize(s));
+        if (h[0] || h[1]) {
+            g_timeouts_seen.fetch_add((unsigned long long)h[0] + h[1]);
+            throw cuda_error((int)cudaErrorLaunchTimeout,
+                             h[0] ? "NTT twiddle copy did not complete" : "NTT work-queue wait ran out");
+        }
+    }
+};
 
 namespace {
 std::mutex g_tw_mu;
@@ -874,6 +991,10 @@ void set_ntt_smem()
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
         cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<2, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             staged);
+        cudaFuncSetAttribute(ntt_dif_pass_tw_kernel<3, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             staged);
         cudaFuncSetAttribute(ntt_queue_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged);
     });
 }
@@ -927,14 +1048,20 @@ const fr_t *pass_twiddles(uint32_t log_n, bool inverse, int s_hi, int g, const f
 // thread), natural order out with the output factors applied.  With two or
 // more passes the first pass writes to a scratch buffer, the middle ones work
 // there in place and the last one writes natural order back to d, so no
-// separate bit-reversal pass is needed; a single pass works in place.
+// separate bit-reversal pass is needed; a single pass works in place.  With
+// `in` (two or more passes only) the first pass gathers its inputs from
+// in->src instead of d (zero padding and input factors, see ntt_input), so d
+// is written but never read.
 static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *tw, int el,
-                       const ntt_factors &fac, cudaStream_t s)
+                       const ntt_factors &fac, uint32_t *status, cudaStream_t s, const ntt_input *in = nullptr)
 {
     const auto passes = pass_split(log_n);
     const size_t P = passes.size();
+    if (in && P < 2) throw cuda_error(-1, "fused NTT input needs two or more passes");
     dev_buf<fr_t> tmp(P > 1 ? count << log_n : 0, s);
     const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+    const ntt_input no_in{nullptr, 0, none};
+    const unsigned spins = wait_spins();
     for (size_t i = 0; i < P; i++) {
         const int s_hi = passes[i].first, g = passes[i].second;
         const int s_lo = s_hi - g + 1;
@@ -962,20 +1089,28 @@ static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, cons
         const uint32_t tw_entries = s_lo > 0 ? nd : 1u << g;
         const size_t smem = ((size_t)nd + tw_entries) * sizeof(fr_t);
         const unsigned threads = nd >> el;
+        const bool fused = in && i == 0;
+        const ntt_input &pin = fused ? *in : no_in;
         if (el == 3) {
             if (last)
-                ntt_dif_pass_tw_kernel<3, true><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
-                                                                                       count, tab, fac);
+                ntt_dif_pass_tw_kernel<3, true><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, fac, pin, status, spins);
+            else if (fused)
+                ntt_dif_pass_tw_kernel<3, false, true><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, none, pin, status, spins);
             else
-                ntt_dif_pass_tw_kernel<3, false><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
-                                                                                        count, tab, none);
+                ntt_dif_pass_tw_kernel<3, false><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, none, pin, status, spins);
         } else {
             if (last)
-                ntt_dif_pass_tw_kernel<2, true><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
-                                                                                       count, tab, fac);
+                ntt_dif_pass_tw_kernel<2, true><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, fac, pin, status, spins);
+            else if (fused)
+                ntt_dif_pass_tw_kernel<2, false, true><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, none, pin, status, spins);
             else
-                ntt_dif_pass_tw_kernel<2, false><<<(unsigned)ctas, threads, smem, s>>>(src, dst, log_n, s_hi, g, q,
-                                                                                        count, tab, none);
+                ntt_dif_pass_tw_kernel<2, false><<<(unsigned)ctas, threads, smem, s>>>(
+                    src, dst, log_n, s_hi, g, q, count, tab, none, pin, status, spins);
         }
         GB_CHECK_LAUNCH();
     }
@@ -987,7 +1122,7 @@ static void ntt_staged(fr_t *d, uint32_t log_n, size_t count, bool inverse, cons
 // passes run through a scratch copy as ntt_staged does; every size needs
 // log_ns[j] >= 3.  Returns the number of launches (0 or 1).
 static int ntt_ragged(fr_t *d, const size_t *offsets, const uint32_t *log_ns, const ntt_factors *fac, size_t count,
-                      bool inverse, cudaStream_t s)
+                      bool inverse, uint32_t *status, cudaStream_t s)
 {
     set_ntt_smem();
     std::vector<ntt_qjob> jobs(count);
@@ -1058,7 +1193,8 @@ static int ntt_ragged(fr_t *d, const size_t *offsets, const uint32_t *log_ns, co
     GB_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ntt_queue_kernel<2>, threads, smem));
     GB_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t grid = std::min(items.size(), (size_t)std::max(per_sm, 1) * (size_t)sms);
-    ntt_queue_kernel<2><<<(unsigned)grid, threads, smem, s>>>(djobs, ditems, (uint32_t)items.size(), ctl);
+    ntt_queue_kernel<2><<<(unsigned)grid, threads, smem, s>>>(djobs, ditems, (uint32_t)items.size(), ctl, status,
+                                                              wait_spins());
     GB_CHECK_LAUNCH();
     return 1;
 }
@@ -1093,19 +1229,22 @@ static void ntt_passes(fr_t *d, uint32_t log_n, size_t count, const fr_t *tw, in
 // bit-reversal pass and a factor pass), 4 / 5 = 4 / 8 elements per thread with
 // the pass's twiddles staged in shared memory (fused as above).
 static void ntt_transform(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *tw, int v,
-                          const ntt_factors &fac, cudaStream_t s)
+                          const ntt_factors &fac, uint32_t *status, cudaStream_t s)
 {
     const size_t n = (size_t)1 << log_n;
     if (v >= 4 && log_n >= 3) {
-        ntt_staged(d, log_n, count, inverse, tw, v == 5 ? 3 : 2, fac, s);
+        ntt_staged(d, log_n, count, inverse, tw, v == 5 ? 3 : 2, fac, status, s);
         return;
     }
     if (log_n > 0) ntt_passes(d, log_n, count, tw, v >= 4 ? 2 : v, s);
     dim3 grid(blocks_for(n, 256), (unsigned)count);
     bitrev_scale_kernel<<<grid, 256, 0, s>>>(d, log_n, false, fr_t::one());
     GB_CHECK_LAUNCH();
-    if (fac.on) {
+    if (fac.on == 1) {
         mul_period3_kernel<<<blocks_for(n * count, 256), 256, 0, s>>>(d, fac.f[0], fac.f[1], fac.f[2], n * count, n);
+        GB_CHECK_LAUNCH();
+    } else if (fac.on == 2) {
+        mul_factors_kernel<<<blocks_for(n * count, 256), 256, 0, s>>>(d, fac, n * count, n);
         GB_CHECK_LAUNCH();
     }
 }
@@ -1116,7 +1255,7 @@ static int g_variant_forced = 0;
 // GB_NTT_VARIANT (1..5) or gb_ntt_variant_set overrides; with the autotuner
 // on, each size times the five variants once on a scratch copy of one
 // transform.
-static int ntt_variant(fr_t *d, uint32_t log_n, bool inverse, const fr_t *tw, cudaStream_t s)
+static int ntt_variant(fr_t *d, uint32_t log_n, bool inverse, const fr_t *tw, uint32_t *status, cudaStream_t s)
 {
     static const int v_env = [] {
         const char *e = getenv("GB_NTT_VARIANT");
@@ -1134,7 +1273,7 @@ static int ntt_variant(fr_t *d, uint32_t log_n, bool inverse, const fr_t *tw, cu
     float best = 1e30f;
     for (int cand = 1; cand <= 5; cand++) {
         GB_CUDA_OK(cudaMemcpyAsync(scratch.get(), d, n * sizeof(fr_t), cudaMemcpyDeviceToDevice, s));
-        float ms = time_on_stream(s, [&] { ntt_transform(scratch, log_n, 1, inverse, tw, cand, none, s); });
+        float ms = time_on_stream(s, [&] { ntt_transform(scratch, log_n, 1, inverse, tw, cand, none, status, s); });
         if (ms < best) {
             best = ms;
             v = cand;
@@ -1144,20 +1283,88 @@ static int ntt_variant(fr_t *d, uint32_t log_n, bool inverse, const fr_t *tw, cu
     return v;
 }
 
-static void ntt_apply(fr_t *d, uint32_t log_n, size_t count, bool inverse, const ntt_factors &fac, cudaStream_t s)
+static void ntt_apply(fr_t *d, uint32_t log_n, size_t count, bool inverse, const ntt_factors &fac, uint32_t *status,
+                      cudaStream_t s)
 {
     if (count == 0) return;
     set_ntt_smem();
     const fr_t *tw = log_n ? twiddles(log_n, inverse, s) : nullptr;
-    const int v = log_n ? ntt_variant(d, log_n, inverse, tw, s) : 1;
-    ntt_transform(d, log_n, count, inverse, tw, v, fac, s);
+    const int v = log_n ? ntt_variant(d, log_n, inverse, tw, status, s) : 1;
+    ntt_transform(d, log_n, count, inverse, tw, v, fac, status, s);
 }
 
-void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, cudaStream_t s)
+void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, uint32_t *status,
+                 cudaStream_t s)
 {
     ntt_factors fac{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
     if (scale) fac = ntt_factors{{*scale, *scale, *scale}, 1};
-    ntt_apply(d, log_n, count, inverse, fac, s);
+    ntt_apply(d, log_n, count, inverse, fac, status, s);
+}
+
+// Forward transforms of `count` polynomials of in_len values at src (count
+// x in_len), zero-padded to 2^log_n, with infac's factor applied to input i:
+// out (count x 2^log_n) = NTT(pad(src[i] * factor(i))), then the output
+// factors `outfac`.  With the staged passes and two or more passes the
+// padding and the input factors are fused into the first pass's gather (no
+// padded copy is written or read); otherwise a prepare kernel writes the
+// padded, scaled input to out first.  src and out may be the same buffer
+// only when in_len = 2^log_n.
+static void ntt_padded(fr_t *out, const fr_t *src, size_t in_len, size_t count, uint32_t log_n,
+                       const ntt_factors &infac, const ntt_factors &outfac, uint32_t *status, cudaStream_t s)
+{
+    if (count == 0) return;
+    set_ntt_smem();
+    const size_t n = (size_t)1 << log_n;
+    const fr_t *tw = log_n ? twiddles(log_n, false, s) : nullptr;
+    const int v = log_n ? ntt_variant(out, log_n, false, tw, status, s) : 1;
+    if (v >= 4 && pass_split(log_n).size() >= 2) {
+        const ntt_input in{src, in_len, infac};
+        ntt_staged(out, log_n, count, false, tw, v == 5 ? 3 : 2, outfac, status, s, &in);
+        return;
+    }
+    c2e_factors_kernel<<<blocks_for(n * count, 256), 256, 0, s>>>(out, src, infac, in_len, n, count);
+    GB_CHECK_LAUNCH();
+    if (log_n) ntt_transform(out, log_n, count, false, tw, v, outfac, status, s);
+}
+
+// The two power tables of mode-2 factors for positions below `len`:
+// factor(i) = scale * shift^i = pw_hi[i >> lo_bits] * pw_lo[i mod 2^lo_bits]
+// with lo_bits = ceil(bits(len - 1) / 2).  Cached per (device, shift,
+// scale, lo_bits); built on stream s the first time.
+namespace {
+std::mutex g_pw_mu;
+std::map<std::string, std::pair<fr_t *, fr_t *>> g_pw;
+}  // namespace
+
+static ntt_factors power_factors(const fr_t &shift, const fr_t &scale, size_t len, cudaStream_t s)
+{
+    uint32_t bits = 0;
+    while (bits < 63 && ((size_t)1 << bits) < len) bits++;
+    const uint32_t lo_bits = (bits + 1) / 2;
+    const size_t n_lo = (size_t)1 << lo_bits, n_hi = (size_t)1 << (bits - lo_bits);
+    std::string key((const char *)&shift, sizeof(fr_t));
+    key.append((const char *)&scale, sizeof(fr_t));
+    key += ":" + std::to_string(current_device()) + ":" + std::to_string(lo_bits) + ":" + std::to_string(n_hi);
+    ntt_factors f{{fr_t::one(), fr_t::one(), fr_t::one()}, 2};
+    f.lo_bits = lo_bits;
+    std::lock_guard<std::mutex> lk(g_pw_mu);
+    auto it = g_pw.find(key);
+    if (it == g_pw.end()) {
+        fr_t *lo = nullptr, *hi = nullptr;
+        GB_CUDA_OK(cudaMalloc(&lo, n_lo * sizeof(fr_t)));
+        GB_CUDA_OK(cudaMalloc(&hi, n_hi * sizeof(fr_t)));
+        fr_t step = shift;  // shift^(2^lo_bits)
+        for (uint32_t b = 0; b < lo_bits; b++) step = step.sqr();
+        powers_table_kernel<<<blocks_for(n_lo, 256), 256, 0, s>>>(lo, shift, fr_t::one(), n_lo);
+        GB_CHECK_LAUNCH();
+        powers_table_kernel<<<blocks_for(n_hi, 256), 256, 0, s>>>(hi, step, scale, n_hi);
+        GB_CHECK_LAUNCH();
+        GB_CUDA_OK(cudaStreamSynchronize(s));
+        it = g_pw.emplace(key, std::make_pair(lo, hi)).first;
+    }
+    f.pw_lo = it->second.first;
+    f.pw_hi = it->second.second;
+    return f;
 }
 
 void launch_mul_assign(fr_t *d, const fr_t &k, size_t len, cudaStream_t s)
@@ -1200,34 +1407,14 @@ void launch_coeff_to_extended_prepare(fr_t *out, const fr_t *in, const fr_t &fir
     GB_CHECK_LAUNCH();
 }
 
-// reads and clears the count of staged-pass CTAs whose twiddle copy did not
-// land within the spin limit, plus the work-queue waits that ran out; throws
-// when there was one
-static uint32_t ntt_take_waits(cudaStream_t s)
-{
-    uint32_t h = 0, zero = 0;
-    uint32_t hq = 0;
-    GB_CUDA_OK(cudaMemcpyFromSymbolAsync(&h, g_ntt_wait_timeouts, sizeof(h), 0, cudaMemcpyDeviceToHost, s));
-    GB_CUDA_OK(cudaMemcpyToSymbolAsync(g_ntt_wait_timeouts, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
-    GB_CUDA_OK(cudaMemcpyFromSymbolAsync(&hq, g_ntt_queue_timeouts, sizeof(hq), 0, cudaMemcpyDeviceToHost, s));
-    GB_CUDA_OK(cudaMemcpyToSymbolAsync(g_ntt_queue_timeouts, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
-    GB_CUDA_OK(cudaStreamSynchronize(s));
-    return h + hq;
-}
-
-static void ntt_check_waits(cudaStream_t s)
-{
-    if (ntt_take_waits(s)) throw cuda_error((int)cudaErrorLaunchTimeout, "NTT twiddle copy did not complete");
-}
-
 // reference NTT semantics: inverse includes 1/n
-static void ntt_ref(fr_t *d, uint32_t log_n, size_t count, bool inverse, cudaStream_t s)
+static void ntt_ref(fr_t *d, uint32_t log_n, size_t count, bool inverse, uint32_t *status, cudaStream_t s)
 {
     if (inverse) {
         fr_t ninv = host_fr_inverse(host_fr_from_u64((uint64_t)1 << log_n));
-        ntt_inplace(d, log_n, count, true, &ninv, s);
+        ntt_inplace(d, log_n, count, true, &ninv, status, s);
     } else {
-        ntt_inplace(d, log_n, count, false, nullptr, s);
+        ntt_inplace(d, log_n, count, false, nullptr, status, s);
     }
 }
 
@@ -1235,12 +1422,52 @@ static void ntt_ref(fr_t *d, uint32_t log_n, size_t count, bool inverse, cudaStr
 // reference's NTT followed by its scale-and-ZETA pass), with the factors
 // applied by the transform's last pass
 static void ntt_ref_zeta(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t &scale, const fr_t &first,
-                         const fr_t &second, cudaStream_t s)
+                         const fr_t &second, uint32_t *status, cudaStream_t s)
 {
     fr_t sc = scale;
     if (inverse) sc = sc * host_fr_inverse(host_fr_from_u64((uint64_t)1 << log_n));
     const ntt_factors fac{{sc, sc * first, sc * second}, 1};
-    ntt_apply(d, log_n, count, inverse, fac, s);
+    ntt_apply(d, log_n, count, inverse, fac, status, s);
+}
+
+// coeff_to_extended (ZETA coset, domain.rs:325-339): count polynomials of
+// input_len coefficients -> evaluations on the 2^ext_log_n extended coset,
+// the distribution a_i [1, first, second][i mod 3] and the zero padding
+// fused into the first NTT pass
+static void c2e_zeta(fr_t *out, const fr_t *in, size_t input_len, size_t count, uint32_t ext_log_n,
+                     const fr_t &first, const fr_t &second, uint32_t *status, cudaStream_t s)
+{
+    const ntt_factors infac{{fr_t::one(), first, second}, 1};
+    const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+    ntt_padded(out, in, input_len, count, ext_log_n, infac, none, status, s);
+}
+
+// the same with the powers of a coset shift: a_i shift^i, zero padding,
+// forward NTT (evaluations on shift * <w_ext>)
+static void c2e_coset(fr_t *out, const fr_t *in, size_t input_len, size_t count, uint32_t ext_log_n,
+                      const fr_t &shift, uint32_t *status, cudaStream_t s)
+{
+    const ntt_factors infac = power_factors(shift, fr_t::one(), input_len, s);
+    const ntt_factors none{{fr_t::one(), fr_t::one(), fr_t::one()}, 0};
+    ntt_padded(out, in, input_len, count, ext_log_n, infac, none, status, s);
+}
+
+// sppark's coset NTT (NTT::Base with Type::coset, NN order;
+// vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:196-209) in place on count
+// polynomials: forward NTT(a_i shift^i), the powers applied by the first
+// pass; inverse iNTT(a)_i shift^-i (the iNTT includes 1/n), the powers and
+// 1/n applied by the last pass
+static void ntt_coset(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t &shift, uint32_t *status,
+                      cudaStream_t s)
+{
+    const size_t n = (size_t)1 << log_n;
+    if (!inverse) {
+        c2e_coset(d, d, n, count, log_n, shift, status, s);
+        return;
+    }
+    const fr_t ninv = host_fr_inverse(host_fr_from_u64((uint64_t)n));
+    const ntt_factors outfac = power_factors(host_fr_inverse(shift), ninv, n, s);
+    ntt_apply(d, log_n, count, true, outfac, status, s);
 }
 
 }  // namespace gb
@@ -1258,12 +1485,12 @@ RustError midnight_sppark_bls12_381_fr_ntt(RawFr *values_raw, uint32_t log_n, bo
     if (!values) return make_error((int)cudaErrorInvalidValue, "null NTT values");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
+    ntt_status st(s);
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
-    ntt_ref(d, log_n, 1, inverse, s);
+    ntt_ref(d, log_n, 1, inverse, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
-    ntt_check_waits(s);
+    st.check();
     return ok();
     GB_ENTRY_END
 }
@@ -1280,12 +1507,12 @@ RustError midnight_sppark_bls12_381_fr_ntt_zeta(RawFr *values_raw, uint32_t log_
     if (log_n > 31 || !values) return make_error((int)cudaErrorInvalidValue, "invalid NTT arguments");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
+    ntt_status st(s);
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
-    ntt_ref_zeta(d, log_n, 1, inverse, scale, first, second, s);
+    ntt_ref_zeta(d, log_n, 1, inverse, scale, first, second, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
-    ntt_check_waits(s);
+    st.check();
     return ok();
     GB_ENTRY_END
 }
@@ -1303,14 +1530,14 @@ RustError midnight_sppark_bls12_381_fr_divide_ntt_zeta(RawFr *values_raw, uint32
     if (log_n > 31 || !values || !factors) return make_error((int)cudaErrorInvalidValue, "invalid NTT arguments");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
+    ntt_status st(s);
     dev_buf<fr_t> d(n, s), f(factor_len, s);
     h2d(d, values, n * sizeof(fr_t), s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(d, f, factor_len, n, s);
-    ntt_ref_zeta(d, log_n, 1, true, scale, first, second, s);
+    ntt_ref_zeta(d, log_n, 1, true, scale, first, second, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
-    ntt_check_waits(s);
+    st.check();
     return ok();
     GB_ENTRY_END
 }
@@ -1329,13 +1556,12 @@ RustError midnight_sppark_bls12_381_fr_coeff_to_extended_batch(RawFr *out_raw, c
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     if (!out || !inputs) return make_error((int)cudaErrorInvalidValue, "null coeff_to_extended buffers");
     cudaStream_t s = lane_stream();
+    ntt_status st(s);
     dev_buf<fr_t> din(input_len * count, s), dout(output_len * count, s);
     h2d(din, inputs, input_len * count * sizeof(fr_t), s);
-    launch_coeff_to_extended_prepare(dout, din, first, second, input_len, output_len, count, s);
-    ntt_ref(dout, extended_log_n, count, false, s);
+    c2e_zeta(dout, din, input_len, count, extended_log_n, first, second, st.ptr(), s);
     d2h(out, dout, output_len * count * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
-    ntt_check_waits(s);
+    st.check();
     return ok();
     GB_ENTRY_END
 }
@@ -1355,12 +1581,13 @@ RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_batch(void **out
     size_t output_len = (size_t)1 << extended_log_n;
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     cudaStream_t s = lane_stream();
+    ntt_status st(s);
     dev_buf<fr_t> din(input_len * count, s);
     h2d(din, inputs, input_len * count * sizeof(fr_t), s);
     fr_device_vec *v = device_vec_new(output_len * count, s);
     try {
-        launch_coeff_to_extended_prepare(v->values, din, first, second, input_len, output_len, count, s);
-        ntt_ref(v->values, extended_log_n, count, false, s);
+        c2e_zeta(v->values, din, input_len, count, extended_log_n, first, second, st.ptr(), s);
+        st.check();
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1388,10 +1615,11 @@ RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_from_device_batc
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     cudaStream_t s = lane_stream();
     device_vec_wait(src, s);
+    ntt_status st(s);
     fr_device_vec *v = device_vec_new(output_len * count, s);
     try {
-        launch_coeff_to_extended_prepare(v->values, src->values, first, second, input_len, output_len, count, s);
-        ntt_ref(v->values, extended_log_n, count, false, s);
+        c2e_zeta(v->values, src->values, input_len, count, extended_log_n, first, second, st.ptr(), s);
+        st.check();
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1417,7 +1645,9 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(void *device_vec, uin
     if (log_n == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_ref_zeta(v->values, log_n, 1, inverse, scale, first, second, s);
+    ntt_status st(s);
+    ntt_ref_zeta(v->values, log_n, 1, inverse, scale, first, second, st.ptr(), s);
+    st.check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1438,7 +1668,9 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(void *device_ve
     if (v->len != n * count) return make_error((int)cudaErrorInvalidValue, "resident NTT batch length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_ref_zeta(v->values, log_n, count, inverse, scale, first, second, s);
+    ntt_status st(s);
+    ntt_ref_zeta(v->values, log_n, count, inverse, scale, first, second, st.ptr(), s);
+    st.check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1471,6 +1703,7 @@ RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, c
     if (count == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
+    ntt_status st(s);
     std::vector<size_t> q_off;
     std::vector<uint32_t> q_log;
     std::vector<ntt_factors> q_fac;
@@ -1478,7 +1711,7 @@ RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, c
         if (log_ns[j] == 0) continue;  // one value: unchanged, as a single call leaves it
         if (log_ns[j] < 3) {
             // 2 or 4 values: the plain path
-            ntt_ref_zeta(v->values + offsets[j], log_ns[j], 1, inverse, scale, first, second, s);
+            ntt_ref_zeta(v->values + offsets[j], log_ns[j], 1, inverse, scale, first, second, st.ptr(), s);
             continue;
         }
         fr_t sc = scale;
@@ -1487,8 +1720,8 @@ RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, c
         q_log.push_back(log_ns[j]);
         q_fac.push_back(ntt_factors{{sc, sc * first, sc * second}, 1});
     }
-    ntt_ragged(v->values, q_off.data(), q_log.data(), q_fac.data(), q_off.size(), inverse, s);
-    ntt_check_waits(s);
+    ntt_ragged(v->values, q_off.data(), q_log.data(), q_fac.data(), q_off.size(), inverse, st.ptr(), s);
+    st.check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1509,10 +1742,12 @@ RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_v
     if (log_n > 31 || v->len != n) return make_error((int)cudaErrorInvalidValue, "resident NTT length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
+    ntt_status st(s);
     dev_buf<fr_t> f(factor_len, s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(v->values, f, factor_len, n, s);
-    ntt_ref_zeta(v->values, log_n, 1, true, scale, first, second, s);
+    ntt_ref_zeta(v->values, log_n, 1, true, scale, first, second, st.ptr(), s);
+    st.check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1522,13 +1757,162 @@ RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_v
 // or autotuned choice.  Process-wide.
 void gb_ntt_variant_set(int variant) { g_variant_forced = variant >= 1 && variant <= 5 ? variant : 0; }
 
-// Staged-pass CTAs, since the last call, whose twiddle copy did not complete
-// within the spin limit (their transform is not valid); the count is reset.
+// Bounded waits (twiddle copies and work-queue waits) that ran out in NTT
+// calls of this process since the last read; every call that saw one
+// returned cudaErrorLaunchTimeout.  The count is reset by the read.
 RustError gb_ntt_wait_timeouts(uint32_t *out)
 {
     if (!out) return make_error((int)cudaErrorInvalidValue, "null output");
+    const unsigned long long v = g_timeouts_seen.exchange(0);
+    *out = v > 0xffffffffull ? 0xffffffffu : (uint32_t)v;
+    return ok();
+}
+
+// Test hook: the poll limit of the first twiddle-copy wait of every staged
+// NTT pass launched from now on (process-wide); negative restores the
+// default.  0 makes the wait give up at once, so the call reports
+// cudaErrorLaunchTimeout; the copy still lands within the CTA's second,
+// longer wait before the CTA moves on.
+void gb_ntt_wait_limit_set(int64_t spins)
+{
+    g_wait_spins_override.store(spins < 0 ? -1 : (spins > 0xffffffffll ? 0xffffffffll : spins));
+}
+
+// ---- coset by the powers of a shift (sppark's coset NTT and LDE form)
+
+// coefficients -> evaluations on the coset shift * <w_ext> of the 2^ext_log_n
+// domain, for count polynomials of input_len coefficients (host buffers):
+// out[p][j] = sum_i in[p][i] (shift w_ext^j)^i.  The reference's sppark
+// distributes the coset generator's powers in its LDE
+// (vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:283-338, kernels.cu:155-230);
+// here the powers and the zero padding are applied by the first NTT pass.
+RustError gb_fr_coeff_to_extended_coset_batch(RawFr *out_raw, const RawFr *inputs_raw, size_t input_len,
+                                              size_t count, uint32_t extended_log_n, RawFr shift_raw)
+{
+    fr_t *out = reinterpret_cast<fr_t *>(out_raw);
+    const fr_t *inputs = reinterpret_cast<const fr_t *>(inputs_raw);
+    const fr_t shift = gb::from_raw(shift_raw);
+    if (input_len == 0 || count == 0) return ok();
     GB_ENTRY_BEGIN
-    *out = ntt_take_waits(lane_stream());
+    if (extended_log_n > 31) return make_error((int)cudaErrorInvalidValue, "extended domain too large");
+    const size_t output_len = (size_t)1 << extended_log_n;
+    if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
+    if (!out || !inputs) return make_error((int)cudaErrorInvalidValue, "null coset LDE buffers");
+    cudaStream_t s = lane_stream();
+    ntt_status st(s);
+    dev_buf<fr_t> din(input_len * count, s), dout(output_len * count, s);
+    h2d(din, inputs, input_len * count * sizeof(fr_t), s);
+    c2e_coset(dout, din, input_len, count, extended_log_n, shift, st.ptr(), s);
+    d2h(out, dout, output_len * count * sizeof(fr_t), s);
+    st.check();
+    return ok();
+    GB_ENTRY_END
+}
+
+// The same from resident coefficients (count polynomials of input_len values
+// at the start of `source`) into a new resident device vector of count x
+// 2^extended_log_n evaluations.
+RustError gb_fr_device_coeff_to_extended_coset_batch(void **out, const void *source, size_t input_len, size_t count,
+                                                     uint32_t extended_log_n, RawFr shift_raw)
+{
+    const fr_t shift = gb::from_raw(shift_raw);
+    if (!out) return make_error((int)cudaErrorInvalidValue, "null device vector output");
+    *out = nullptr;
+    if (!source || input_len == 0 || count == 0)
+        return make_error((int)cudaErrorInvalidValue, "invalid resident coset LDE arguments");
+    GB_ENTRY_BEGIN
+    auto *src = reinterpret_cast<const fr_device_vec *>(source);
+    if (count > SIZE_MAX / input_len || src->len < input_len * count)
+        return make_error((int)cudaErrorInvalidValue, "source device vector too short");
+    if (extended_log_n > 31) return make_error((int)cudaErrorInvalidValue, "extended domain too large");
+    const size_t output_len = (size_t)1 << extended_log_n;
+    if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
+    cudaStream_t s = lane_stream();
+    device_vec_wait(src, s);
+    ntt_status st(s);
+    fr_device_vec *v = device_vec_new(output_len * count, s);
+    try {
+        c2e_coset(v->values, src->values, input_len, count, extended_log_n, shift, st.ptr(), s);
+        st.check();
+        device_vec_mark_ready(v, s);
+    } catch (...) {
+        device_vec_delete(v);
+        throw;
+    }
+    *out = v;
+    return ok();
+    GB_ENTRY_END
+}
+
+// sppark's coset NTT (NTT::Base with Type::coset, natural order in and out;
+// vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:196-209) in place on count
+// resident polynomials of 2^log_n values: forward NTT(a_i shift^i), inverse
+// iNTT(a)_i shift^-i, the iNTT including 1/n.
+RustError gb_fr_device_vec_ntt_coset_batch(void *device_vec, uint32_t log_n, size_t count, bool inverse,
+                                           RawFr shift_raw)
+{
+    const fr_t shift = gb::from_raw(shift_raw);
+    if (!device_vec || count == 0) return make_error((int)cudaErrorInvalidValue, "invalid resident coset NTT arguments");
+    GB_ENTRY_BEGIN
+    auto *v = reinterpret_cast<fr_device_vec *>(device_vec);
+    if (log_n > 31) return make_error((int)cudaErrorInvalidValue, "resident coset NTT size overflow");
+    const size_t n = (size_t)1 << log_n;
+    if (count > SIZE_MAX / n || v->len != n * count)
+        return make_error((int)cudaErrorInvalidValue, "resident coset NTT length mismatch");
+    if (shift.is_zero()) return make_error((int)cudaErrorInvalidValue, "zero coset shift");
+    if (log_n == 0) return ok();
+    cudaStream_t s = lane_stream();
+    device_vec_wait(v, s);
+    ntt_status st(s);
+    ntt_coset(v->values, log_n, count, inverse, shift, st.ptr(), s);
+    st.check();
+    device_vec_mark_ready(v, s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// The same on one host polynomial (sppark NTT::Base(..., Type::coset)).
+RustError gb_fr_ntt_coset(RawFr *values_raw, uint32_t log_n, bool inverse, RawFr shift_raw)
+{
+    fr_t *values = reinterpret_cast<fr_t *>(values_raw);
+    const fr_t shift = gb::from_raw(shift_raw);
+    if (log_n == 0) return ok();
+    GB_ENTRY_BEGIN
+    if (log_n > 31 || !values) return make_error((int)cudaErrorInvalidValue, "invalid coset NTT arguments");
+    if (shift.is_zero()) return make_error((int)cudaErrorInvalidValue, "zero coset shift");
+    const size_t n = (size_t)1 << log_n;
+    cudaStream_t s = lane_stream();
+    ntt_status st(s);
+    dev_buf<fr_t> d(n, s);
+    h2d(d, values, n * sizeof(fr_t), s);
+    ntt_coset(d, log_n, 1, inverse, shift, st.ptr(), s);
+    d2h(values, d, n * sizeof(fr_t), s);
+    st.check();
+    return ok();
+    GB_ENTRY_END
+}
+
+// sppark's NTT::LDE (vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:283-342): the
+// 2^lg_domain_size evaluations at `in` -> the 2^(lg_domain_size +
+// lg_blowup) evaluations at `out` of the same polynomial on the coset of the
+// multiplicative generator 7 (group_gen, parameters/bls12_381.h:11; fq.rs
+// GENERATOR): inverse NTT, then the coset LDE.  Natural order throughout.
+RustError gb_fr_lde_coset(RawFr *out_raw, const RawFr *in_raw, uint32_t lg_domain_size, uint32_t lg_blowup)
+{
+    fr_t *out = reinterpret_cast<fr_t *>(out_raw);
+    const fr_t *in = reinterpret_cast<const fr_t *>(in_raw);
+    GB_ENTRY_BEGIN
+    if (lg_domain_size + lg_blowup > 31 || !out || !in)
+        return make_error((int)cudaErrorInvalidValue, "invalid LDE arguments");
+    const size_t n = (size_t)1 << lg_domain_size, N = n << lg_blowup;
+    cudaStream_t s = lane_stream();
+    ntt_status st(s);
+    dev_buf<fr_t> d(n, s), e(N, s);
+    h2d(d, in, n * sizeof(fr_t), s);
+    if (lg_domain_size) ntt_ref(d, lg_domain_size, 1, true, st.ptr(), s);
+    c2e_coset(e, d, n, 1, lg_domain_size + lg_blowup, host_fr_from_u64(7), st.ptr(), s);
+    d2h(out, e, N * sizeof(fr_t), s);
+    st.check();
     return ok();
     GB_ENTRY_END
 }

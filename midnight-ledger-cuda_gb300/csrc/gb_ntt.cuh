@@ -16,8 +16,11 @@ fr_t host_fr_inverse(const fr_t &a);
 // In-place NTT of `count` contiguous polynomials of length 2^log_n on stream s,
 // natural order in and out (the reference's NN order).  forward: a_k =
 // sum_j a_j w^(jk); inverse uses w^-1 and multiplies by `scale`
-// (pass n^-1 for the reference's inverse, which includes 1/n).
-void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, cudaStream_t s);
+// (pass n^-1 for the reference's inverse, which includes 1/n).  Bounded
+// waits that run out are counted in status[0..1] (device memory the caller
+// owns and zeroes; may be null to not count them).
+void ntt_inplace(fr_t *d, uint32_t log_n, size_t count, bool inverse, const fr_t *scale, uint32_t *status,
+                 cudaStream_t s);
 
 // elementwise helpers (launch on stream s)
 void launch_mul_assign(fr_t *d, const fr_t &k, size_t len, cudaStream_t s);

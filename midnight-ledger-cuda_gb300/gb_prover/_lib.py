@@ -172,6 +172,14 @@ def _declare(L):
         "gb_ntt_variant_set": (None, [ctypes.c_int]),
         "gb_ntt_wait_timeouts": (E, [ctypes.POINTER(ctypes.c_uint32)]),
         "gb_fr_device_vec_ntt_ragged": (E, [vp, vp, vp, sz, b, fr, fr, fr]),
+        "gb_ntt_wait_limit_set": (None, [ctypes.c_int64]),
+        "gb_g1_msm_device": (E, [vp, vp, vp, sz]),
+        "gb_g1_msm_context_device_bytes": (sz, [vp]),
+        "gb_fr_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),
+        "gb_fr_device_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),
+        "gb_fr_device_vec_ntt_coset_batch": (E, [vp, u32, sz, b, fr]),
+        "gb_fr_ntt_coset": (E, [vp, u32, b, fr]),
+        "gb_fr_lde_coset": (E, [vp, vp, u32, u32]),
         "gb_autotune_reset": (None, []),
         "gb_autotune_report": (sz, [vp, sz]),
     }

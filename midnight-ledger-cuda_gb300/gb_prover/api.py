@@ -28,8 +28,15 @@ __all__ = [
     "fr_lookup_permute_device", "NumeratorContext", "bls12_381_fr_multiopen_prepare",
     "bls12_381_fr_multiopen_prepare_device", "bls12_381_fr_multiopen_f_poly_device",
     "bls12_381_fr_multiopen_pi_device", "bls12_381_fr_lookup_permute_batch", "hook_mask_delay",
-    "hook_delayed_scale", "autotune_set", "autotune_reset", "autotune_report",
+    "hook_delayed_scale", "autotune_set", "autotune_reset", "autotune_report", "ntt_wait_limit_set",
+    "FR_GENERATOR", "fr_coeff_to_extended_coset_batch", "fr_device_coeff_to_extended_coset_batch", "fr_ntt_coset",
+    "fr_lde_coset", "g1_msm_device",
 ]
+
+# GENERATOR = 7 (vendor/midnight-curves-0.3.1/src/bls12_381/fq.rs:31-33), Montgomery limbs: the coset
+# generator of sppark's coset NTT and LDE (vendor/sppark-0.1.15/sppark/ntt/parameters/bls12_381.h:11)
+FR_GENERATOR = np.array([0x0000000EFFFFFFF1, 0x17E363D300189C0F, 0xFF9C57876F8457B0, 0x351332208FC5A8C4],
+                        dtype=np.uint64)
 
 PROFILE_MSM_ACCUMULATE, PROFILE_MSM_TOTAL, PROFILE_NTT = 0, 1, 2
 # MSM phases: recode + sort, bucket fix-up, bucket reduction + window combination
@@ -92,6 +99,10 @@ class Bls12_381G1MsmContext:
         check(lib().midnight_sppark_bls12_381_g1_msm_context_create_with_config(ctypes.byref(h), _ptr(p),
                                                                                 len(p), cfg))
         self.raw = h
+
+    def device_bytes(self):
+        """bytes of device memory the context holds (its precomputed table)"""
+        return lib().gb_g1_msm_context_device_bytes(self.raw) if self.raw else 0
 
     def close(self):
         if self.raw:
@@ -227,6 +238,11 @@ class Bls12_381FrDeviceVec:
         check(lib().gb_fr_device_vec_ntt_ragged(self.raw, _ptr(off), _ptr(lg), len(off), inverse, _fr(scale),
                                                 _fr(first), _fr(second)))
 
+    def ntt_coset_batch(self, log_n, count, inverse, shift=FR_GENERATOR):
+        """sppark's coset NTT in place (gb_fr_device_vec_ntt_coset_batch):
+        forward NTT(a_i shift^i), inverse iNTT(a)_i shift^-i."""
+        check(lib().gb_fr_device_vec_ntt_coset_batch(self.raw, log_n, count, inverse, _fr(shift)))
+
     def divide_ntt_zeta(self, log_n, factors, scale, first, second):
         f = _fr_arr(factors)
         check(lib().midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(self.raw, log_n, _ptr(f), len(f),
@@ -291,6 +307,43 @@ def bls12_381_fr_device_coeff_to_extended_batch(inputs, extended_log_n, first, s
                                                                             a.shape[0], extended_log_n, _fr(first),
                                                                             _fr(second)))
     return Bls12_381FrDeviceVec(h)
+
+
+def fr_coeff_to_extended_coset_batch(inputs, extended_log_n, shift=FR_GENERATOR):
+    """coefficients (count, input_len, 4) -> evaluations on shift * <w_ext>,
+    (count, 2^extended_log_n, 4): the coset LDE by the powers of shift."""
+    a = np.ascontiguousarray(inputs, dtype=np.uint64)
+    a = a.reshape(a.shape[0], -1, 4) if a.ndim == 3 else a.reshape(1, -1, 4)
+    count, input_len = a.shape[0], a.shape[1]
+    out = np.zeros((count, 1 << extended_log_n, 4), dtype=np.uint64)
+    check(lib().gb_fr_coeff_to_extended_coset_batch(_ptr(out), _ptr(a), input_len, count, extended_log_n,
+                                                    _fr(shift)))
+    return out
+
+
+def fr_device_coeff_to_extended_coset_batch(source, input_len, count, extended_log_n, shift=FR_GENERATOR):
+    """the same from a resident vector into a new one"""
+    h = ctypes.c_void_p()
+    check(lib().gb_fr_device_coeff_to_extended_coset_batch(ctypes.byref(h), source.raw, input_len, count,
+                                                           extended_log_n, _fr(shift)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def fr_ntt_coset(values, inverse=False, shift=FR_GENERATOR):
+    """sppark NTT::Base(..., Type::coset) on one polynomial"""
+    v = _fr_arr(values).copy()
+    check(lib().gb_fr_ntt_coset(_ptr(v), _log2_exact(len(v)), inverse, _fr(shift)))
+    return v
+
+
+def fr_lde_coset(values, lg_blowup):
+    """sppark NTT::LDE: evaluations -> evaluations on the generator coset of
+    the domain 2^lg_blowup times larger"""
+    v = _fr_arr(values)
+    lg = _log2_exact(len(v))
+    out = np.zeros((len(v) << lg_blowup, 4), dtype=np.uint64)
+    check(lib().gb_fr_lde_coset(_ptr(out), _ptr(v), lg, lg_blowup))
+    return out
 
 
 # ---------------------------------------------------------------- vector ops
@@ -397,6 +450,15 @@ def g1_generator_mul(scalars):
     s = _fr_arr(scalars)
     out = np.zeros((len(s), 12), dtype=np.uint64)
     check(lib().gb_g1_generator_mul(_ptr(out), _ptr(s), len(s)))
+    return out
+
+
+def g1_msm_device(d_points, d_scalars, n):
+    """gb_g1_msm_device: one MSM over n affine bases and n scalars at device
+    addresses d_points / d_scalars (ints, e.g. torch data_ptr()), no
+    precomputed table; the projective result as (18,) uint64."""
+    out = np.zeros(18, dtype=np.uint64)
+    check(lib().gb_g1_msm_device(_ptr(out), ctypes.c_void_p(d_points), ctypes.c_void_p(d_scalars), n))
     return out
 
 
@@ -808,6 +870,12 @@ class NumeratorContext:
 def ntt_variant_set(variant):
     """Force the NTT pass variant (1..5, see gb_ntt_variant_set); 0 = default."""
     lib().gb_ntt_variant_set(int(variant))
+
+
+def ntt_wait_limit_set(spins):
+    """test hook (gb_ntt_wait_limit_set): poll limit of the first twiddle-copy
+    wait; None or negative restores the default"""
+    lib().gb_ntt_wait_limit_set(-1 if spins is None else int(spins))
 
 
 def ntt_wait_timeouts():

@@ -152,6 +152,11 @@ class ParamsKZG:
         gl = g_to_lagrange(g, new_k)
         return ParamsKZG(new_k, g, gl)
 
+    def device_bytes(self):
+        """device memory held by this SRS's resident MSM contexts (their
+        precomputed tables)"""
+        return sum(c.device_bytes() for c in self._ctx.values())
+
     def context(self, lagrange):
         key = bool(lagrange)
         if key not in self._ctx:

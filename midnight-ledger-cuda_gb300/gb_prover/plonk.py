@@ -492,6 +492,10 @@ class ProvingKey:
     forms and extended cosets (backend handles), commitments, and the
     compiled numerator graphs (keygen.rs:307-430)."""
 
+    def device_bytes(self):
+        """device memory held by the key's resident vectors"""
+        return sum(32 * v.len for v in vars(self).values() if hasattr(v, "len") and hasattr(v, "raw"))
+
 
 def keygen(params, circuit, backend, fixed=None, copies=None):
     """keygen_vk + keygen_pk for a synthetic circuit (plonk/keygen.rs:240-430)."""

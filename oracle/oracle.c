@@ -1027,6 +1027,74 @@ int orc_fr_coeff_to_extended_batch(orc_fr *out, const orc_fr *in, size_t input_l
     return 0;
 }
 
+void orc_fr_distribute_powers(orc_fr *a, size_t len, const orc_fr *shift)
+{
+    /* vendor/sppark-0.1.15/sppark/ntt/kernels.cu:133-153 (LDE_distribute_powers):
+     * element i (natural order) times shift^i */
+    INIT();
+    u64 cur[4];
+    memcpy(cur, FR.one, 32);
+    for (size_t i = 0; i < len; i++) {
+        f_mul(a[i].l, a[i].l, cur, &FR);
+        f_mul(cur, cur, shift->l, &FR);
+    }
+}
+
+void orc_fr_ntt_coset(orc_fr *a, uint32_t log_n, int inverse, const orc_fr *shift, int threads)
+{
+    /* vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:196-209 (NTT_internal, Type::coset, NN
+     * order): the forward transform distributes shift^i before the NTT, the
+     * inverse distributes shift^-i after the iNTT (which includes 1/n) */
+    INIT();
+    if (log_n == 0) return;
+    size_t n = (size_t)1 << log_n;
+    if (!inverse) {
+        orc_fr_distribute_powers(a, n, shift);
+        orc_fr_ntt(a, log_n, 0, threads);
+    } else {
+        orc_fr sinv;
+        f_inv(sinv.l, shift->l, &FR);
+        orc_fr_ntt(a, log_n, 1, threads);
+        orc_fr_distribute_powers(a, n, &sinv);
+    }
+}
+
+int orc_fr_coeff_to_extended_coset_batch(orc_fr *out, const orc_fr *in, size_t input_len, size_t count,
+                                         uint32_t ext_log_n, const orc_fr *shift, int threads)
+{
+    /* coefficients -> evaluations on shift * <w_ext>: the coset LDE with the
+     * coset generator's powers (sppark ntt.cuh:283-338 LDE_aux after its iNTT:
+     * LDE_spread_distribute_powers kernels.cu:155-230 multiplies coefficient i
+     * by gen^i and spreads it into the zero-padded extended vector, then the
+     * forward NTT of the extended domain) */
+    INIT();
+    size_t out_len = (size_t)1 << ext_log_n;
+    if (input_len == 0 || count == 0) return 0;
+    if (input_len > out_len) return -1;
+    for (size_t p = 0; p < count; p++) {
+        orc_fr *o = out + p * out_len;
+        memcpy(o, in + p * input_len, sizeof(orc_fr) * input_len);
+        memset(o + input_len, 0, sizeof(orc_fr) * (out_len - input_len));
+        orc_fr_distribute_powers(o, input_len, shift);
+        orc_fr_ntt(o, ext_log_n, 0, threads);
+    }
+    return 0;
+}
+
+void orc_fr_lde_coset(orc_fr *out, const orc_fr *in, uint32_t lg_dsz, uint32_t lg_blowup, int threads)
+{
+    /* vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:283-338 (NTT::LDE): evaluations on
+     * the 2^lg_dsz domain -> coefficients (iNTT) -> coset LDE by the group
+     * generator (parameters/bls12_381.h:11, group_gen = 7 = fq.rs GENERATOR) */
+    INIT();
+    size_t n = (size_t)1 << lg_dsz;
+    orc_fr *coeffs = (orc_fr *)malloc(sizeof(orc_fr) * n);
+    memcpy(coeffs, in, sizeof(orc_fr) * n);
+    orc_fr_ntt(coeffs, lg_dsz, 1, threads);
+    orc_fr_coeff_to_extended_coset_batch(out, coeffs, n, 1, lg_dsz + lg_blowup, &FR_CONST[1], threads);
+    free(coeffs);
+}
+
 uint32_t orc_domain_extended_k(uint32_t j, uint32_t k)
 {
     /* domain.rs:56-68 */

@@ -108,6 +108,18 @@ void orc_fr_divide_ntt_zeta(orc_fr *a, uint32_t log_n, const orc_fr *factors, si
 int orc_fr_coeff_to_extended_batch(orc_fr *out, const orc_fr *in, size_t input_len, size_t count,
                                    uint32_t ext_log_n, const orc_fr *first, const orc_fr *second,
                                    int threads);
+/* a[i] *= shift^i for i < len (sppark LDE_distribute_powers, natural index) */
+void orc_fr_distribute_powers(orc_fr *a, size_t len, const orc_fr *shift);
+/* coset NTT by powers of `shift`, natural order in and out (sppark NTT::Base with
+ * Type::coset): forward = NTT(a_i shift^i); inverse = iNTT(a)_i shift^-i */
+void orc_fr_ntt_coset(orc_fr *a, uint32_t log_n, int inverse, const orc_fr *shift, int threads);
+/* coefficients -> evaluations on the coset shift * <w_ext>: a_i shift^i, zero-pad to
+ * 2^ext_log_n, forward NTT, for `count` polynomials of input_len coefficients */
+int orc_fr_coeff_to_extended_coset_batch(orc_fr *out, const orc_fr *in, size_t input_len, size_t count,
+                                         uint32_t ext_log_n, const orc_fr *shift, int threads);
+/* sppark NTT::LDE: 2^lg_dsz evaluations -> 2^(lg_dsz+lg_blowup) evaluations on the coset
+ * by the multiplicative generator (iNTT, distribute powers, zero-pad, NTT) */
+void orc_fr_lde_coset(orc_fr *out, const orc_fr *in, uint32_t lg_dsz, uint32_t lg_blowup, int threads);
 /* EvaluationDomain::new(j, k) constants: extended_k and t_evaluations (inverted) */
 uint32_t orc_domain_extended_k(uint32_t j, uint32_t k);
 void orc_domain_t_evaluations(orc_fr *out, uint32_t j, uint32_t k); /* 2^(ext_k-k) entries */

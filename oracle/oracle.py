@@ -77,6 +77,10 @@ def _declare(L):
         "orc_fr_ntt_zeta": (None, [vp, u32, i32, vp, vp, vp, i32]),
         "orc_fr_divide_ntt_zeta": (None, [vp, u32, vp, sz, vp, vp, vp, i32]),
         "orc_fr_coeff_to_extended_batch": (i32, [vp, vp, sz, sz, u32, vp, vp, i32]),
+        "orc_fr_distribute_powers": (None, [vp, sz, vp]),
+        "orc_fr_ntt_coset": (None, [vp, u32, i32, vp, i32]),
+        "orc_fr_coeff_to_extended_coset_batch": (i32, [vp, vp, sz, sz, u32, vp, i32]),
+        "orc_fr_lde_coset": (None, [vp, vp, u32, u32, i32]),
         "orc_domain_extended_k": (u32, [u32, u32]),
         "orc_domain_t_evaluations": (None, [vp, u32, u32]),
         "orc_fr_batch_invert": (None, [vp, sz]),
@@ -319,6 +323,42 @@ def fr_coeff_to_extended_batch(inputs, input_len, count, ext_log_n, first, secon
                                               threads or threads_default())
     if rc:
         raise ValueError("coeff_to_extended: input longer than the extended domain")
+    return o
+
+
+def fr_distribute_powers(a, shift):
+    """a[i] * shift^i (sppark LDE_distribute_powers, natural index)"""
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_distribute_powers(_p(a), len(a), _p(np.ascontiguousarray(shift, dtype=np.uint64)))
+    return a
+
+
+def fr_ntt_coset(a, log_n, inverse, shift, threads=None):
+    """sppark NTT::Base with Type::coset, natural order in and out"""
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 4).copy()
+    lib().orc_fr_ntt_coset(_p(a), log_n, int(inverse), _p(np.ascontiguousarray(shift, dtype=np.uint64)),
+                           threads or threads_default())
+    return a
+
+
+def fr_coeff_to_extended_coset_batch(inputs, input_len, count, ext_log_n, shift, threads=None):
+    """coefficients -> evaluations on the coset shift * <w_ext> (powers of shift)"""
+    i = np.ascontiguousarray(inputs, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros((count << ext_log_n, 4), dtype=np.uint64)
+    rc = lib().orc_fr_coeff_to_extended_coset_batch(_p(o), _p(i), input_len, count, ext_log_n,
+                                                    _p(np.ascontiguousarray(shift, dtype=np.uint64)),
+                                                    threads or threads_default())
+    if rc:
+        raise ValueError("coeff_to_extended_coset: input longer than the extended domain")
+    return o
+
+
+def fr_lde_coset(values, lg_dsz, lg_blowup, threads=None):
+    """sppark NTT::LDE: evaluations -> evaluations on the generator coset of the
+    2^(lg_dsz + lg_blowup) domain"""
+    i = np.ascontiguousarray(values, dtype=np.uint64).reshape(-1, 4)
+    o = np.zeros((1 << (lg_dsz + lg_blowup), 4), dtype=np.uint64)
+    lib().orc_fr_lde_coset(_p(o), _p(i), lg_dsz, lg_blowup, threads or threads_default())
     return o
 
 

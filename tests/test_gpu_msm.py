@@ -297,3 +297,22 @@ def test_context_batch_pinned_host_scalars(gb, orc):
     want = ctx.batch(np.array(scalars))
     assert (affine_of(orc, got) == affine_of(orc, want)).all()
     assert (affine_of(orc, got[1:2]) == affine_of(orc, orc.g1_msm(bases, scalars[1])[None])).all()
+
+
+@pytest.mark.parametrize("log_n", [0, 5, 12, 16])
+def test_msm_device_pointers_no_table(gb, orc, log_n):
+    """gb_g1_msm_device on torch-owned device memory equals the oracle."""
+    import torch
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(900 + log_n)
+    n = 1 << log_n if log_n else 0
+    b = gb.g1_generator_mul(orc.fr_random(max(n, 1), rng))[:n]
+    s = orc.fr_random(n, rng)
+    db = torch.from_numpy(b.view(np.int64).copy()).cuda()
+    ds = torch.from_numpy(s.view(np.int64).copy()).cuda()
+    torch.cuda.synchronize()
+    got = gb.g1_msm_device(db.data_ptr(), ds.data_ptr(), n)
+    if n == 0:
+        assert (affine_of(orc, got) == 0).all()
+    else:
+        assert (affine_of(orc, got) == affine_of(orc, orc.g1_msm(b, s))).all()

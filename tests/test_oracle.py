@@ -146,6 +146,54 @@ def test_coeff_to_extended_matches_definition(orc):
         assert out[i] == sum(c * pow(x, j, R) for j, c in enumerate(vals)) % R
 
 
+def test_sppark_group_gen_is_the_generator(orc):
+    # group_gen / group_gen_inverse of vendor/sppark-0.1.15/sppark/ntt/parameters/bls12_381.h:11-12
+    # (the coset generator of sppark's coset NTT and LDE) are GENERATOR = 7 and 1/7 (fq.rs:31-33)
+    gen = [0x0000000EFFFFFFF1, 0x17E363D300189C0F, 0xFF9C57876F8457B0, 0x351332208FC5A8C4]
+    gen_inv = [0xDB6DB6DADB6DB6DC, 0xE6B5824ADB6CC6DA, 0xF8B356E005810DB9, 0x66D0F1E660EC4796]
+    assert orc.fr_to_ints(np.array([gen], dtype=np.uint64))[0] == 7
+    assert orc.fr_to_ints(np.array([gen_inv], dtype=np.uint64))[0] == pow(7, -1, R)
+    assert [int(x) for x in orc.fr_const(orc.CONST_GENERATOR)] == gen
+
+
+@pytest.mark.parametrize("k,ek", [(3, 5), (4, 4), (2, 6)])
+def test_coeff_to_extended_coset_matches_definition(orc, k, ek):
+    """a(X) evaluated at shift * w_ext^i, with the generator 7 and another shift"""
+    vals = [(31 * i + 5) % 65521 for i in range(1 << k)]
+    w = orc.fr_to_ints(orc.fr_omega(ek))[0]
+    for shift in (7, 123456789):
+        sh = orc.fr_from_ints([shift])[0]
+        out = orc.fr_to_ints(orc.fr_coeff_to_extended_coset_batch(orc.fr_from_ints(vals + vals[::-1]), 1 << k,
+                                                                  2, ek, sh))
+        for p, poly in enumerate((vals, vals[::-1])):
+            for i in range(1 << ek):
+                x = shift * pow(w, i, R) % R
+                assert out[(p << ek) + i] == sum(c * pow(x, j, R) for j, c in enumerate(poly)) % R
+
+
+def test_ntt_coset_and_lde_definitions(orc):
+    log_n = 4
+    n = 1 << log_n
+    vals = [(17 * i + 3) % 65521 for i in range(n)]
+    a = orc.fr_from_ints(vals)
+    g = orc.fr_const(orc.CONST_GENERATOR)
+    w = orc.fr_to_ints(orc.fr_omega(log_n))[0]
+    fwd = orc.fr_to_ints(orc.fr_ntt_coset(a, log_n, False, g))
+    # forward coset NTT: evaluations at 7 w^i
+    for i in range(n):
+        x = 7 * pow(w, i, R) % R
+        assert fwd[i] == sum(c * pow(x, j, R) for j, c in enumerate(vals)) % R
+    # the inverse undoes it
+    assert (orc.fr_ntt_coset(orc.fr_ntt_coset(a, log_n, False, g), log_n, True, g) == a).all()
+    # LDE: the evaluations' polynomial on the coset 7 * <w_ext>, blowup 4
+    lde = orc.fr_to_ints(orc.fr_lde_coset(a, log_n, 2))
+    coeffs = orc.fr_to_ints(orc.fr_ntt(a, log_n, True))
+    we = orc.fr_to_ints(orc.fr_omega(log_n + 2))[0]
+    for i in (0, 1, 17, 63):
+        x = 7 * pow(we, i, R) % R
+        assert lde[i] == sum(c * pow(x, j, R) for j, c in enumerate(coeffs)) % R
+
+
 def test_t_evaluations(orc):
     j, k = 4, 3
     ek = orc.domain_extended_k(j, k)
