@@ -490,15 +490,18 @@ GB_API void gb_autotune_set(int enabled);
  * in shared memory by a bulk copy; 0 restores the default (4) or the
  * autotuned choice */
 GB_API void gb_ntt_variant_set(int variant);
-/* bounded waits of NTT calls (staged-pass twiddle copies, work-queue waits)
- * that ran out since the last read, process-wide; every call that saw one
- * returned cudaErrorLaunchTimeout and its output is invalid.  Resets the
- * count.  Each call counts its own waits in a status word it owns. */
+/* bounded waits of NTT work (staged-pass twiddle copies, work-queue waits)
+ * that ran out since the last read, process-wide, after synchronising the
+ * calling lane; resets the count.  A wait that runs out is recorded in its
+ * lane's status word, and the lane's next synchronising call (every call
+ * that returns data to the host, e.g. a download or an MSM) returns
+ * cudaErrorLaunchTimeout: results that depend on it are never returned as
+ * success, as CUDA reports errors of asynchronous work at a later call. */
 GB_API RustError gb_ntt_wait_timeouts(uint32_t *out);
 /* test hook: poll limit of the first twiddle-copy wait of staged NTT passes
  * launched from now on, process-wide (negative = default; 0 = the wait gives
- * up at once and the call returns cudaErrorLaunchTimeout, while the copy
- * still lands in a second, longer wait before the CTA moves on) */
+ * up at once and the error is reported as above, while the copy still lands
+ * in a second, longer wait before the CTA moves on) */
 GB_API void gb_ntt_wait_limit_set(int64_t spins);
 /* ---- coset by the powers of a shift: sppark's coset NTT and LDE form
  * (vendor/sppark-0.1.15/sppark/ntt/ntt.cuh:78-97,196-209,283-342; kernels.cu

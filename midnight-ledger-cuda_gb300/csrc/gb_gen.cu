@@ -90,7 +90,7 @@ const affine_t *generator_table(cudaStream_t s)
     GB_CHECK_LAUNCH();
     gen_table_fill_kernel<<<32, 256, 0, s>>>(bases, table);
     GB_CHECK_LAUNCH();
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     cudaFree(bases);
     g_gen_table[dev] = table;
     return table;
@@ -184,7 +184,7 @@ RustError gb_g1_generator_mul(RawG1Affine *out_raw, const RawFr *scalars_raw, si
     h2d(ds, scalars, n * sizeof(fr_t), s);
     generator_mul_device(dout, ds, n, s);
     d2h(out, dout, n * sizeof(affine_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }

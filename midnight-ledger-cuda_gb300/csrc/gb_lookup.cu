@@ -209,7 +209,7 @@ const char *lookup_permute_core(const fr_t *inputs, const fr_t *tables, size_t i
             }
         }
         d2h(flags, d_flags, 3 * sizeof(int), s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
         if (!flags[2]) break;
     }
     if (flags[0]) return "lookup input value missing from the table";

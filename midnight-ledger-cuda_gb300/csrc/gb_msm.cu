@@ -1089,7 +1089,7 @@ static int tuned_window(const std::vector<msm_item> &items, const affine_t *poin
     GB_CHECK_LAUNCH();
     unsigned h[2] = {0, 0};
     d2h(h, counts, sizeof(h), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     auto cls = [&](unsigned v) { return v * 20 < sample ? 0 : (v * 10 < sample * 3 ? 1 : 2); };
     int lg = 0;
     while (((size_t)1 << (lg + 1)) <= n_max) lg++;
@@ -1124,7 +1124,7 @@ static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *
     for (size_t m = 0; m < nmsms; m++) items.push_back(msm_item{d_scalars.get() + m * n, n, 0});
     msm_run_batch(items, tuned_window(items, d_points, 0, s), false, d_points, 0, d_out, s);
     d2h(out, d_out, nmsms * sizeof(jacobian_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     timed_collect();
 }
 
@@ -1160,7 +1160,7 @@ static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const st
     std::vector<jacobian_t> hb(big.size()), hs(small.size());
     d2h(hb.data(), d_big, big.size() * sizeof(jacobian_t), s);
     d2h(hs.data(), d_small, small.size() * sizeof(jacobian_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     for (size_t i = 0; i < big.size(); i++) out_host[big_idx[i]] = hb[i];
     for (size_t i = 0; i < small.size(); i++) out_host[small_idx[i]] = hs[i];
     timed_collect();
@@ -1227,7 +1227,7 @@ RustError gb_g1_msm_device(RawG1Projective *out_raw, const RawG1Affine *d_points
     std::vector<msm_item> items{msm_item{d_scalars, n, 0}};
     msm_run_batch(items, tuned_window(items, d_points, 0, s), false, d_points, 0, d_out, s);
     d2h(out, d_out, sizeof(jacobian_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     timed_collect();
     return ok();
     GB_ENTRY_END
@@ -1275,7 +1275,7 @@ RustError midnight_sppark_bls12_381_g1_msm_context_create_with_config(void **out
                                                                            ctx->nwin);
             GB_CHECK_LAUNCH();
         }
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         if (ctx->table) cudaFree(ctx->table);
         delete ctx;
@@ -1424,7 +1424,7 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_scrambled_batch(RawG1P
     dev_buf<fr_t> masked(count, s);
     if (t_mask_delay_ms) {
         GB_CUDA_OK(cudaMemsetAsync(masked.get(), 0, count * sizeof(fr_t), s));
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
         stream_host_delay(s, t_mask_delay_ms);
     }
     add_mask_kernel<<<blocks_for(count, 256), 256, 0, s>>>(masked, dv->values + scalar_offset, mv->values, npoints,

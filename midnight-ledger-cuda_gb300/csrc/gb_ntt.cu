@@ -925,34 +925,12 @@ static unsigned wait_spins()
     return v < 0 ? kWaitSpins : (unsigned)v;
 }
 
-// Bounded waits that ran out in NTT calls since the last gb_ntt_wait_timeouts
-// (each such call also returned an error).
-static std::atomic<unsigned long long> g_timeouts_seen{0};
-
-// The status words of one NTT call on stream s, in memory the call owns:
-// [0] staged-pass CTAs whose twiddle copy did not land within the wait
-// limit, [1] work-queue waits that ran out.  check() waits for the call's
-// work and throws cudaErrorLaunchTimeout when either is non-zero (the
-// transform is then not valid).
+// The calling lane's wait-status words (see lane_status_device), which the
+// kernels of an NTT call add to when a bounded wait runs out.
 struct ntt_status {
-    dev_buf<uint32_t> w;
-    cudaStream_t s;
-    explicit ntt_status(cudaStream_t st) : w(2, st), s(st)
-    {
-        GB_CUDA_OK(cudaMemsetAsync(w.get(), 0, 2 * sizeof(uint32_t), s));
-    }
-    uint32_t *ptr() const { return w.get(); }
-    void check()
-    {
-        uint32_t h[2] = {0, 0};
-        GB_CUDA_OK(cudaMemcpyAsync(h, w.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
-        GB_CUDA_OK(cudaStreamSynchronize(s));
-        if (h[0] || h[1]) {
-            g_timeouts_seen.fetch_add((unsigned long long)h[0] + h[1]);
-            throw cuda_error((int)cudaErrorLaunchTimeout,
-                             h[0] ? "NTT twiddle copy did not complete" : "NTT work-queue wait ran out");
-        }
-    }
+    uint32_t *p;
+    ntt_status() : p(lane_status_device()) {}
+    uint32_t *ptr() const { return p; }
 };
 
 namespace {
@@ -1485,12 +1463,12 @@ RustError midnight_sppark_bls12_381_fr_ntt(RawFr *values_raw, uint32_t log_n, bo
     if (!values) return make_error((int)cudaErrorInvalidValue, "null NTT values");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
     ntt_ref(d, log_n, 1, inverse, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1507,12 +1485,12 @@ RustError midnight_sppark_bls12_381_fr_ntt_zeta(RawFr *values_raw, uint32_t log_
     if (log_n > 31 || !values) return make_error((int)cudaErrorInvalidValue, "invalid NTT arguments");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
     ntt_ref_zeta(d, log_n, 1, inverse, scale, first, second, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1530,14 +1508,14 @@ RustError midnight_sppark_bls12_381_fr_divide_ntt_zeta(RawFr *values_raw, uint32
     if (log_n > 31 || !values || !factors) return make_error((int)cudaErrorInvalidValue, "invalid NTT arguments");
     size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> d(n, s), f(factor_len, s);
     h2d(d, values, n * sizeof(fr_t), s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(d, f, factor_len, n, s);
     ntt_ref_zeta(d, log_n, 1, true, scale, first, second, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1556,12 +1534,12 @@ RustError midnight_sppark_bls12_381_fr_coeff_to_extended_batch(RawFr *out_raw, c
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     if (!out || !inputs) return make_error((int)cudaErrorInvalidValue, "null coeff_to_extended buffers");
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> din(input_len * count, s), dout(output_len * count, s);
     h2d(din, inputs, input_len * count * sizeof(fr_t), s);
     c2e_zeta(dout, din, input_len, count, extended_log_n, first, second, st.ptr(), s);
     d2h(out, dout, output_len * count * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1581,13 +1559,13 @@ RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_batch(void **out
     size_t output_len = (size_t)1 << extended_log_n;
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> din(input_len * count, s);
     h2d(din, inputs, input_len * count * sizeof(fr_t), s);
     fr_device_vec *v = device_vec_new(output_len * count, s);
     try {
         c2e_zeta(v->values, din, input_len, count, extended_log_n, first, second, st.ptr(), s);
-        st.check();
+        lane_check();
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1615,11 +1593,11 @@ RustError midnight_sppark_bls12_381_fr_device_coeff_to_extended_from_device_batc
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     cudaStream_t s = lane_stream();
     device_vec_wait(src, s);
-    ntt_status st(s);
+    ntt_status st;
     fr_device_vec *v = device_vec_new(output_len * count, s);
     try {
         c2e_zeta(v->values, src->values, input_len, count, extended_log_n, first, second, st.ptr(), s);
-        st.check();
+        lane_check();
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1645,9 +1623,9 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta(void *device_vec, uin
     if (log_n == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_status st(s);
+    ntt_status st;
     ntt_ref_zeta(v->values, log_n, 1, inverse, scale, first, second, st.ptr(), s);
-    st.check();
+    lane_check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1668,9 +1646,9 @@ RustError midnight_sppark_bls12_381_fr_device_vec_ntt_zeta_batch(void *device_ve
     if (v->len != n * count) return make_error((int)cudaErrorInvalidValue, "resident NTT batch length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_status st(s);
+    ntt_status st;
     ntt_ref_zeta(v->values, log_n, count, inverse, scale, first, second, st.ptr(), s);
-    st.check();
+    lane_check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1703,7 +1681,7 @@ RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, c
     if (count == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_status st(s);
+    ntt_status st;
     std::vector<size_t> q_off;
     std::vector<uint32_t> q_log;
     std::vector<ntt_factors> q_fac;
@@ -1721,7 +1699,7 @@ RustError gb_fr_device_vec_ntt_ragged(void *device_vec, const size_t *offsets, c
         q_fac.push_back(ntt_factors{{sc, sc * first, sc * second}, 1});
     }
     ntt_ragged(v->values, q_off.data(), q_log.data(), q_fac.data(), q_off.size(), inverse, st.ptr(), s);
-    st.check();
+    lane_check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1742,12 +1720,12 @@ RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_v
     if (log_n > 31 || v->len != n) return make_error((int)cudaErrorInvalidValue, "resident NTT length mismatch");
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> f(factor_len, s);
     h2d(f, factors, factor_len * sizeof(fr_t), s);
     launch_mul_assign_repeating(v->values, f, factor_len, n, s);
     ntt_ref_zeta(v->values, log_n, 1, true, scale, first, second, st.ptr(), s);
-    st.check();
+    lane_check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1757,15 +1735,24 @@ RustError midnight_sppark_bls12_381_fr_device_vec_divide_ntt_zeta(void *device_v
 // or autotuned choice.  Process-wide.
 void gb_ntt_variant_set(int variant) { g_variant_forced = variant >= 1 && variant <= 5 ? variant : 0; }
 
-// Bounded waits (twiddle copies and work-queue waits) that ran out in NTT
-// calls of this process since the last read; every call that saw one
-// returned cudaErrorLaunchTimeout.  The count is reset by the read.
+// Bounded waits (twiddle copies and work-queue waits) of NTT work that ran
+// out since the last read, process-wide; the calling lane is synchronised
+// first so its own pending work is counted.  Each was (or, on another lane,
+// will be) reported as cudaErrorLaunchTimeout by its lane's next
+// synchronising call.  The count is reset by the read.
 RustError gb_ntt_wait_timeouts(uint32_t *out)
 {
     if (!out) return make_error((int)cudaErrorInvalidValue, "null output");
-    const unsigned long long v = g_timeouts_seen.exchange(0);
+    GB_ENTRY_BEGIN
+    try {
+        lane_sync(lane_stream());
+    } catch (const cuda_error &e) {
+        if (e.code() != (int)cudaErrorLaunchTimeout) throw;
+    }
+    const unsigned long long v = lane_timeouts_take();
     *out = v > 0xffffffffull ? 0xffffffffu : (uint32_t)v;
     return ok();
+    GB_ENTRY_END
 }
 
 // Test hook: the poll limit of the first twiddle-copy wait of every staged
@@ -1799,12 +1786,12 @@ RustError gb_fr_coeff_to_extended_coset_batch(RawFr *out_raw, const RawFr *input
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     if (!out || !inputs) return make_error((int)cudaErrorInvalidValue, "null coset LDE buffers");
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> din(input_len * count, s), dout(output_len * count, s);
     h2d(din, inputs, input_len * count * sizeof(fr_t), s);
     c2e_coset(dout, din, input_len, count, extended_log_n, shift, st.ptr(), s);
     d2h(out, dout, output_len * count * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1829,11 +1816,11 @@ RustError gb_fr_device_coeff_to_extended_coset_batch(void **out, const void *sou
     if (input_len > output_len) return make_error(-1, "input length exceeds extended domain length");
     cudaStream_t s = lane_stream();
     device_vec_wait(src, s);
-    ntt_status st(s);
+    ntt_status st;
     fr_device_vec *v = device_vec_new(output_len * count, s);
     try {
         c2e_coset(v->values, src->values, input_len, count, extended_log_n, shift, st.ptr(), s);
-        st.check();
+        lane_check();
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1863,9 +1850,9 @@ RustError gb_fr_device_vec_ntt_coset_batch(void *device_vec, uint32_t log_n, siz
     if (log_n == 0) return ok();
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    ntt_status st(s);
+    ntt_status st;
     ntt_coset(v->values, log_n, count, inverse, shift, st.ptr(), s);
-    st.check();
+    lane_check();
     device_vec_mark_ready(v, s);
     return ok();
     GB_ENTRY_END
@@ -1882,12 +1869,12 @@ RustError gb_fr_ntt_coset(RawFr *values_raw, uint32_t log_n, bool inverse, RawFr
     if (shift.is_zero()) return make_error((int)cudaErrorInvalidValue, "zero coset shift");
     const size_t n = (size_t)1 << log_n;
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> d(n, s);
     h2d(d, values, n * sizeof(fr_t), s);
     ntt_coset(d, log_n, 1, inverse, shift, st.ptr(), s);
     d2h(values, d, n * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1906,13 +1893,13 @@ RustError gb_fr_lde_coset(RawFr *out_raw, const RawFr *in_raw, uint32_t lg_domai
         return make_error((int)cudaErrorInvalidValue, "invalid LDE arguments");
     const size_t n = (size_t)1 << lg_domain_size, N = n << lg_blowup;
     cudaStream_t s = lane_stream();
-    ntt_status st(s);
+    ntt_status st;
     dev_buf<fr_t> d(n, s), e(N, s);
     h2d(d, in, n * sizeof(fr_t), s);
     if (lg_domain_size) ntt_ref(d, lg_domain_size, 1, true, st.ptr(), s);
     c2e_coset(e, d, n, 1, lg_domain_size + lg_blowup, host_fr_from_u64(7), st.ptr(), s);
     d2h(out, e, N * sizeof(fr_t), s);
-    st.check();
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }

@@ -260,7 +260,7 @@ RustError midnight_sppark_bls12_381_fr_device_eval_polys(RawFr *out_raw, const v
     dev_buf<fr_t> d(poly_count, s);
     eval_polys(d, v->values, poly_len, poly_count, from_raw(point_raw), s);
     d2h(out_raw, d, poly_count * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -288,7 +288,7 @@ RustError gb_fr_device_eval_many(RawFr *out_raw, const void *const *vecs, const 
     dev_buf<fr_t> d_out(total, s);
     eval_pairs(d_out, pairs, points_raw, requests, poly_len, s);
     d2h(out_raw, d_out, total * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -350,7 +350,7 @@ RustError midnight_sppark_bls12_381_fr_multiopen_prepare(
                            q_items_len, points, point_count, query_poly_indices, query_point_indices, query_count, s);
     d2h(q_out, d_q, poly_len * q_count * sizeof(fr_t), s);
     d2h(eval_out, d_eval, query_count * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -399,7 +399,7 @@ RustError midnight_sppark_bls12_381_fr_multiopen_prepare_device(
         device_vec_mark_ready(q, s);
         if (q_out) d2h(q_out, q->values, poly_len * q_count * sizeof(fr_t), s);
         d2h(eval_out, d_eval, query_count * sizeof(fr_t), s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         device_vec_delete(q);
         throw;

@@ -9,6 +9,8 @@
 // list (uniform control flow, broadcast loads), with its intermediates in a
 // per-thread local array sized to the graph.
 #include <algorithm>
+#include <functional>
+#include <mutex>
 #include <memory>
 #include <vector>
 
@@ -26,7 +28,20 @@ struct dgraph {
     const RawValueSource *parts;
     uint32_t nparts;
     uint32_t ninter;
+    // the same program with its intermediates given slots by liveness
+    // (compile_graph): kind-1 sources name a slot, a target of kNoSlot is
+    // not stored; nslots = kNoSlot when the graph needs more slots than a
+    // block's shared memory holds (the kernels then interpret `calcs`)
+    const RawCalculation *ccalcs;
+    const RawValueSource *cparts;
+    uint32_t nslots;
 };
+
+static constexpr uint32_t kNoSlot = 0xffffffffu;
+// slots of one row in shared memory: 128 rows a block x 48 slots x 32 B
+// = 192 KB at most
+static constexpr uint32_t kMaxSlots = 48;
+static constexpr unsigned kNumThreads = 128;
 
 struct num_params {
     fr_t *out;
@@ -91,7 +106,7 @@ __device__ fr_t source_value(const RawValueSource &src, const dgraph &g, const n
     case 0:
         return src.a < g.nconst ? g.constants[src.a] : fr_t::zero();
     case 1:
-        return src.a < MAX ? inter[src.a] : fr_t::zero();
+        return src.a < MAX && src.a < g.ninter ? inter[src.a] : fr_t::zero();
     case 2:
     case 3:
     case 4: {
@@ -166,20 +181,133 @@ __device__ fr_t evaluate_graph(const dgraph &g, const num_params &p, size_t idx,
             v = fr_t::zero();
             break;
         }
-        if (calc.target < MAX) inter[calc.target] = v;
+        if (calc.target < nint) inter[calc.target] = v;
         last = v;
     }
     return last;
 }
 
-template <int MAX>
+// Products of the interpreted graphs go through the out-of-line Fr product:
+// one copy of its code instead of one per call site keeps the interpreter's
+// loop and the argument terms small enough for the instruction cache.
+__device__ __forceinline__ fr_t qmul(const fr_t &a, const fr_t &b)
+{
+#if defined(__CUDA_ARCH__) && !defined(GB_FP_MUL_INLINE)
+    return fr_t::mul_by_value(a, b);
+#else
+    return a * b;
+#endif
+}
+
+// A row's slots: slot k of the calling thread at sh[k * blockDim.x].
+__device__ __forceinline__ fr_t slot_ld(const fr_t *sh, uint32_t k) { return sh[(size_t)k * blockDim.x]; }
+__device__ __forceinline__ void slot_st(fr_t *sh, uint32_t k, const fr_t &v) { sh[(size_t)k * blockDim.x] = v; }
+
+__device__ fr_t source_value_slots(const RawValueSource &src, const dgraph &g, const num_params &p, size_t idx,
+                                   const fr_t *sh, const fr_t &prev)
+{
+    switch (src.kind) {
+    case 0:
+        return src.a < g.nconst ? g.constants[src.a] : fr_t::zero();
+    case 1:
+        return slot_ld(sh, src.a);
+    case 2:
+    case 3:
+    case 4: {
+        const fr_t *base = column_base(p, src.kind - 2, src.a);
+        if (!base || src.b >= g.nrot) return fr_t::zero();
+        return base[rot_index(idx, g.rotations[src.b], p.rot_scale, p.len)];
+    }
+    case 5:
+        return src.a < p.challenge_len ? p.challenges[src.a] : fr_t::zero();
+    case 6:
+        return p.beta;
+    case 7:
+        return p.gamma;
+    case 8:
+        return p.theta;
+    case 9:
+        return p.trash;
+    case 10:
+        return p.y;
+    case 11:
+        return prev;
+    default:
+        return fr_t::zero();
+    }
+}
+
+// evaluate_graph over the compiled program: intermediates live in the row's
+// shared-memory slots, so nothing goes to local memory
+__device__ fr_t evaluate_graph_slots(const dgraph &g, const num_params &p, size_t idx, const fr_t &prev, fr_t *sh)
+{
+    fr_t last = fr_t::zero();
+    for (uint32_t c = 0; c < g.ncalc; c++) {
+        const RawCalculation calc = g.ccalcs[c];
+        const fr_t a = source_value_slots(calc.lhs, g, p, idx, sh, prev);
+        fr_t v;
+        switch (calc.op) {
+        case 0:
+            v = a + source_value_slots(calc.rhs, g, p, idx, sh, prev);
+            break;
+        case 1:
+            v = a - source_value_slots(calc.rhs, g, p, idx, sh, prev);
+            break;
+        case 2:
+            v = qmul(a, source_value_slots(calc.rhs, g, p, idx, sh, prev));
+            break;
+        case 3:
+            v = qmul(a, a);
+            break;
+        case 4:
+            v = a.dbl();
+            break;
+        case 5:
+            v = -a;
+            break;
+        case 6: {
+            const fr_t factor = source_value_slots(calc.rhs, g, p, idx, sh, prev);
+            v = a;
+            for (uint32_t k = 0; k < calc.parts_len; k++) {
+                const uint32_t pi = calc.parts_offset + k;
+                const fr_t part = pi < g.nparts ? source_value_slots(g.cparts[pi], g, p, idx, sh, prev) : fr_t::zero();
+                v = qmul(v, factor) + part;
+            }
+            break;
+        }
+        case 7:
+            v = a;
+            break;
+        default:
+            v = fr_t::zero();
+            break;
+        }
+        if (calc.target != kNoSlot) slot_st(sh, calc.target, v);
+        last = v;
+    }
+    return last;
+}
+
+// The graph of a row: the compiled program when SLOTS, else the interpreter
+// with a local array of MAX intermediates.
+template <int MAX, bool SLOTS>
+__device__ __forceinline__ fr_t eval_row_graph(const dgraph &g, const num_params &p, size_t idx, const fr_t &prev,
+                                               fr_t *sh)
+{
+    if (SLOTS) return evaluate_graph_slots(g, p, idx, prev, sh);
+    return evaluate_graph<MAX>(g, p, idx, prev);
+}
+
+template <int MAX, bool SLOTS = false>
 __global__ void numerator_kernel(num_params p)
 {
+    extern __shared__ fr_t num_slots[];
+    fr_t *sh = num_slots + threadIdx.x;
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= p.len) return;
     const fr_t one = fr_t::one();
     const fr_t zero = fr_t::zero();
-    fr_t value = p.run_custom ? evaluate_graph<MAX>(p.custom, p, idx, zero) : p.initial[idx];
+    fr_t value = p.run_custom ? eval_row_graph<MAX, SLOTS>(p.custom, p, idx, zero, sh) : p.initial[idx];
 
     if (p.perm_sets && p.chunk_len) {
         // permutation argument (evaluation.rs:3282-3352)
@@ -221,7 +349,7 @@ __global__ void numerator_kernel(num_params p)
         const fr_t *prod = p.lk_product + n * len;
         const fr_t *pin = p.lk_input + n * p.lk_stride;
         const fr_t *ptab = p.lk_table + n * p.lk_stride;
-        const fr_t table_value = evaluate_graph<MAX>(p.lookup_graphs[n], p, idx, zero);
+        const fr_t table_value = eval_row_graph<MAX, SLOTS>(p.lookup_graphs[n], p, idx, zero, sh);
         const fr_t a_minus_s = pin[idx] - ptab[idx];
         const fr_t l0 = p.l0[idx], l_active = p.l_active[idx];
         value = value * p.y + (one - prod[idx]) * l0;
@@ -236,19 +364,20 @@ __global__ void numerator_kernel(num_params p)
         // trash argument (evaluation.rs:3489-3521)
         const uint32_t sel = p.trash_sel[n];
         if (sel >= p.fixed_cols) continue;
-        const fr_t compressed = evaluate_graph<MAX>(p.trash_graphs[n], p, idx, zero);
+        const fr_t compressed = eval_row_graph<MAX, SLOTS>(p.trash_graphs[n], p, idx, zero, sh);
         const fr_t q = p.fixed[(size_t)sel * p.len + idx];
         value = value * p.y + (compressed - (one - q) * p.trash_cosets[n * p.len + idx]);
     }
     p.out[idx] = value;
 }
 
-template <int MAX>
+template <int MAX, bool SLOTS = false>
 __global__ void graph_batch_kernel(num_params p, fr_t *out)
 {
+    extern __shared__ fr_t num_slots[];
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= p.len) return;
-    out[idx] = evaluate_graph<MAX>(p.custom, p, idx, fr_t::zero());
+    out[idx] = eval_row_graph<MAX, SLOTS>(p.custom, p, idx, fr_t::zero(), num_slots + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- host
@@ -256,10 +385,128 @@ __global__ void graph_batch_kernel(num_params p, fr_t *out)
 struct graph_upload {
     dev_buf<fr_t> constants;
     dev_buf<int32_t> rotations;
-    dev_buf<RawCalculation> calcs;
-    dev_buf<RawValueSource> parts;
+    dev_buf<RawCalculation> calcs, ccalcs;
+    dev_buf<RawValueSource> parts, cparts;
     dgraph g{};
 };
+
+static int capacity_for(uint32_t n);
+
+// Gives the graph's intermediates slots by liveness, for the slot
+// interpreter: every write of an intermediate starts a new value, which
+// takes the lowest free slot and holds it until its last read (a value never
+// read takes none).  Reads follow the interpreter exactly: an intermediate
+// not yet written, or with an index at or above num_intermediates, reads
+// zero; a target at or above num_intermediates is not stored.  Operands are
+// read before the target is written, so a target may take a slot that one of
+// its own operands frees.  Returns the slots used, or kNoSlot if more than
+// kMaxSlots would be live at once.
+static uint32_t compile_graph(const RawGraph &raw, std::vector<RawCalculation> &out_calcs,
+                              std::vector<RawValueSource> &out_parts)
+{
+    const uint32_t cap = raw.num_intermediates;
+    const size_t nc = raw.calculations_len;
+    // the sources each calculation reads, as the interpreter reads them
+    auto reads = [&](const RawCalculation &c, std::vector<const RawValueSource *> &r) {
+        r.clear();
+        switch (c.op) {
+        case 0: case 1: case 2: r.push_back(&c.lhs); r.push_back(&c.rhs); break;
+        case 3: case 4: case 5: case 7: r.push_back(&c.lhs); break;
+        case 6:
+            r.push_back(&c.rhs);
+            r.push_back(&c.lhs);
+            for (uint32_t k = 0; k < c.parts_len; k++) {
+                const uint64_t pi = (uint64_t)c.parts_offset + k;
+                if (pi < raw.horner_parts_len) r.push_back(&raw.horner_parts[pi]);
+            }
+            break;
+        default: break;
+        }
+    };
+    // pass 1: versions and their last reads
+    std::vector<int64_t> cur(cap, -1), last_read;
+    std::vector<int64_t> ver_of(nc, -1);
+    std::vector<const RawValueSource *> r;
+    for (size_t c = 0; c < nc; c++) {
+        const RawCalculation &calc = raw.calculations[c];
+        reads(calc, r);
+        for (const RawValueSource *v : r)
+            if (v->kind == 1 && v->a < cap && cur[v->a] >= 0) last_read[cur[v->a]] = (int64_t)c;
+        if (calc.target < cap) {
+            ver_of[c] = (int64_t)last_read.size();
+            cur[calc.target] = ver_of[c];
+            last_read.push_back(-1);
+        }
+    }
+    // pass 2: slots
+    std::fill(cur.begin(), cur.end(), -1);
+    std::vector<uint32_t> slot_of(last_read.size(), kNoSlot);
+    std::vector<uint32_t> free_slots;  // a min-heap by slot number
+    uint32_t nslots = 0;
+    auto take = [&]() {
+        if (free_slots.empty()) return nslots++;
+        std::pop_heap(free_slots.begin(), free_slots.end(), std::greater<uint32_t>());
+        const uint32_t k = free_slots.back();
+        free_slots.pop_back();
+        return k;
+    };
+    auto give = [&](uint32_t k) {
+        free_slots.push_back(k);
+        std::push_heap(free_slots.begin(), free_slots.end(), std::greater<uint32_t>());
+    };
+    auto map_src = [&](const RawValueSource &v) {
+        RawValueSource o = v;
+        if (v.kind == 1) {
+            if (v.a < cap && cur[v.a] >= 0) {
+                o.a = slot_of[cur[v.a]];
+            } else {
+                o.kind = 0;  // reads zero: an out-of-range constant index
+                o.a = kNoSlot;
+            }
+        }
+        return o;
+    };
+    out_calcs.resize(nc);
+    out_parts.clear();
+    for (size_t c = 0; c < nc; c++) {
+        const RawCalculation &calc = raw.calculations[c];
+        RawCalculation o = calc;
+        o.lhs = map_src(calc.lhs);
+        o.rhs = map_src(calc.rhs);
+        if (calc.op == 6) {
+            o.parts_offset = (uint32_t)out_parts.size();
+            for (uint32_t k = 0; k < calc.parts_len; k++) {
+                const uint64_t pi = (uint64_t)calc.parts_offset + k;
+                if (pi < raw.horner_parts_len) {
+                    out_parts.push_back(map_src(raw.horner_parts[pi]));
+                } else {
+                    RawValueSource z{0, kNoSlot, 0};
+                    out_parts.push_back(z);
+                }
+            }
+        }
+        // values whose last read is this calculation free their slots
+        reads(calc, r);
+        std::vector<int64_t> done;
+        for (const RawValueSource *v : r)
+            if (v->kind == 1 && v->a < cap && cur[v->a] >= 0 && last_read[cur[v->a]] == (int64_t)c)
+                done.push_back(cur[v->a]);
+        std::sort(done.begin(), done.end());
+        done.erase(std::unique(done.begin(), done.end()), done.end());
+        for (int64_t v : done) give(slot_of[v]);
+        o.target = kNoSlot;
+        if (ver_of[c] >= 0) {
+            const int64_t v = ver_of[c];
+            if (last_read[v] >= 0) {
+                slot_of[v] = take();
+                o.target = slot_of[v];
+            }
+            cur[calc.target] = v;
+        }
+        out_calcs[c] = o;
+    }
+    return nslots > kMaxSlots ? kNoSlot : nslots;
+}
 
 static void upload_graph(graph_upload &u, const RawGraph &raw, cudaStream_t s)
 {
@@ -283,6 +530,38 @@ static void upload_graph(graph_upload &u, const RawGraph &raw, cudaStream_t s)
     u.g.parts = u.parts;
     u.g.nparts = (uint32_t)raw.horner_parts_len;
     u.g.ninter = raw.num_intermediates;
+    u.g.nslots = kNoSlot;
+    if (capacity_for(raw.num_intermediates)) {
+        std::vector<RawCalculation> cc;
+        std::vector<RawValueSource> cp;
+        const uint32_t ns = compile_graph(raw, cc, cp);
+        if (ns != kNoSlot) {
+            u.ccalcs = dev_buf<RawCalculation>(cc.size(), s);
+            u.cparts = dev_buf<RawValueSource>(cp.size(), s);
+            h2d(u.ccalcs, cc.data(), cc.size() * sizeof(RawCalculation), s);
+            h2d(u.cparts, cp.data(), cp.size() * sizeof(RawValueSource), s);
+            u.g.ccalcs = u.ccalcs;
+            u.g.cparts = u.cparts;
+            u.g.nslots = ns;
+        }
+    }
+}
+
+// the slot count a launch over these graphs needs: kNoSlot when one of them
+// could not be compiled
+static uint32_t slots_for(uint32_t acc, const dgraph &g)
+{
+    return acc == kNoSlot || g.nslots == kNoSlot ? kNoSlot : std::max(acc, g.nslots);
+}
+
+static void set_slot_smem()
+{
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const int bytes = (int)(kNumThreads * kMaxSlots * sizeof(fr_t));
+        cudaFuncSetAttribute(numerator_kernel<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(graph_batch_kernel<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    });
 }
 
 static int capacity_for(uint32_t n)
@@ -314,25 +593,39 @@ static dev_buf<fr_t> upload_fr(const RawFr *h, size_t n, cudaStream_t s)
 // host) into d_out + gi * p.len; p carries the columns and challenges
 static void graph_batch_launch(fr_t *d_out, num_params p, const dgraph *graphs, size_t graph_count, cudaStream_t s)
 {
-    const unsigned grid = blocks_for(p.len, 128);
+    set_slot_smem();
+    const unsigned grid = blocks_for(p.len, kNumThreads);
     for (size_t gi = 0; gi < graph_count; gi++) {
         p.custom = graphs[gi];
         fr_t *o = d_out + gi * p.len;
-        launch_by_capacity(
-            capacity_for(graphs[gi].ninter), [&] { graph_batch_kernel<16><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<64><<<grid, 128, 0, s>>>(p, o); },
-            [&] { graph_batch_kernel<256><<<grid, 128, 0, s>>>(p, o); });
+        if (graphs[gi].nslots != kNoSlot) {
+            const size_t smem = (size_t)kNumThreads * graphs[gi].nslots * sizeof(fr_t);
+            graph_batch_kernel<16, true><<<grid, kNumThreads, smem, s>>>(p, o);
+        } else {
+            launch_by_capacity(
+                capacity_for(graphs[gi].ninter), [&] { graph_batch_kernel<16><<<grid, kNumThreads, 0, s>>>(p, o); },
+                [&] { graph_batch_kernel<64><<<grid, kNumThreads, 0, s>>>(p, o); },
+                [&] { graph_batch_kernel<256><<<grid, kNumThreads, 0, s>>>(p, o); });
+        }
         GB_CHECK_LAUNCH();
     }
 }
 
-// the numerator kernel sized for max_inter intermediates per row
-static void numerator_launch(const num_params &p, uint32_t max_inter, cudaStream_t s)
+// the numerator kernel: the slot interpreter when every graph compiled
+// (max_slots != kNoSlot), else the local-array interpreter sized for
+// max_inter intermediates per row
+static void numerator_launch(const num_params &p, uint32_t max_inter, uint32_t max_slots, cudaStream_t s)
 {
-    const unsigned grid = blocks_for(p.len, 128);
-    launch_by_capacity(
-        capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, 128, 0, s>>>(p); },
-        [&] { numerator_kernel<64><<<grid, 128, 0, s>>>(p); }, [&] { numerator_kernel<256><<<grid, 128, 0, s>>>(p); });
+    set_slot_smem();
+    const unsigned grid = blocks_for(p.len, kNumThreads);
+    if (max_slots != kNoSlot) {
+        numerator_kernel<16, true><<<grid, kNumThreads, (size_t)kNumThreads * max_slots * sizeof(fr_t), s>>>(p);
+    } else {
+        launch_by_capacity(
+            capacity_for(max_inter), [&] { numerator_kernel<16><<<grid, kNumThreads, 0, s>>>(p); },
+            [&] { numerator_kernel<64><<<grid, kNumThreads, 0, s>>>(p); },
+            [&] { numerator_kernel<256><<<grid, kNumThreads, 0, s>>>(p); });
+    }
     GB_CHECK_LAUNCH();
 }
 
@@ -413,8 +706,12 @@ static void numerator_core(fr_t *d_out, const numerator_inputs &in, RawFr beta, 
     p.run_custom = in.run_custom ? 1 : 0;
     p.initial = in.initial;
     uint32_t max_inter = in.run_custom ? in.custom_graph->num_intermediates : 0;
+    uint32_t max_slots = 0;
     graph_upload custom;
-    if (in.run_custom) upload_graph(custom, *in.custom_graph, s);
+    if (in.run_custom) {
+        upload_graph(custom, *in.custom_graph, s);
+        max_slots = slots_for(max_slots, custom.g);
+    }
     p.custom = custom.g;
     p.l0 = in.l0;
     p.l_last = in.l_last;
@@ -439,11 +736,13 @@ static void numerator_core(fr_t *d_out, const numerator_inputs &in, RawFr beta, 
         upload_graph(lk[i], in.lookup_graphs[i], s);
         lkg[i] = lk[i].g;
         max_inter = std::max(max_inter, in.lookup_graphs[i].num_intermediates);
+        max_slots = slots_for(max_slots, lkg[i]);
     }
     for (size_t i = 0; i < in.trash_count; i++) {
         upload_graph(tr[i], in.trash_graphs[i], s);
         trg[i] = tr[i].g;
         max_inter = std::max(max_inter, in.trash_graphs[i].num_intermediates);
+        max_slots = slots_for(max_slots, trg[i]);
     }
     dev_buf<dgraph> d_lkg(in.lookup_count, s), d_trg(in.trash_count, s);
     h2d(d_lkg, lkg.data(), in.lookup_count * sizeof(dgraph), s);
@@ -460,7 +759,7 @@ static void numerator_core(fr_t *d_out, const numerator_inputs &in, RawFr beta, 
     p.trash_cosets = in.trash_cosets;
     p.trash_sel = d_tsel;
     p.trash_graphs = d_trg;
-    numerator_launch(p, max_inter, s);
+    numerator_launch(p, max_inter, max_slots, s);
     // the graph and column-reference buffers are released in stream order
     // after the launch; the caller's stream keeps the kernel ahead of them
 }
@@ -476,7 +775,7 @@ struct numerator_context {
     size_t len = 0, input_len = 0, fixed_cols = 0, perm_columns_len = 0, perm_pk_len = 0;
     size_t lookup_count = 0, trash_count = 0;
     int32_t rot_scale = 1, last_rotation = 0;
-    uint32_t chunk_len = 0, max_inter = 0;
+    uint32_t chunk_len = 0, max_inter = 0, max_slots = 0;
     fr_t g_coset, delta_const, trace_omega;
     dev_buf<fr_t> fixed, fixed_lagrange, l0, l_last, l_active, pk_cosets, pk_lagrange, omega_pows;
     std::vector<RawColumnRef> perm_columns;
@@ -634,7 +933,7 @@ RustError midnight_sppark_bls12_381_eval_numerator(
     numerator_core(d_out, in, beta, gamma, theta, trash_challenge, y, omega, delta_start, delta_const, rot_scale,
                    last_rotation, chunk_len, s);
     d2h(out_raw, d_out, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -781,13 +1080,16 @@ RustError midnight_sppark_bls12_381_numerator_context_create(
     upload_graphs(c->trash, c->trash_g, trash_graphs, trash_count, s);
     for (const dgraph &g : lookup_g) c->max_inter = std::max(c->max_inter, g.ninter);
     for (const dgraph &g : c->trash_g) c->max_inter = std::max(c->max_inter, g.ninter);
+    c->max_slots = slots_for(0, c->custom.g);
+    for (const dgraph &g : lookup_g) c->max_slots = slots_for(c->max_slots, g);
+    for (const dgraph &g : c->trash_g) c->max_slots = slots_for(c->max_slots, g);
     if (!capacity_for(c->max_inter))
         return make_error((int)cudaErrorInvalidValue, "graph needs more than 256 intermediates");
     c->d_lookup = dev_buf<dgraph>(lookup_count, s);
     h2d(c->d_lookup, lookup_g.data(), lookup_count * sizeof(dgraph), s);
     c->d_trash = dev_buf<dgraph>(trash_count, s);
     h2d(c->d_trash, c->trash_g.data(), trash_count * sizeof(dgraph), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     *out = c.release();
     return ok();
     GB_ENTRY_END
@@ -879,7 +1181,7 @@ RustError midnight_sppark_bls12_381_numerator_context_eval(
     fr_device_vec *v = device_vec_new(len, s);
     try {
         p.out = v->values;
-        numerator_launch(p, c->max_inter, s);
+        numerator_launch(p, c->max_inter, c->max_slots, s);
         device_vec_mark_ready(v, s);
     } catch (...) {
         device_vec_delete(v);
@@ -1040,7 +1342,7 @@ RustError midnight_sppark_bls12_381_eval_graph_batch(RawFr *out_raw, size_t len,
     graph_batch_core(d_out, len, d_fixed, fixed_cols, d_advice, advice_cols, d_instance, instance_cols, challenges,
                      challenge_len, beta, gamma, theta, trash_challenge, y, rot_scale, graphs, graph_count, s);
     d2h(out_raw, d_out, len * graph_count * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }

@@ -185,7 +185,7 @@ RustError gb_fr_random_chacha20(void **out, const uint8_t *key32, uint64_t word_
         uint32_t last_pos = 0, last_flag = 0;
         d2h(&last_pos, pos.get() + count - 1, sizeof(uint32_t), s);
         d2h(&last_flag, flags.get() + count - 1, sizeof(uint32_t), s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
         if ((size_t)last_pos + last_flag < n) continue;
         fr_device_vec *v = device_vec_new(n, s);
         try {
@@ -195,7 +195,7 @@ RustError gb_fr_random_chacha20(void **out, const uint8_t *key32, uint64_t word_
             unsigned long long used = 0;
             d2h(&used, d_used, sizeof(used), s);
             device_vec_mark_ready(v, s);
-            GB_CUDA_OK(cudaStreamSynchronize(s));
+            lane_sync(s);
             *words_consumed = used;
         } catch (...) {
             device_vec_delete(v);

@@ -31,6 +31,10 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 cudaStream_t g_streams[kMaxDevices][GB_MAX_LANES + 1];
+// lane status words: host view and device view of 2 words per lane
+uint32_t *g_status_host[kMaxDevices][GB_MAX_LANES + 1];
+uint32_t *g_status_dev[kMaxDevices][GB_MAX_LANES + 1];
+std::atomic<unsigned long long> g_timeouts{0};
 bool g_pool_ready[kMaxDevices];
 std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
 
@@ -56,6 +60,58 @@ cudaStream_t lane_stream()
     if (!s) GB_CUDA_OK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     return s;
 }
+
+// the calling thread's lane status words (created with the lane's stream)
+static void lane_status_words(uint32_t **host, uint32_t **dev)
+{
+    const int d = current_device();
+    if (d < 0 || d >= kMaxDevices) throw cuda_error(-1, "device index out of range");
+    const uint32_t lane = t_lane;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (!g_status_host[d][lane]) {
+        uint32_t *h = nullptr, *dv = nullptr;
+        GB_CUDA_OK(cudaHostAlloc((void **)&h, 2 * sizeof(uint32_t), cudaHostAllocMapped | cudaHostAllocPortable));
+        h[0] = h[1] = 0;
+        GB_CUDA_OK(cudaHostGetDevicePointer((void **)&dv, h, 0));
+        g_status_host[d][lane] = h;
+        g_status_dev[d][lane] = dv;
+    }
+    *host = g_status_host[d][lane];
+    *dev = g_status_dev[d][lane];
+}
+
+uint32_t *lane_status_device()
+{
+    uint32_t *h, *d;
+    lane_status_words(&h, &d);
+    return d;
+}
+
+void lane_check()
+{
+    uint32_t *h, *d;
+    lane_status_words(&h, &d);
+    volatile uint32_t *w = h;
+    const uint32_t a = w[0], b = w[1];
+    if (a || b) {
+        w[0] = 0;
+        w[1] = 0;
+        g_timeouts.fetch_add((unsigned long long)a + b);
+        throw cuda_error((int)cudaErrorLaunchTimeout,
+                         a ? "an NTT twiddle copy of this lane's work did not complete; results since the "
+                             "previous synchronisation are invalid"
+                           : "an NTT work-queue wait of this lane's work ran out; results since the previous "
+                             "synchronisation are invalid");
+    }
+}
+
+void lane_sync(cudaStream_t s)
+{
+    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_check();
+}
+
+unsigned long long lane_timeouts_take() { return g_timeouts.exchange(0); }
 
 void *dev_alloc(size_t bytes, cudaStream_t s)
 {

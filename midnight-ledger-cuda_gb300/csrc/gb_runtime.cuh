@@ -94,6 +94,23 @@ void set_lane(uint32_t lane);
 cudaStream_t lane_stream();
 int current_device();
 
+// Status words of the bounded device waits (NTT twiddle copies, work-queue
+// dependencies), two per (device, lane), in mapped page-locked host memory:
+// a kernel whose wait runs out adds to its lane's word instead of failing,
+// and the host reads the word after the lane's next synchronisation, as
+// CUDA reports errors of asynchronous work at a later call.  lane_sync()
+// synchronises the calling thread's lane stream and then throws
+// cudaErrorLaunchTimeout if a wait of the lane's work ran out since the last
+// check (the words are cleared); lane_check() does the check alone, without
+// waiting.  Entry points that return data to the host synchronise through
+// lane_sync(), so results that depend on a failed wait are never returned
+// as success.
+uint32_t *lane_status_device();
+void lane_check();
+void lane_sync(cudaStream_t s);
+// waits that ran out since the last call, process-wide (the count is reset)
+unsigned long long lane_timeouts_take();
+
 // Stream-ordered device memory from the device's default memory pool, whose
 // release threshold is raised once so freed blocks are reused, not returned.
 void *dev_alloc(size_t bytes, cudaStream_t s);

@@ -129,7 +129,7 @@ RustError gb_g1_to_lagrange(RawG1Affine *out_raw, const RawG1Affine *g_raw, uint
     h2d(din, g_raw, n * sizeof(affine_t), s);
     g_to_lagrange_device(dout, din, k, s);
     d2h(out_raw, dout, n * sizeof(affine_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -161,7 +161,7 @@ RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, RawFr ta
         generator_mul_device(pts, sc, n, s);
         d2h(g_lagrange_out, pts, n * sizeof(affine_t), s);
     }
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }

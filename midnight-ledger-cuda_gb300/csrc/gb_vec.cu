@@ -606,7 +606,7 @@ RustError midnight_sppark_bls12_381_fr_mul_assign(RawFr *values_raw, RawFr scala
     auto d = upload(values, len, s);
     launch_mul_assign(d, scalar, len, s);
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -622,7 +622,7 @@ RustError midnight_sppark_bls12_381_fr_mul_assign_zeta(RawFr *values_raw, RawFr 
     auto d = upload(values, len, s);
     launch_mul_assign_zeta(d, first, second, len, len, s);
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -639,7 +639,7 @@ RustError midnight_sppark_bls12_381_fr_mul_assign_repeating(RawFr *values_raw, c
     auto f = upload(factors, factor_len, s);
     launch_mul_assign_repeating(d, f, factor_len, len, s);
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -655,7 +655,7 @@ RustError midnight_sppark_bls12_381_fr_invert_assign(RawFr *values_raw, size_t l
     auto d = upload(values, len, s);
     batch_invert(d, d, len, nullptr, s);
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -669,7 +669,7 @@ RustError midnight_sppark_bls12_381_fr_sort_canonical(RawFr *values_raw, size_t 
     auto d = upload(values, len, s);
     sort_canonical(d, len, s);
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -691,7 +691,7 @@ RustError midnight_sppark_bls12_381_fr_poly_lincomb(RawFr *out_raw, const RawFr 
     lincomb_kernel<<<blocks_for(poly_len, 256), 256, 0, s>>>(o, d, k, poly_len, poly_count);
     GB_CHECK_LAUNCH();
     d2h(out, o, poly_len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -712,7 +712,7 @@ RustError midnight_sppark_bls12_381_fr_shifted_prefix_product(RawFr *values_raw,
     shifted_apply_kernel<<<blocks_for(len, 256), 256, 0, s>>>(d, prefix, init, len);
     GB_CHECK_LAUNCH();
     d2h(values, d, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -745,7 +745,7 @@ RustError midnight_sppark_bls12_381_fr_permutation_products(void **out, const Ra
         permutation_products(v->values, dc, nullptr, dp, len, column_count, chunk_len, beta, gamma, omega, dd, db,
                              blinding_factors, s);
         device_vec_mark_ready(v, s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         device_vec_delete(v);
         throw;
@@ -823,7 +823,7 @@ RustError midnight_sppark_bls12_381_fr_lookup_products(void **out, const RawFr *
     try {
         lookup_products(v->values, a, b, c, d, len, lookup_count, beta, gamma, bl, blinding_factors, s);
         device_vec_mark_ready(v, s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         device_vec_delete(v);
         throw;
@@ -859,7 +859,7 @@ RustError midnight_sppark_bls12_381_fr_lookup_products_device(void **out, const 
         lookup_products(v->values, base, base + total, base + 2 * total, base + 3 * total, len, lookup_count, beta,
                         gamma, bl, blinding_factors, s);
         device_vec_mark_ready(v, s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         device_vec_delete(v);
         throw;
@@ -892,7 +892,7 @@ RustError midnight_sppark_bls12_381_fr_device_quotient_pieces(void **out, const 
         blind_quotient_pieces_kernel<<<1, 32, 0, s>>>(v->values, b, poly_len, piece_count);
         GB_CHECK_LAUNCH();
         device_vec_mark_ready(v, s);
-        GB_CUDA_OK(cudaStreamSynchronize(s));
+        lane_sync(s);
     } catch (...) {
         device_vec_delete(v);
         throw;
@@ -994,7 +994,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_download(RawFr *out_raw, const
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
     d2h(out, v->values, len * sizeof(fr_t), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1025,7 +1025,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_scatter_host(void *device_vec,
     scatter_kernel<<<blocks_for(count, 256), 256, 0, s>>>(v->values, di, dv, count);
     GB_CHECK_LAUNCH();
     device_vec_mark_ready(v, s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     return ok();
     GB_ENTRY_END
 }
@@ -1159,7 +1159,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes(RawF
     }
     std::vector<unsigned long long> h(2 * count);
     d2h(h.data(), d_stats, 2 * count * sizeof(unsigned long long), s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     size_t total = 0;
     for (size_t p = 0; p < count; p++) {
         starts[p] = (size_t)h[p];
@@ -1177,7 +1177,7 @@ RustError midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes(RawF
         if (n) d2h(out + cursor, base + p * poly_len + starts[p], n * sizeof(fr_t), s);
         cursor += n;
     }
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     *out_len = total;
     return ok();
     GB_ENTRY_END
@@ -1194,7 +1194,7 @@ RustError midnight_sppark_test_delayed_scale(void *device_vec, RawFr scale, uint
     auto *v = reinterpret_cast<fr_device_vec *>(device_vec);
     cudaStream_t s = lane_stream();
     device_vec_wait(v, s);
-    GB_CUDA_OK(cudaStreamSynchronize(s));
+    lane_sync(s);
     stream_host_delay(s, delay_ms);
     if (v->len) launch_mul_assign(v->values, gb::from_raw(scale), v->len, s);
     device_vec_mark_ready(v, s);

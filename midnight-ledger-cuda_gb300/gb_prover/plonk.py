@@ -503,25 +503,41 @@ def keygen(params, circuit, backend, fixed=None, copies=None):
         fixed, _, copies = circuit.synthesize()
     n, k = circuit.n, circuit.k
     dom = Domain(k, circuit.cs_degree)
-    pk = ProvingKey()
-    pk.circuit, pk.domain = circuit, dom
-    bf = circuit.blinding_factors
-    # fixed: values, coefficients, extended cosets, Lagrange commitments
     fixed_vals = ints_to_mont([v for col in fixed for v in col])
-    pk.fixed_lagrange = backend.put(fixed_vals)
-    pk.fixed_coeffs = backend.lagrange_to_coeff(pk.fixed_lagrange, k, circuit.num_fixed)
-    pk.fixed_cosets = backend.coeff_to_extended(pk.fixed_coeffs, k, circuit.num_fixed, dom.extended_k)
-    pk.fixed_commitments = backend.commit_lagrange(pk.fixed_lagrange, n, circuit.num_fixed)
-    # permutation
+    # permutation (permutation/keygen.rs): sigma values from the copy cycles
     asm = PermutationAssembly(n, circuit.m)
     for (sc, sr), (dc, dr) in copies:
         asm.copy(sc, sr, dc, dr)
     sigma = asm.sigma_values(dom.omega)
-    pk.sigma_lagrange_host = ints_to_mont([v for col in sigma for v in col])
+    return keygen_from_values(params, circuit, backend, fixed_vals, ints_to_mont([v for col in sigma for v in col]))
+
+
+def keygen_from_values(params, circuit, backend, fixed_vals, sigma_vals, fixed_commitments=None,
+                       sigma_commitments=None):
+    """The resident proving key from the fixed columns' and the permutation's
+    Lagrange values (Montgomery rows, [num_fixed][n] and [m][n]), as
+    ProvingKey::read rebuilds it from a key file (plonk/mod.rs:538-590):
+    coefficient forms and extended cosets of both, l0 / l_last / l_active,
+    the compiled graphs; the commitments are computed unless given (the file's
+    verifying key carries them)."""
+    n, k = circuit.n, circuit.k
+    dom = Domain(k, circuit.cs_degree)
+    pk = ProvingKey()
+    pk.circuit, pk.domain = circuit, dom
+    bf = circuit.blinding_factors
+    # fixed: values, coefficients, extended cosets, Lagrange commitments
+    pk.fixed_lagrange = backend.put(np.ascontiguousarray(fixed_vals, dtype=np.uint64).reshape(-1, 4))
+    pk.fixed_coeffs = backend.lagrange_to_coeff(pk.fixed_lagrange, k, circuit.num_fixed)
+    pk.fixed_cosets = backend.coeff_to_extended(pk.fixed_coeffs, k, circuit.num_fixed, dom.extended_k)
+    pk.fixed_commitments = (backend.commit_lagrange(pk.fixed_lagrange, n, circuit.num_fixed)
+                            if fixed_commitments is None else list(fixed_commitments))
+    # permutation
+    pk.sigma_lagrange_host = np.ascontiguousarray(sigma_vals, dtype=np.uint64).reshape(-1, 4)
     pk.sigma_lagrange = backend.put(pk.sigma_lagrange_host)
     pk.sigma_coeffs = backend.lagrange_to_coeff(pk.sigma_lagrange, k, circuit.m)
     pk.sigma_cosets = backend.coeff_to_extended(pk.sigma_coeffs, k, circuit.m, dom.extended_k)
-    pk.sigma_commitments = backend.commit_lagrange(pk.sigma_lagrange, n, circuit.m)
+    pk.sigma_commitments = (backend.commit_lagrange(pk.sigma_lagrange, n, circuit.m)
+                            if sigma_commitments is None else list(sigma_commitments))
     # l0, l_last, l_active (keygen.rs:395-430); l_active is the LDE of its
     # Lagrange values, equal to 1 - (l_last + l_blind) since the LDE is linear
     lag = np.zeros((3, n), dtype=object)

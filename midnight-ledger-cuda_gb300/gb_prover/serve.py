@@ -43,14 +43,65 @@ def proof_footprint_bytes(circuit):
 
 
 class Request:
-    __slots__ = ("circuit_id", "witness", "seed", "arrival", "start", "finish", "future", "bytes", "proof")
+    __slots__ = ("circuit_id", "witness", "seed", "arrival", "start", "finish", "future", "bytes", "proof",
+                 "params", "pk", "backend")
 
-    def __init__(self, circuit_id, witness, seed, nbytes):
+    def __init__(self, circuit_id, witness, seed, nbytes, params, pk, backend):
         self.circuit_id, self.witness, self.seed, self.bytes = circuit_id, witness, seed, nbytes
+        self.params, self.pk, self.backend = params, pk, backend
         self.arrival = time.perf_counter()
         self.start = self.finish = None
         self.future = Future()
         self.proof = None
+
+
+class KeyStore:
+    """Proving keys by the SHA-256 of their key-file bytes (keyfile.py), built
+    resident on first use and kept for the `capacity` most recently used
+    keys: the reference's PK_CACHE (transient-crypto/src/proofs.rs:408-470,
+    an LRU of 5 keys keyed by the persistent hash of the key bytes).
+    params_for(k) gives the SRS of size 2^k (from_srs: the server's largest
+    SRS downsized, params.rs:60-77, each size built once)."""
+
+    def __init__(self, params_for, capacity=5, backend_factory=GpuBackend):
+        self.params_for = params_for
+        self.capacity = capacity
+        self.backend_factory = backend_factory
+        self._keys = collections.OrderedDict()
+        self._lock = threading.Lock()
+
+    @classmethod
+    def from_srs(cls, srs, capacity=5, backend_factory=GpuBackend):
+        sizes = {srs.k: srs}
+
+        def params_for(k):
+            if k > srs.k:
+                raise ValueError("key needs a larger SRS than the server holds")
+            if k not in sizes:
+                sizes[k] = srs.downsize(k)
+            return sizes[k]
+        return cls(params_for, capacity, backend_factory)
+
+    def get(self, key_id, key_bytes=None):
+        """(params, pk, backend) of a key, building it from key_bytes when it
+        is not held; raises KeyError for an unknown key sent without bytes"""
+        from .keyfile import parse_pk, read_pk
+        with self._lock:
+            if key_id in self._keys:
+                self._keys.move_to_end(key_id)
+                return self._keys[key_id]
+            if key_bytes is None:
+                raise KeyError("unknown proving key and no key material in the request")
+            params = self.params_for(parse_pk(key_bytes)[0].k)
+            backend = self.backend_factory(params)
+            entry = (params, read_pk(key_bytes, params, backend), backend)
+            self._keys[key_id] = entry
+            while len(self._keys) > self.capacity:
+                self._keys.popitem(last=False)
+            return entry
+
+    def __len__(self):
+        return len(self._keys)
 
 
 class ProofServer:
@@ -59,8 +110,9 @@ class ProofServer:
     limit beyond the slots)."""
 
     def __init__(self, entries, slots=4, hbm_budget=None, backend_factory=GpuBackend, lane_base=1,
-                 set_lane=api.execution_lane_set):
+                 set_lane=api.execution_lane_set, keystore=None):
         self.entries = entries
+        self.keystore = keystore
         self.slots = slots
         self.budget = hbm_budget
         self.backends = {cid: backend_factory(params) for cid, (params, _) in entries.items()}
@@ -84,7 +136,23 @@ class ProofServer:
 
     def submit(self, circuit_id, witness, seed):
         params, pk = self.entries[circuit_id]
-        req = Request(circuit_id, witness, seed, proof_footprint_bytes(pk.circuit))
+        return self._submit(circuit_id, params, pk, self.backends[circuit_id], witness, seed)
+
+    def handle(self, request):
+        """The /prove request loop (proof-server/src/endpoints.rs:246-343): a
+        tagged ProveRequest (wire.py) in, the tagged proof out.  The key is
+        the one the request carries or names, resolved through the key
+        store; the proof runs on a lane like any submitted request."""
+        from . import wire
+        key_bytes, key_id, witness, seed = wire.decode_request(request)
+        if self.keystore is None:
+            raise ValueError("this server holds no key store for /prove requests")
+        params, pk, backend = self.keystore.get(key_id, key_bytes)
+        req = self._submit(key_id, params, pk, backend, witness, seed)
+        return wire.encode_response(req.future.result())
+
+    def _submit(self, circuit_id, params, pk, backend, witness, seed):
+        req = Request(circuit_id, witness, seed, proof_footprint_bytes(pk.circuit), params, pk, backend)
         if self.budget is not None and req.bytes > self.budget:
             raise ValueError("request needs more device memory than the whole budget")
         with self._cv:
@@ -117,9 +185,8 @@ class ProofServer:
                 self.peak_in_use = max(self.peak_in_use, self._in_use)
                 self.peak_running = max(self.peak_running, self._running)
             try:
-                params, pk = self.entries[req.circuit_id]
                 req.start = time.perf_counter()
-                req.proof = create_proof(params, pk, req.witness, self.backends[req.circuit_id],
+                req.proof = create_proof(req.params, req.pk, req.witness, req.backend,
                                          CircuitTranscript(), ChaCha20Rng.from_label(req.seed))
                 req.finish = time.perf_counter()
                 req.future.set_result(req.proof)

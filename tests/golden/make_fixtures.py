@@ -11,8 +11,8 @@ G1 points in the 48-byte zcash compressed encoding to halve the size:
                     2^k compressed g_lagrange
   srs_2p14_g1.sha256 : sha256 of the source file and of srs_2p14_g1.bin
 
-Run in a container that has the reference mounted:
-    python tests/golden/make_fixtures.py /root/reference
+Run where the reference tree is checked out, giving its root:
+    python tests/golden/make_fixtures.py <reference-root>
 """
 import hashlib
 import os
@@ -46,4 +46,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py <reference-root>")
+    main(sys.argv[1])
