@@ -643,8 +643,9 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
     share the rest.  The arrival rate loads the sequential prover to each of
     `loads` of its capacity (below and above it); each stream runs through
     the one-at-a-time prover (1 slot) and the continuous-batching server
-    (`slots` lanes).  The saturated throughput of the mix (every request
-    queued at once) is measured for 1 and `slots` lanes."""
+    (`slots` lanes), without and with the proofs' commitments fused into
+    shared MSM batches (CommitBatcher).  The saturated throughput of the mix
+    (every request queued at once) is measured the same three ways."""
     from gb_prover import plonk, serve
     from gb_prover.kzg import CircuitTranscript, ParamsKZG
     from gb_prover.rng import ChaCha20Rng, ints_to_mont
@@ -688,22 +689,26 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
         arrivals = serve.poisson_arrivals(np.random.default_rng(2025), rate, requests)
         tag = "load%03d" % int(round(load * 100))
         out["serve_%s_rate_per_s" % tag] = rate
-        for name, nslots in (("sequential", 1), ("batched", slots)):
-            srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget)
+        for name, nslots, fuse in (("sequential", 1, False), ("batched", slots, False), ("fused", slots, True)):
+            srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse)
             done, ts = serve.run_stream(srv, reqs, arrivals)
             srv.close()
             summ = serve.latency_summary(done, ts)
             for key in ("proofs_per_s", "p50_ms", "p99_ms", "mean_ms"):
                 out["serve_%s_%s_%s" % (tag, name, key)] = summ[key]
+            if fuse:
+                out["serve_%s_fused_commit_batches" % tag] = srv.batcher.batches
+                out["serve_%s_fused_commit_requests" % tag] = srv.batcher.fused_requests
             proofs[(tag, name)] = [r.future.result() for r in done]
-    out["serve_batched_equals_sequential"] = all(proofs[(t, "batched")] == proofs[(t, "sequential")]
-                                                 for t, _ in proofs)
+    out["serve_batched_equals_sequential"] = all(proofs[(t, m)] == proofs[(t, "sequential")]
+                                                 for t, m in proofs if m != "sequential")
     # saturated: the whole stream queued at once
-    for nslots in (1, slots):
-        srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget)
+    for name, nslots, fuse in (("1lane", 1, False), ("%dlane" % slots, slots, False),
+                               ("%dlane_fused" % slots, slots, True)):
+        srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse)
         done, ts = serve.run_stream(srv, reqs, [0.0] * requests)
         srv.close()
-        out["serve_saturated_%dlane_proofs_per_s" % nslots] = serve.latency_summary(done, ts)["proofs_per_s"]
+        out["serve_saturated_%s_proofs_per_s" % name] = serve.latency_summary(done, ts)["proofs_per_s"]
     return out
 
 

@@ -23,6 +23,8 @@ import threading
 import time
 from concurrent.futures import Future
 
+import numpy as np
+
 from . import api
 from .kzg import CircuitTranscript
 from .plonk import GpuBackend, create_proof
@@ -104,35 +106,155 @@ class KeyStore:
         return len(self._keys)
 
 
+class CommitBatcher:
+    """Commitments of the proofs in flight, fused into shared launches.
+
+    A proof's commitment calls (advice, lookup, product, quotient and
+    opening commitments, each a batch of MSMs over one SRS basis) come here
+    instead of running on the proof's own lane.  A dispatcher thread, on a
+    lane of its own, takes what is waiting once every running proof is
+    waiting here or `window_s` after the first request, whichever comes
+    first; groups the requests by basis (the same SRS size and Lagrange or
+    coefficient form); concatenates each group's scalar vectors on the
+    device; and runs the group as ONE ragged batch through the basis's
+    resident context: every stage of the MSM engine (recode, sort,
+    accumulation, fix-up, reduction) is one launch for all the proofs'
+    MSMs.  The reference fans a context batch out over up to 16 host threads
+    with an engine each (midnight-sppark-msm/src/bls12_381_g1_msm.cu:
+    172-215); here the batch is one launch per stage.  Results are split
+    back in request order, so each proof's bytes are unchanged."""
+
+    def __init__(self, server, lane, window_s=0.0005):
+        self.server = server
+        self.window_s = window_s
+        self._cv = threading.Condition()
+        self._pending = []
+        self._stop = False
+        self.batches = 0
+        self.fused_requests = 0
+        self._lane = lane
+        self._thread = threading.Thread(target=self._run, daemon=True)
+        self._thread.start()
+
+    def commit(self, params, lagrange, h, n, count):
+        fut = Future()
+        with self._cv:
+            self._pending.append((params, lagrange, h, n, count, fut))
+            self._cv.notify_all()
+        return fut.result()
+
+    def close(self):
+        with self._cv:
+            self._stop = True
+            self._cv.notify_all()
+        self._thread.join()
+
+    def _take(self):
+        with self._cv:
+            while not self._pending and not self._stop:
+                self._cv.wait()
+            if not self._pending:
+                return None
+            deadline = time.perf_counter() + self.window_s
+            while not self._stop:
+                if len(self._pending) >= max(1, self.server.running()):
+                    break
+                left = deadline - time.perf_counter()
+                if left <= 0:
+                    break
+                self._cv.wait(left)
+            batch, self._pending = self._pending, []
+            return batch
+
+    def _run(self):
+        from .kzg import affine_from_projective_batch
+        if self.server._set_lane is not None:
+            self.server._set_lane(self._lane)
+        while True:
+            batch = self._take()
+            if batch is None:
+                return
+            groups = collections.OrderedDict()
+            for req in batch:
+                groups.setdefault((id(req[0]), req[1]), []).append(req)
+            for reqs in groups.values():
+                try:
+                    params, lagrange = reqs[0][0], reqs[0][1]
+                    ctx = params.context(lagrange)
+                    if len(reqs) == 1:
+                        _, _, h, n, count, fut = reqs[0]
+                        res = ctx.device_batch(h, 0, n, count)
+                    else:
+                        vec = api.Bls12_381FrDeviceVec.concat_many_host([r[2] for r in reqs],
+                                                                       np.zeros((0, 4), np.uint64))
+                        slices, off = [], 0
+                        for _, _, h, n, count, _ in reqs:
+                            slices += [(off + i * n, 0, n) for i in range(count)]
+                            off += h.len
+                        res = ctx.device_ragged(vec, slices)
+                        vec.free()
+                    pts = affine_from_projective_batch(res)
+                    at = 0
+                    for _, _, _, _, count, fut in reqs:
+                        fut.set_result(list(pts[at:at + count]))
+                        at += count
+                    self.batches += 1
+                    self.fused_requests += len(reqs)
+                except BaseException as e:  # every waiting proof sees the failure
+                    for r in reqs:
+                        if not r[5].done():
+                            r[5].set_exception(e)
+
+
+class FusedCommitBackend(GpuBackend):
+    """GpuBackend whose commitments go through a CommitBatcher."""
+
+    def __init__(self, params, batcher):
+        super().__init__(params)
+        self.batcher = batcher
+
+    def _commit(self, h, n, count, lagrange):
+        return self.batcher.commit(self.params, lagrange, h, n, count)
+
+
 class ProofServer:
     """entries: {circuit_id: (params, pk)}; slots: proofs in flight;
     hbm_budget: bytes the proofs in flight may hold together (None = no
     limit beyond the slots)."""
 
     def __init__(self, entries, slots=4, hbm_budget=None, backend_factory=GpuBackend, lane_base=1,
-                 set_lane=api.execution_lane_set, keystore=None):
+                 set_lane=api.execution_lane_set, keystore=None, fuse_commits=False):
         self.entries = entries
         self.keystore = keystore
         self.slots = slots
         self.budget = hbm_budget
+        self._set_lane = set_lane
+        self._running = 0
+        self._cv = threading.Condition()
+        # fuse_commits: the proofs' commitments run as shared batches on a
+        # lane of their own (CommitBatcher)
+        self.batcher = CommitBatcher(self, lane_base + slots) if fuse_commits else None
+        if self.batcher is not None:
+            backend_factory = lambda params: FusedCommitBackend(params, self.batcher)  # noqa: E731
         self.backends = {cid: backend_factory(params) for cid, (params, _) in entries.items()}
         for params, _ in entries.values():
             if hasattr(params, "context"):
                 params.context(True)
                 params.context(False)
         self._pending = collections.deque()
-        self._cv = threading.Condition()
         self._in_use = 0
-        self._running = 0
         self.peak_in_use = 0
         self.peak_running = 0
         self._stop = False
-        self._set_lane = set_lane
         self.completed = []
         self._workers = [threading.Thread(target=self._worker, args=(lane_base + i,), daemon=True)
                          for i in range(slots)]
         for t in self._workers:
             t.start()
+
+    def running(self):
+        """proofs on a worker now"""
+        return self._running
 
     def submit(self, circuit_id, witness, seed):
         params, pk = self.entries[circuit_id]
@@ -212,6 +334,8 @@ class ProofServer:
             self._cv.notify_all()
         for t in self._workers:
             t.join()
+        if self.batcher is not None:
+            self.batcher.close()
 
 
 def poisson_arrivals(rng, rate, count):

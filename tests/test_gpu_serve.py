@@ -34,3 +34,27 @@ def test_gpu_serving_mix_equals_alone(gb):
         p, pk = entries[cid]
         alone = plonk.create_proof(p, pk, w, plonk.GpuBackend(p), CircuitTranscript(), ChaCha20Rng.from_label(seed))
         assert r.future.result() == alone
+
+
+def test_gpu_fused_commitments_equal_alone(gb):
+    """The server with the proofs' commitments fused into shared ragged MSM
+    batches (CommitBatcher): same proof bytes as each request alone, with
+    batches that really held several proofs' commitments."""
+    srs = ParamsKZG.unsafe_setup(10, plonk.fr_mont(TAU))
+    entries, wit = {}, {}
+    for cid, shape in enumerate([(9, 3, 3, 1), (10, 4, 4, 1)]):
+        c = circuit(*shape)
+        fixed, advice, copies = c.synthesize()
+        p = srs.downsize(c.k)
+        entries[cid] = (p, plonk.keygen(p, c, plonk.GpuBackend(p), fixed, copies))
+        wit[cid] = ints_to_mont([v for col in advice for v in col])
+    rng = np.random.default_rng(17)
+    reqs = [(int(c), wit[int(c)], "f%d" % i) for i, c in enumerate(rng.integers(0, 2, size=16))]
+    srv = serve.ProofServer(entries, slots=4, fuse_commits=True)
+    done, _ = serve.run_stream(srv, reqs, [0.0] * len(reqs))
+    srv.close()
+    assert srv.batcher.fused_requests > srv.batcher.batches  # some batches held several requests
+    for (cid, w, seed), r in zip(reqs, done):
+        p, pk = entries[cid]
+        alone = plonk.create_proof(p, pk, w, plonk.GpuBackend(p), CircuitTranscript(), ChaCha20Rng.from_label(seed))
+        assert r.future.result() == alone
