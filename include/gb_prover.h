@@ -461,6 +461,19 @@ GB_API RustError gb_g1_generator_mul_device(RawG1Affine *d_out, const RawFr *d_s
  * no precomputed table (a context keeps nwin x n x 96 bytes) */
 GB_API RustError gb_g1_msm_device(RawG1Projective *out, const RawG1Affine *d_points, const RawFr *d_scalars,
                                   size_t n);
+/* midnight_sppark_bls12_381_g1_msm_context_device_batch
+ * (bls12_381_g1_msm.cu:6310-6344) queued on the calling lane without
+ * waiting: *ticket receives a handle that gb_msm_ticket_wait completes.
+ * Work queued on the lane meanwhile runs after the batch; the host is free
+ * until it needs the points (a prover queues the transforms that do not
+ * depend on the next challenge before waiting for the commitments).  Every
+ * ticket must be waited for exactly once. */
+GB_API RustError gb_g1_msm_context_device_batch_async(void **ticket, void *context, const void *device_vec,
+                                                      size_t scalar_offset, size_t npoints, size_t nmsms);
+/* waits for a ticket's batch, writes its nmsms points to out in batch order
+ * (out may be NULL) and releases the ticket; a lane wait status set since
+ * the lane's previous synchronisation is returned as cudaErrorLaunchTimeout */
+GB_API RustError gb_msm_ticket_wait(void *ticket, RawG1Projective *out);
 /* KZG SRS (no FFI counterpart; the reference does these in Rust on the CPU):
  * g_lagrange = iFFT(g) * n^-1 over G1 for 2^k points (arithmetic.rs:34-50,
  * params.rs:60-77 downsize), and the seeded-tau setup of params.rs:79-129

@@ -26,6 +26,7 @@
 // Both decode a digit's point as point_base + (d / n) * stride + d % n.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <initializer_list>
 #include <vector>
@@ -477,6 +478,7 @@ static constexpr uint32_t kCoopLanes = 8;
 static constexpr uint32_t kCoopGroups = 16;  // groups per 128-thread block
 static constexpr uint64_t kCoopMaxBuckets = 8u << 15;  // cooperative reduction up to 8 x 2^15 buckets
 static constexpr uint64_t kCoopGroupBudget = 6144;     // groups of the cooperative reduction over a batch
+static constexpr uint32_t kCoopFixupMaxBuckets = 1u << 14;  // cooperative fix-up up to 2^14 buckets in all
 // slots of a group: RUN, SUM, OPD (operand), RES (4 each: X, Y, ZZ, ZZZ),
 // then 12 temporaries
 enum { CO_RUN = 0, CO_SUM = 4, CO_OPD = 8, CO_RES = 12, CO_TMP = 16, CO_SLOTS = 28 };
@@ -645,6 +647,44 @@ __device__ void coop_block_tree(fp_t *sh, const coop_t &c, uint32_t grp)
             coop_add(c, CO_SUM, CO_OPD);
         }
     }
+}
+
+// 7'. msm_fixup_kernel with one 8-lane group per bucket: the partials of a
+//     bucket spanning several chunks are added by cooperative additions.
+//     The kernel's time is the longest span's chain (bucket sizes vary), so
+//     the shorter cooperative additions shorten it most where there are few
+//     buckets and short chunks (proof-size MSMs).
+__global__ void __launch_bounds__(128) msm_fixup_coop_kernel(const uint32_t *__restrict__ starts, uint32_t G,
+                                                             uint32_t L, const xyzz_t *__restrict__ head,
+                                                             const xyzz_t *__restrict__ tail,
+                                                             xyzz_t *__restrict__ buckets,
+                                                             uint32_t *__restrict__ longs,
+                                                             uint32_t *__restrict__ nlong)
+{
+    __shared__ __align__(16) fp_t sh[kCoopGroups * CO_SLOTS];
+    const uint32_t grp = threadIdx.x / kCoopLanes;
+    const coop_t c{sh + (size_t)grp * CO_SLOTS, threadIdx.x % kCoopLanes, 0xffu << (threadIdx.x & 24u)};
+    const uint32_t g = blockIdx.x * kCoopGroups + grp;
+    if (g >= G) return;  // whole groups leave together; no block barrier follows
+    const uint32_t s = starts[g], e = starts[g + 1];
+    if (s == e) {
+        coop_set_inf(c, CO_SUM);
+        coop_store(c, CO_SUM, buckets + g);
+        return;
+    }
+    const uint32_t cs = s / L, ce = (e - 1) / L;
+    if (cs == ce) return;
+    if (ce - cs > kShortSpan) {
+        if (c.lane == 0) longs[atomicAdd(nlong, 1u)] = g;
+        return;
+    }
+    coop_load(c, CO_SUM, tail + cs);
+    for (uint32_t k = cs + 1; k <= ce; k++) {
+        c.sync();
+        coop_load(c, CO_OPD, k == ce ? head + k : tail + k);
+        coop_add(c, CO_SUM, CO_OPD);
+    }
+    coop_store(c, CO_SUM, buckets + g);
 }
 
 // 8a'. msm_reduce_partial_kernel with one 8-lane group per (segment,
@@ -859,8 +899,14 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     }
     if (points_total + stride * (uint64_t)nwin >= 0x80000000ull && precomputed)
         throw cuda_error((int)cudaErrorInvalidValue, "MSM table too large for 31-bit point references");
-    // ~4 sort blocks per SM pair over the whole batch, 4096..65536 digits each
-    uint64_t per = std::max<uint64_t>(4096, std::min<uint64_t>(65536, (digits_total + 607) / 608));
+    // ~4 sort blocks per SM pair over the whole batch, 4096..65536 digits
+    // each, and at least K (2K from 2^23 digits): every block writes and the
+    // column scan and scatter read a K-entry histogram, so blocks far
+    // shorter than K move more histogram than digits (measured on GB300: the
+    // sort of a 2^18-point MSM 0.192 -> 0.098 ms, of three 2^16-point MSMs
+    // 0.183 -> 0.093 ms, of a 2^20-point MSM 0.387 -> 0.311 ms)
+    const uint64_t per_min = std::max<uint64_t>(4096, (uint64_t)K << (digits_total >= (1u << 23) ? 1 : 0));
+    uint64_t per = std::max<uint64_t>(per_min, std::min<uint64_t>(65536, (digits_total + 607) / 608));
     std::vector<blk_desc> bdesc;
     for (uint32_t sidx = 0; sidx < nseg; sidx++) {
         seg_desc &sd = sdesc[sidx];
@@ -938,7 +984,16 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     {
         dev_buf<uint32_t> longs(G, s), nlong(1, s);
         GB_CUDA_OK(cudaMemsetAsync(nlong.get(), 0, sizeof(uint32_t), s));
-        msm_fixup_kernel<<<blocks_for(G, 128), 128, 0, s>>>(starts, G, L, head, tail, buckets, longs, nlong);
+        // few buckets: cooperative groups shorten the longest chain (measured
+        // on GB300: 2^12 points, 4096 buckets 0.121 -> 0.051 ms; 3 x 4096
+        // buckets 0.108 -> 0.071 ms); 2^15 buckets and more: one thread per
+        // bucket keeps more of the multiply-add pipe busy (2^16 points
+        // 0.104 -> 0.136 ms with groups)
+        if (G <= kCoopFixupMaxBuckets)
+            msm_fixup_coop_kernel<<<(G + kCoopGroups - 1) / kCoopGroups, 128, 0, s>>>(starts, G, L, head, tail,
+                                                                                     buckets, longs, nlong);
+        else
+            msm_fixup_kernel<<<blocks_for(G, 128), 128, 0, s>>>(starts, G, L, head, tail, buckets, longs, nlong);
         GB_CHECK_LAUNCH();
         int sms = 0;
         GB_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, current_device()));
@@ -1134,16 +1189,17 @@ static void msm_host_plain(jacobian_t *out, const affine_t *points, const fr_t *
 // this ratio of points to buckets the plain path is taken.
 static constexpr size_t kPrecomputedMinRatio = 8;
 
-// A batch against the context; results to the host.  Large items use the
+// A batch against the context, queued on stream s.  Large items use the
 // precomputed table; small ones run as one plain batch over table row 0 (the
-// bases themselves) with a window sized for them.
-static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const std::vector<msm_item> &items,
-                              cudaStream_t s)
+// bases themselves) with a window sized for them.  The results (one Jacobian
+// point per item) are copied to `staging` on s, large items first; the
+// returned vector gives the item index of each staging slot.  `staging` must
+// be page-locked when the caller does not synchronise s before reading it.
+static std::vector<size_t> context_enqueue_items(msm_context_t *ctx, jacobian_t *staging,
+                                                 const std::vector<msm_item> &items, cudaStream_t s)
 {
-    dev_buf<jacobian_t> d_out(std::max<size_t>(items.size(), 1), s);
     std::vector<msm_item> big, small;
     std::vector<size_t> big_idx, small_idx;
-    size_t small_max = 0;
     for (size_t i = 0; i < items.size(); i++) {
         if (items[i].n * kPrecomputedMinRatio >= ((size_t)1 << (ctx->c - 1)) || items.size() == 1) {
             big.push_back(items[i]);
@@ -1151,19 +1207,76 @@ static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const st
         } else {
             small.push_back(items[i]);
             small_idx.push_back(i);
-            small_max = std::max(small_max, items[i].n);
         }
     }
     dev_buf<jacobian_t> d_big(std::max<size_t>(big.size(), 1), s), d_small(std::max<size_t>(small.size(), 1), s);
     if (!big.empty()) msm_run_batch(big, ctx->c, true, ctx->table, ctx->npoints, d_big, s);
     if (!small.empty()) msm_run_batch(small, tuned_window(small, ctx->table, 0, s), false, ctx->table, 0, d_small, s);
-    std::vector<jacobian_t> hb(big.size()), hs(small.size());
-    d2h(hb.data(), d_big, big.size() * sizeof(jacobian_t), s);
-    d2h(hs.data(), d_small, small.size() * sizeof(jacobian_t), s);
+    d2h(staging, d_big, big.size() * sizeof(jacobian_t), s);
+    d2h(staging + big.size(), d_small, small.size() * sizeof(jacobian_t), s);
+    big_idx.insert(big_idx.end(), small_idx.begin(), small_idx.end());
+    return big_idx;
+}
+
+// The same, results to the host when it returns.
+static void context_run_items(msm_context_t *ctx, jacobian_t *out_host, const std::vector<msm_item> &items,
+                              cudaStream_t s)
+{
+    std::vector<jacobian_t> staging(items.size());
+    const std::vector<size_t> order = context_enqueue_items(ctx, staging.data(), items, s);
     lane_sync(s);
-    for (size_t i = 0; i < big.size(); i++) out_host[big_idx[i]] = hb[i];
-    for (size_t i = 0; i < small.size(); i++) out_host[small_idx[i]] = hs[i];
+    for (size_t i = 0; i < order.size(); i++) out_host[order[i]] = staging[i];
     timed_collect();
+}
+
+// Page-locked staging buffers of the asynchronous MSM calls, reused: a
+// cudaFreeHost would synchronise the device, so buffers are kept until exit.
+static std::mutex g_pinned_mu;
+static std::multimap<size_t, jacobian_t *> g_pinned_free;
+
+static jacobian_t *pinned_take(size_t n, size_t *cap)
+{
+    n = std::max<size_t>(n, 64);
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        auto it = g_pinned_free.lower_bound(n);
+        if (it != g_pinned_free.end()) {
+            *cap = it->first;
+            jacobian_t *p = it->second;
+            g_pinned_free.erase(it);
+            return p;
+        }
+    }
+    jacobian_t *p = nullptr;
+    GB_CUDA_OK(cudaHostAlloc((void **)&p, n * sizeof(jacobian_t), cudaHostAllocPortable));
+    *cap = n;
+    return p;
+}
+
+static void pinned_give(jacobian_t *p, size_t cap)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned_free.emplace(cap, p);
+}
+
+// An MSM batch in flight: its completion event, the page-locked buffer its
+// results land in and the item order of that buffer.
+struct msm_ticket_t {
+    int device = 0;
+    uint32_t lane = 0;
+    cudaEvent_t done = nullptr;
+    jacobian_t *staging = nullptr;
+    size_t cap = 0;
+    std::vector<size_t> order;
+};
+
+static void ticket_release(msm_ticket_t *t)
+{
+    if (!t) return;
+    if (t->done) cudaEventDestroy(t->done);
+    pinned_give(t->staging, t->cap);
+    delete t;
 }
 
 // The device address of page-locked host memory (mapped into the unified
@@ -1353,6 +1466,89 @@ RustError midnight_sppark_bls12_381_g1_msm_context_device_batch(RawG1Projective 
     cudaStream_t s = lane_stream();
     device_vec_wait(dv, s);
     context_run_device(ctx, out, dv->values + scalar_offset, npoints, nmsms, s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// The resident batch of midnight_sppark_bls12_381_g1_msm_context_device_batch,
+// queued on the calling lane and returned at once: *ticket is completed by
+// gb_msm_ticket_wait, which waits for the batch and writes its points.  The
+// host can queue further work on the lane meanwhile (work that does not
+// need the points), so the device is not left idle while the host waits for
+// them.  No reference counterpart (the reference's calls return the points).
+RustError gb_g1_msm_context_device_batch_async(void **ticket, void *context, const void *device_vec,
+                                               size_t scalar_offset, size_t npoints, size_t nmsms)
+{
+    if (!ticket) return make_error((int)cudaErrorInvalidValue, "null MSM ticket output");
+    *ticket = nullptr;
+    if (!context || !device_vec) return make_error(-1, "invalid resident BLS12-381 G1 MSM arguments");
+    GB_ENTRY_BEGIN
+    auto *ctx = reinterpret_cast<msm_context_t *>(context);
+    auto *dv = reinterpret_cast<const fr_device_vec *>(device_vec);
+    if (npoints != 0 && nmsms > (SIZE_MAX - scalar_offset) / npoints)
+        return make_error((int)cudaErrorInvalidValue, "resident MSM range overflow");
+    if (scalar_offset + npoints * nmsms > dv->len)
+        return make_error((int)cudaErrorInvalidValue, "resident MSM range exceeds device vector");
+    if (npoints > ctx->npoints) return make_error((int)cudaErrorInvalidValue, "more scalars than context bases");
+    cudaStream_t s = lane_stream();
+    auto *t = new msm_ticket_t();
+    try {
+        t->device = current_device();
+        t->lane = current_lane();
+        t->staging = pinned_take(nmsms, &t->cap);
+        GB_CUDA_OK(cudaEventCreateWithFlags(&t->done, cudaEventDisableTiming));
+        if (nmsms) {
+            device_vec_wait(dv, s);
+            std::vector<msm_item> items;
+            for (size_t m = 0; m < nmsms; m++)
+                items.push_back(msm_item{dv->values + scalar_offset + m * npoints, npoints, 0});
+            t->order = context_enqueue_items(ctx, t->staging, items, s);
+        }
+        GB_CUDA_OK(cudaEventRecord(t->done, s));
+    } catch (...) {
+        ticket_release(t);
+        throw;
+    }
+    *ticket = t;
+    return ok();
+    GB_ENTRY_END
+}
+
+// Waits for the batch of `ticket`, writes its points to out (nmsms of them,
+// in batch order; out may be null to discard them) and releases the ticket,
+// which must not be used again.  A wait that ran out in the lane's NTT work
+// since its previous synchronisation is reported here, as by the lane's
+// synchronising calls.
+RustError gb_msm_ticket_wait(void *ticket, RawG1Projective *out_raw)
+{
+    auto *t = reinterpret_cast<msm_ticket_t *>(ticket);
+    if (!t) return make_error((int)cudaErrorInvalidValue, "null MSM ticket");
+    jacobian_t *out = reinterpret_cast<jacobian_t *>(out_raw);
+    GB_ENTRY_BEGIN
+    const cudaError_t e = cudaEventSynchronize(t->done);
+    if (e != cudaSuccess) {
+        ticket_release(t);
+        return make_error((int)e, cudaGetErrorString(e));
+    }
+    int prev_dev = 0;
+    GB_CUDA_OK(cudaGetDevice(&prev_dev));
+    const uint32_t prev_lane = current_lane();
+    try {
+        if (prev_dev != t->device) GB_CUDA_OK(cudaSetDevice(t->device));
+        set_lane(t->lane);
+        lane_check();
+    } catch (...) {
+        set_lane(prev_lane);
+        cudaSetDevice(prev_dev);
+        ticket_release(t);
+        throw;
+    }
+    set_lane(prev_lane);
+    if (prev_dev != t->device) GB_CUDA_OK(cudaSetDevice(prev_dev));
+    if (out)
+        for (size_t i = 0; i < t->order.size(); i++) out[t->order[i]] = t->staging[i];
+    ticket_release(t);
+    timed_collect();
     return ok();
     GB_ENTRY_END
 }

@@ -174,6 +174,8 @@ def _declare(L):
         "gb_fr_device_vec_ntt_ragged": (E, [vp, vp, vp, sz, b, fr, fr, fr]),
         "gb_ntt_wait_limit_set": (None, [ctypes.c_int64]),
         "gb_g1_msm_device": (E, [vp, vp, vp, sz]),
+        "gb_g1_msm_context_device_batch_async": (E, [vp, vp, vp, sz, sz, sz]),
+        "gb_msm_ticket_wait": (E, [vp, vp]),
         "gb_g1_msm_context_device_bytes": (sz, [vp]),
         "gb_fr_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),
         "gb_fr_device_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),

@@ -12,7 +12,7 @@ import numpy as np
 from ._lib import MsmError, RawFr, RawMsmConfig, RawMsmSlice, check, lib
 
 __all__ = [
-    "execution_lane_set", "bls12_381_g1_msm", "bls12_381_g1_msm_batch", "Bls12_381G1MsmContext",
+    "execution_lane_set", "bls12_381_g1_msm", "bls12_381_g1_msm_batch", "Bls12_381G1MsmContext", "MsmTicket",
     "Bls12_381FrDeviceVec", "bls12_381_fr_ntt", "bls12_381_fr_ntt_zeta", "bls12_381_fr_divide_ntt_zeta",
     "bls12_381_fr_coeff_to_extended_batch", "bls12_381_fr_device_coeff_to_extended_batch",
     "bls12_381_fr_mul_assign", "bls12_381_fr_mul_assign_zeta", "bls12_381_fr_mul_assign_repeating",
@@ -131,6 +131,14 @@ class Bls12_381G1MsmContext:
                                                                          scalar_offset, npoints, nmsms))
         return out[:nmsms]
 
+    def device_batch_async(self, devvec, scalar_offset, npoints, nmsms):
+        """device_batch queued without waiting (gb_g1_msm_context_device_batch_async):
+        returns an MsmTicket whose wait() gives the points"""
+        h = ctypes.c_void_p()
+        check(lib().gb_g1_msm_context_device_batch_async(ctypes.byref(h), self.raw, devvec.raw, scalar_offset,
+                                                          npoints, nmsms))
+        return MsmTicket(h, nmsms)
+
     def device_ragged(self, devvec, slices):
         arr = (RawMsmSlice * max(len(slices), 1))()
         for i, (so, po, ln) in enumerate(slices):
@@ -149,6 +157,30 @@ class Bls12_381G1MsmContext:
 
 
 # ---------------------------------------------------------------- device vectors
+
+class MsmTicket:
+    """An MSM batch in flight; wait() returns its (nmsms, 18) projective
+    points once, and releases the library's handle."""
+
+    def __init__(self, raw, nmsms):
+        self.raw, self.nmsms = raw, nmsms
+
+    def wait(self):
+        if not self.raw:
+            raise RuntimeError("MSM ticket already waited for")
+        out = np.zeros((max(self.nmsms, 1), 18), dtype=np.uint64)
+        raw, self.raw = self.raw, None
+        check(lib().gb_msm_ticket_wait(raw, _ptr(out)))
+        return out[:self.nmsms]
+
+    def __del__(self):
+        if getattr(self, "raw", None):
+            try:
+                lib().gb_msm_ticket_wait(self.raw, None)
+            except Exception:
+                pass
+            self.raw = None
+
 
 class Bls12_381FrDeviceVec:
     """lib.rs Bls12_381FrDeviceVec: an opaque resident vector of Fr."""

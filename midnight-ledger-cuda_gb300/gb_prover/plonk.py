@@ -251,7 +251,18 @@ class GraphBuilder:
         return self.add_calculation((HORNER, start, tuple(parts), factor))
 
     def compile(self, graph_cls=Graph):
-        """Flatten into the RawGraph arrays (lib.rs:38-79)."""
+        """Flatten into the RawGraph arrays (lib.rs:38-79).  A builder is
+        complete once its key is made, so the flattened graph is kept and
+        returned again by later calls (proofs reuse their key's graphs)."""
+        key = (graph_cls, len(self.calcs), len(self.constants), len(self.rotations), self.num_intermediates)
+        cached = getattr(self, "_compiled", None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        graph = self._compile(graph_cls)
+        self._compiled = (key, graph)
+        return graph
+
+    def _compile(self, graph_cls):
         none = (0, 0, 0)
         calcs, parts = [], []
         for calc, target in self.calcs:
@@ -620,6 +631,25 @@ def _permute_expression_pair(backend, inp, tab, usable, input_blinds, table_blin
     return a_full, t_full
 
 
+class _Ready:
+    """a commitment batch already computed (backends without asynchronous
+    commitments)"""
+
+    def __init__(self, points):
+        self.points = points
+
+    def result(self):
+        return self.points
+
+
+def _commit_async(backend, h, n, count, lagrange=True):
+    """queue a commitment batch; .result() gives the affine points"""
+    f = getattr(backend, "commit_async", None)
+    if f is not None:
+        return f(h, n, count, lagrange)
+    return _Ready((backend.commit_lagrange if lagrange else backend.commit)(h, n, count))
+
+
 def create_proof(params, pk, advice_values, backend, transcript, rng):
     """One proof. advice_values: [m][n] canonical ints (usable rows assigned)
     or an (m*n, 4) Montgomery array; rows from usable_rows on are blinded."""
@@ -639,7 +669,13 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     for col in range(m):
         adv[col, u:] = fr_random(rng, n - u)
     adv_l = backend.put(adv.reshape(-1, 4))
-    for cm in backend.commit_lagrange(adv_l, n, m):
+    # the commitments are queued first; the transforms that need no
+    # challenge run on the device while the host waits for them and writes
+    # the transcript
+    pending = _commit_async(backend, adv_l, n, m)
+    adv_c = backend.lagrange_to_coeff(adv_l, k, m)
+    adv_e = backend.coeff_to_extended(adv_c, k, m, ek)
+    for cm in pending.result():
         transcript.write_point(cm)
     theta = fr_int(transcript.squeeze_challenge())
 
@@ -651,7 +687,10 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
                                             theta=w(theta))
         blinds = [fr_random(rng, bf + 1) for _ in range(2 * L)]  # per lookup: input, then table
         perm_l = backend.permute_lookups(comp, n, u, L, np.concatenate(blinds[0::2]), np.concatenate(blinds[1::2]))
-        for cm in backend.commit_lagrange(perm_l, n, 2 * L):
+        pending = _commit_async(backend, perm_l, n, 2 * L)
+        perm_c = backend.lagrange_to_coeff(perm_l, k, 2 * L)
+        perm_e = backend.coeff_to_extended(perm_c, k, 2 * L, ek)
+        for cm in pending.result():
             transcript.write_point(cm)
     beta = fr_int(transcript.squeeze_challenge())
     gamma = fr_int(transcript.squeeze_challenge())
@@ -671,24 +710,21 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     # same point as its coefficients against g
     random_poly = backend.random_mont(rng, n)
     parts = [z_perm] + ([z_lk] if L else []) + [backend.coeff_to_lagrange(random_poly, k, 1)]
-    cms = backend.commit_lagrange(backend.cat(parts), n, sets + L + 1)
+    pending = _commit_async(backend, backend.cat(parts), n, sets + L + 1)
+    zp_c = backend.lagrange_to_coeff(z_perm, k, sets)
+    zp_e = backend.coeff_to_extended(zp_c, k, sets, ek)
+    if L:
+        zl_c = backend.lagrange_to_coeff(z_lk, k, L)
+        zl_e = backend.coeff_to_extended(zl_c, k, L, ek)
+    cms = pending.result()
     for cm in cms[:sets + L]:
         transcript.write_point(cm)
     transcript.squeeze_challenge()  # trash challenge (no trash arguments)
     transcript.write_point(cms[sets + L])
     y = fr_int(transcript.squeeze_challenge())
 
-    # ---- quotient (prover.rs:1743-1990, evaluation.rs:3114-3528)
-    adv_c = backend.lagrange_to_coeff(adv_l, k, m)
-    adv_e = backend.coeff_to_extended(adv_c, k, m, ek)
-    zp_c = backend.lagrange_to_coeff(z_perm, k, sets)
-    zp_e = backend.coeff_to_extended(zp_c, k, sets, ek)
-    lk_polys = []
-    if L:
-        zl_c = backend.lagrange_to_coeff(z_lk, k, L)
-        zl_e = backend.coeff_to_extended(zl_c, k, L, ek)
-        perm_c = backend.lagrange_to_coeff(perm_l, k, 2 * L)
-        perm_e = backend.coeff_to_extended(perm_c, k, 2 * L, ek)
+    # ---- quotient (prover.rs:1743-1990, evaluation.rs:3114-3528); the
+    # coefficient forms and extended cosets were queued with the commitments
     numer = backend.numerator(
         pk, ek, adv_e, m, w(beta), w(gamma), w(theta), w(y), w(dom.extended_omega), w(beta * ZETA % R),
         w(DELTA), 1 << (ek - k), -(bf + 1), c.chunk_len, zp_e, sets,
@@ -797,39 +833,58 @@ def multi_open(params, backend, n, queries, transcript):
     x2 = fr_int(transcript.squeeze_challenge())
     commits, set_of, point_sets = construct_intermediate_sets(queries)
     nsets = len(point_sets)
-    # q_j = sum over the set's commitments (in commitment order) of x1^i p_i
-    gathered = backend.gather(commits, n)
-    q_polys = []
-    for sid in range(nsets):
-        idx = [i for i, s in enumerate(set_of) if s == sid]
-        coeffs = ints_to_mont([pow(x1, i, R) for i in range(len(idx))])
-        q_polys.append(backend.lincomb_rows(gathered, n, idx, coeffs))
+    # q_j = sum over the set's commitments (in commitment order) of x1^i p_i;
+    # the sets are then taken by (number of points, set number)
+    members = [[i for i, s in enumerate(set_of) if s == sid] for sid in range(nsets)]
     order = sorted(range(nsets), key=lambda i: (len(point_sets[i]), i))
-    q_polys = [q_polys[i] for i in order]
+    members = [members[i] for i in order]
     point_sets = [point_sets[i] for i in order]
-    # f = sum_j x2^j (q_j / prod_{p in set_j} (X - p)), each division a Kate quotient
-    f_parts = []
-    for q, pts in zip(q_polys, point_sets):
-        cur = q
-        for p in pts:
-            cur = backend.kate_divide(cur, n, 1, fr_mont(p))
-        f_parts.append(cur)
-    stack = backend.cat(f_parts)
-    f_poly = backend.lincomb(stack, n, nsets, ints_to_mont([pow(x2, j, R) for j in range(nsets)]))
+    fused = getattr(backend, "multi_open_q_f", None)
+    if fused is not None:
+        # the q polynomials and f in two device calls (the reference's
+        # multi-open entry points)
+        qstack, f_poly = fused(commits, members, point_sets, x1, x2, n)
+    else:
+        gathered = backend.gather(commits, n)
+        q_polys = [backend.lincomb_rows(gathered, n, idx, ints_to_mont([pow(x1, i, R) for i in range(len(idx))]))
+                   for idx in members]
+        # f = sum_j x2^j (q_j / prod_{p in set_j} (X - p)), each division a Kate quotient
+        f_parts = []
+        for q, pts in zip(q_polys, point_sets):
+            cur = q
+            for p in pts:
+                cur = backend.kate_divide(cur, n, 1, fr_mont(p))
+            f_parts.append(cur)
+        stack = backend.cat(f_parts)
+        f_poly = backend.lincomb(stack, n, nsets, ints_to_mont([pow(x2, j, R) for j in range(nsets)]))
+        qstack = backend.cat(q_polys)
     transcript.write_point(backend.commit(f_poly, n, 1)[0])
     x3 = fr_int(transcript.squeeze_challenge())
-    qstack = backend.cat(q_polys)
     for v in backend.eval_polys(qstack, n, nsets, fr_mont(x3)):
         transcript.write_scalar(v)
     x4 = fr_int(transcript.squeeze_challenge())
-    allp = backend.cat(q_polys + [f_poly])
-    final = backend.lincomb(allp, n, nsets + 1, ints_to_mont([pow(x4, j, R) for j in range(nsets + 1)]))
-    # pi = commit((final - final(x3)) / (X - x3)); the Kate quotient ignores the constant term
-    pi_poly = backend.kate_divide(final, n, 1, fr_mont(x3))
-    transcript.write_point(backend.commit(pi_poly, n, 1)[0])
+    scalars = ints_to_mont([pow(x4, j, R) for j in range(nsets + 1)])
+    # pi = commit((final - final(x3)) / (X - x3)), final = sum_j x4^j q_j +
+    # x4^nsets f; the Kate quotient ignores the constant term
+    fused_pi = getattr(backend, "multi_open_pi", None)
+    if fused_pi is not None:
+        pi_poly, pi_len = fused_pi(qstack, f_poly, n, scalars, fr_mont(x3))
+    else:
+        allp = backend.cat([qstack, f_poly])
+        final = backend.lincomb(allp, n, nsets + 1, scalars)
+        pi_poly, pi_len = backend.kate_divide(final, n, 1, fr_mont(x3)), n
+    transcript.write_point(backend.commit(pi_poly, pi_len, 1)[0])
 
 
 # ---------------------------------------------------------------- GPU backend
+
+class _PendingCommit:
+    def __init__(self, ticket):
+        self.ticket = ticket
+
+    def result(self):
+        return list(affine_from_projective_batch(self.ticket.wait()))
+
 
 class GpuBackend:
     """The product backend: polynomials stay in device vectors, commitments go
@@ -910,6 +965,47 @@ class GpuBackend:
 
     def commit_lagrange(self, h, n, count):
         return self._commit(h, n, count, True)
+
+    def multi_open_q_f(self, commits, members, point_sets, x1, x2, n):
+        """the multi-open's q polynomials (one per point set, set order as
+        given) as one device vector, and f, through
+        ..._fr_multiopen_prepare_device and ..._fr_multiopen_f_poly_device;
+        the committed polynomials are read in place when they share one
+        device vector, else from one concatenated copy"""
+        vecs, base, at = [], {}, 0
+        for h, _ in commits:
+            if id(h) not in base:
+                base[id(h)] = at
+                at += h.len // n
+                vecs.append(h)
+        src = vecs[0] if len(vecs) == 1 else api.Bls12_381FrDeviceVec.concat_many_host(vecs, np.zeros((0, 4), np.uint64))
+        refs = [(0, base[id(h)] + i) for h, i in commits]
+        q_off, q_idx, q_co = [0], [], []
+        for idx in members:
+            q_idx += idx
+            q_co += [pow(x1, t, R) for t in range(len(idx))]
+            q_off.append(len(q_idx))
+        pts = ints_to_mont([p for ps in point_sets for p in ps])
+        # (one evaluation is asked for, unused: the entry point wants a query)
+        _, qvec, _ = api.bls12_381_fr_multiopen_prepare_device((src, src, src), n, refs, q_off, q_idx,
+                                                              ints_to_mont(q_co), pts, [0], [0], q_host=False)
+        if src is not vecs[0]:
+            src.free()
+        p_off = [0]
+        for ps in point_sets:
+            p_off.append(p_off[-1] + len(ps))
+        f = api.bls12_381_fr_multiopen_f_poly_device(qvec, n, p_off, pts,
+                                                     ints_to_mont([pow(x2, j, R) for j in range(len(point_sets))]))
+        return qvec, f
+
+    def multi_open_pi(self, qvec, f, n, scalars, point):
+        """(sum_j scalars[j] q_j + scalars[last] f) / (X - point) through
+        ..._fr_multiopen_pi_device: n - 1 coefficients"""
+        return api.bls12_381_fr_multiopen_pi_device(qvec, f, n, scalars, point), n - 1
+
+    def commit_async(self, h, n, count, lagrange):
+        """the commitments of _commit, queued: .result() waits for them"""
+        return _PendingCommit(self.params.context(lagrange).device_batch_async(h, 0, n, count))
 
     def commit(self, h, n, count):
         return self._commit(h, n, count, False)

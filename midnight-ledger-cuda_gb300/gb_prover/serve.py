@@ -216,6 +216,17 @@ class FusedCommitBackend(GpuBackend):
     def _commit(self, h, n, count, lagrange):
         return self.batcher.commit(self.params, lagrange, h, n, count)
 
+    def commit_async(self, h, n, count, lagrange):
+        return _ReadyPoints(self._commit(h, n, count, lagrange))
+
+
+class _ReadyPoints:
+    def __init__(self, points):
+        self.points = points
+
+    def result(self):
+        return self.points
+
 
 class ProofServer:
     """entries: {circuit_id: (params, pk)}; slots: proofs in flight;

@@ -316,3 +316,40 @@ def test_msm_device_pointers_no_table(gb, orc, log_n):
         assert (affine_of(orc, got) == 0).all()
     else:
         assert (affine_of(orc, got) == affine_of(orc, orc.g1_msm(b, s))).all()
+
+
+def test_context_device_batch_async(gb, orc):
+    """gb_g1_msm_context_device_batch_async: several batches in flight at
+    once, with NTT work queued behind them on the same lane, waited for out
+    of order; each equals the oracle.  A ticket dropped without a wait is
+    released, and an empty batch completes."""
+    rng = np.random.default_rng(31)
+    n = 3000
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    sb = np.stack([orc.fr_random(n, rng) for _ in range(4)])
+    want = [affine_of(orc, orc.g1_msm(b, sb[i])) for i in range(4)]
+    ctx = gb.Bls12_381G1MsmContext(b)
+    dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
+    t1 = ctx.device_batch_async(dv, 0, n, 2)
+    other = gb.Bls12_381FrDeviceVec.upload(orc.fr_random(1 << 12, rng))
+    one = orc.fr_from_ints([1])[0]
+    other.ntt_zeta_batch(12, 1, False, one, one, one)
+    t2 = ctx.device_batch_async(dv, 2 * n, n, 2)
+    dropped = ctx.device_batch_async(dv, 0, n, 1)
+    empty = ctx.device_batch_async(dv, 0, n, 0)
+    got2 = t2.wait()
+    got1 = t1.wait()
+    del dropped
+    assert len(empty.wait()) == 0
+    for i in range(2):
+        assert (affine_of(orc, got1[i]) == want[i]).all()
+        assert (affine_of(orc, got2[i]) == want[2 + i]).all()
+    with pytest.raises(RuntimeError):
+        t1.wait()
+    # the same points as the synchronous call
+    sync = ctx.device_batch(dv, 0, n, 4)
+    for i in range(4):
+        assert (affine_of(orc, sync[i]) == want[i]).all()
+    with pytest.raises(Exception):
+        ctx.device_batch_async(dv, 0, n, 5)  # past the end of the vector
+    ctx.close()
