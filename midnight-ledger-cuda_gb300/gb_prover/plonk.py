@@ -663,12 +663,20 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     transcript.common_scalar(w(pk.transcript_repr))
     # ---- advice (prover.rs:1342-1720)
     if isinstance(advice_values, np.ndarray):
-        adv = np.array(advice_values, dtype=np.uint64).reshape(m, n, 4)
+        adv = np.ascontiguousarray(advice_values, dtype=np.uint64).reshape(m * n, 4)
     else:
-        adv = ints_to_mont([v for col in advice_values for v in col]).reshape(m, n, 4)
-    for col in range(m):
-        adv[col, u:] = fr_random(rng, n - u)
-    adv_l = backend.put(adv.reshape(-1, 4))
+        adv = ints_to_mont([v for col in advice_values for v in col]).reshape(m * n, 4)
+    blind_rows = np.concatenate([fr_random(rng, n - u) for _ in range(m)])
+    blind_idx = (np.arange(m, dtype=np.uint32)[:, None] * n + np.arange(u, n, dtype=np.uint32)[None, :]).reshape(-1)
+    put_rows = getattr(backend, "put_with_rows", None)
+    if put_rows is not None:
+        # the caller's rows go up as they are and the blinding rows are
+        # written on the device (no host copy of the witness)
+        adv_l = put_rows(adv, blind_idx, blind_rows)
+    else:
+        adv = adv.copy()
+        adv[blind_idx] = blind_rows
+        adv_l = backend.put(adv)
     # the commitments are queued first; the transforms that need no
     # challenge run on the device while the host waits for them and writes
     # the transcript
@@ -900,6 +908,13 @@ class GpuBackend:
 
     def get(self, h):
         return h.download()
+
+    def put_with_rows(self, arr, indices, rows):
+        """put(arr) with arr[indices] replaced by rows, the rows written on
+        the device"""
+        v = self.put(arr)
+        v.scatter_host(indices, rows)
+        return v
 
     def free(self, *hs):
         for h in hs:
