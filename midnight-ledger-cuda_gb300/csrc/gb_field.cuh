@@ -226,8 +226,38 @@ template <>
 GB_D void row_mac_mod<FrCfg>(uint32_t *acc, int parity, uint32_t m)
 {
     typedef FrCfg C;
-    if (parity == 0) GB_ROW8_IMM(acc, C::M0, C::M2, C::M4, C::M6, m);
-    else GB_ROW8_IMM(acc, C::M1, C::M3, C::M5, C::M7, m);
+    // r's two lowest limbs are 1 and 2^32 - 1: m * 1 = m and m (2^32 - 1)
+    // = (m - [m != 0]) 2^32 + (-m mod 2^32), so those two products of the
+    // row are additions (measured on GB300: Fr products 7% faster, the
+    // 16 x 2^20 NTT 3.61 -> 3.55 ms)
+    if (parity == 0) {
+        asm("add.cc.u32 %0, %0, %9;\n\t"
+            "addc.cc.u32 %1, %1, 0;\n\t"
+            "madc.lo.cc.u32 %2, %9, %10, %2;\n\t"
+            "madc.hi.cc.u32 %3, %9, %10, %3;\n\t"
+            "madc.lo.cc.u32 %4, %9, %11, %4;\n\t"
+            "madc.hi.cc.u32 %5, %9, %11, %5;\n\t"
+            "madc.lo.cc.u32 %6, %9, %12, %6;\n\t"
+            "madc.hi.cc.u32 %7, %9, %12, %7;\n\t"
+            "addc.u32 %8, %8, 0;"
+            : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+              "+r"(acc[7]), "+r"(acc[8])
+            : "r"(m), "n"(C::M2), "n"(C::M4), "n"(C::M6));
+    } else {
+        const uint32_t lo = 0u - m, hi = m - (m != 0u);
+        asm("add.cc.u32 %0, %0, %10;\n\t"
+            "addc.cc.u32 %1, %1, %11;\n\t"
+            "madc.lo.cc.u32 %2, %9, %12, %2;\n\t"
+            "madc.hi.cc.u32 %3, %9, %12, %3;\n\t"
+            "madc.lo.cc.u32 %4, %9, %13, %4;\n\t"
+            "madc.hi.cc.u32 %5, %9, %13, %5;\n\t"
+            "madc.lo.cc.u32 %6, %9, %14, %6;\n\t"
+            "madc.hi.cc.u32 %7, %9, %14, %7;\n\t"
+            "addc.u32 %8, %8, 0;"
+            : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+              "+r"(acc[7]), "+r"(acc[8])
+            : "r"(m), "r"(lo), "r"(hi), "n"(C::M3), "n"(C::M5), "n"(C::M7));
+    }
 }
 
 // even[0..N-1] = even[1..N] + odd[0..N-1], even[N] = odd[N] + carry: the

@@ -288,92 +288,11 @@ __device__ __forceinline__ fr_t bfly_sub(const fr_t &a, const fr_t &b)
     return r;
 }
 
-#if defined(GB_NTT_MUL2) && defined(__CUDA_ARCH__)
-// x * w * 2^-256 mod r below 2r (x < 2r, w < r), CIOS with one accumulator
-// t[0..9] and two carry chains per row (low words, then high words) instead
-// of the even/odd rows and their fold: per step 30 multiply-adds and 8
-// additions.  r's lowest limb is 1, so m = -t0 (INV = -1) and the reduction
-// row's lowest product is m itself: t0 + m carries exactly when t0 != 0.
-__device__ __forceinline__ void fr_mul_lazy2(uint32_t *out, const uint32_t *a, const uint32_t *b)
-{
-    typedef FrCfg C;
-    uint32_t t[10];
-#pragma unroll
-    for (int i = 0; i < 10; i++) t[i] = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint32_t bi = b[i];
-        asm("mad.lo.cc.u32 %0, %10, %18, %0;\n\t"
-            "madc.lo.cc.u32 %1, %11, %18, %1;\n\t"
-            "madc.lo.cc.u32 %2, %12, %18, %2;\n\t"
-            "madc.lo.cc.u32 %3, %13, %18, %3;\n\t"
-            "madc.lo.cc.u32 %4, %14, %18, %4;\n\t"
-            "madc.lo.cc.u32 %5, %15, %18, %5;\n\t"
-            "madc.lo.cc.u32 %6, %16, %18, %6;\n\t"
-            "madc.lo.cc.u32 %7, %17, %18, %7;\n\t"
-            "addc.cc.u32 %8, %8, 0;\n\t"
-            "addc.u32 %9, %9, 0;"
-            : "+r"(t[0]), "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]),
-              "+r"(t[8]), "+r"(t[9])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(bi));
-        asm("mad.hi.cc.u32 %0, %9, %17, %0;\n\t"
-            "madc.hi.cc.u32 %1, %10, %17, %1;\n\t"
-            "madc.hi.cc.u32 %2, %11, %17, %2;\n\t"
-            "madc.hi.cc.u32 %3, %12, %17, %3;\n\t"
-            "madc.hi.cc.u32 %4, %13, %17, %4;\n\t"
-            "madc.hi.cc.u32 %5, %14, %17, %5;\n\t"
-            "madc.hi.cc.u32 %6, %15, %17, %6;\n\t"
-            "madc.hi.cc.u32 %7, %16, %17, %7;\n\t"
-            "addc.u32 %8, %8, 0;"
-            : "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]), "+r"(t[8]),
-              "+r"(t[9])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(bi));
-        const uint32_t m = 0u - t[0];  // t0 * INV with INV = -1
-        uint32_t z;
-        asm("add.cc.u32 %9, %10, %11;\n\t"
-            "madc.lo.cc.u32 %0, %11, %12, %0;\n\t"
-            "madc.lo.cc.u32 %1, %11, %13, %1;\n\t"
-            "madc.lo.cc.u32 %2, %11, %14, %2;\n\t"
-            "madc.lo.cc.u32 %3, %11, %15, %3;\n\t"
-            "madc.lo.cc.u32 %4, %11, %16, %4;\n\t"
-            "madc.lo.cc.u32 %5, %11, %17, %5;\n\t"
-            "madc.lo.cc.u32 %6, %11, %18, %6;\n\t"
-            "addc.cc.u32 %7, %7, 0;\n\t"
-            "addc.u32 %8, %8, 0;"
-            : "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]), "+r"(t[8]),
-              "+r"(t[9]), "=r"(z)
-            : "r"(t[0]), "r"(m), "n"(C::M1), "n"(C::M2), "n"(C::M3), "n"(C::M4), "n"(C::M5), "n"(C::M6),
-              "n"(C::M7));
-        (void)z;
-        asm("mad.hi.cc.u32 %0, %8, %9, %0;\n\t"
-            "madc.hi.cc.u32 %1, %8, %10, %1;\n\t"
-            "madc.hi.cc.u32 %2, %8, %11, %2;\n\t"
-            "madc.hi.cc.u32 %3, %8, %12, %3;\n\t"
-            "madc.hi.cc.u32 %4, %8, %13, %4;\n\t"
-            "madc.hi.cc.u32 %5, %8, %14, %5;\n\t"
-            "madc.hi.cc.u32 %6, %8, %15, %6;\n\t"
-            "addc.u32 %7, %7, 0;"
-            : "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]), "+r"(t[8]), "+r"(t[9])
-            : "r"(m), "n"(C::M1), "n"(C::M2), "n"(C::M3), "n"(C::M4), "n"(C::M5), "n"(C::M6), "n"(C::M7));
-        // divide by 2^32 (t0 is zero)
-#pragma unroll
-        for (int j = 0; j < 9; j++) t[j] = t[j + 1];
-        t[9] = 0;
-    }
-#pragma unroll
-    for (int i = 0; i < 8; i++) out[i] = t[i];
-}
-#endif
-
 __device__ __forceinline__ fr_t bfly_mul(const fr_t &x, const fr_t &w)
 {
     fr_t r;
 #if defined(__CUDA_ARCH__)
-#if defined(GB_NTT_MUL2)
-    fr_mul_lazy2(r.v, x.v, w.v);
-#else
     mont_mul_device<FrCfg, false>(r.v, x.v, w.v);
-#endif
 #endif
     return r;
 }
