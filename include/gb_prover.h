@@ -414,6 +414,41 @@ GB_API RustError midnight_sppark_bls12_381_fr_multiopen_pi_device(void **out, co
                                                                   const RawFr *combination_scalars,
                                                                   size_t scalar_count, RawFr point);
 
+/* ---- Poseidon hash chains (default-off in the reference's Rust callers) --- */
+/* bls12_381_g1_msm.cu:4121-4190 (lib.rs:1029-1040,4185-4236): out[i] = the
+ * i-th hash of a chain of len 3-element Poseidon hashes (width 3, x^5,
+ * 4 + 60 + 4 rounds): prev = initial; per hash, permute (prev, tail0,
+ * input_len), add tail1 to the first element, permute again, prev = its
+ * first element.  mds: 9 values (row-major), round_constants: 68 x 3. */
+GB_API RustError midnight_sppark_bls12_381_fr_poseidon_hash_chain(RawFr *out, size_t len, RawFr initial,
+                                                                  RawFr tail0, RawFr tail1, RawFr input_len,
+                                                                  const RawFr *mds, size_t mds_len,
+                                                                  const RawFr *round_constants,
+                                                                  size_t round_constants_len);
+/* bls12_381_g1_msm.cu:4192-4268 (lib.rs:1042-1053,4238-4290): the chain's
+ * circuit witness, 256 values per hash (128 per permutation: per full
+ * round the three cubes then the three new state values; per run of six
+ * partial rounds five new third elements, then the three new values) */
+GB_API RustError midnight_sppark_bls12_381_fr_poseidon_hash_chain_witness(RawFr *out, size_t len, RawFr initial,
+                                                                          RawFr tail0, RawFr tail1,
+                                                                          RawFr input_len, const RawFr *mds,
+                                                                          size_t mds_len,
+                                                                          const RawFr *round_constants,
+                                                                          size_t round_constants_len);
+/* bls12_381_g1_msm.cu:2820-2876 (lib.rs:854-863,1687-1730): a new device
+ * vector of 8 advice columns x domain_len rows holding the chip's cells for
+ * hash_count hashes: witness (256 per hash) placed by layout (128 entries,
+ * column << 8 | row within a permutation's 21-row region; hash h's regions
+ * start at rows 2 + 41 h and 2 + 41 h + 21), each permutation's input rows
+ * and the chain's first cells from metadata (11 values).  Every layout
+ * entry must name a column below 8 and a row inside the domain. */
+GB_API RustError midnight_sppark_bls12_381_fr_poseidon_advice_from_witness(void **out, const RawFr *witness,
+                                                                           size_t hash_count, size_t domain_len,
+                                                                           const RawFr *metadata,
+                                                                           size_t metadata_len,
+                                                                           const uint16_t *layout,
+                                                                           size_t layout_len);
+
 /* ---- device vectors --------------------------------------------------------- */
 /* bls12_381_g1_msm.cu:2741-3442 */
 GB_API RustError midnight_sppark_bls12_381_fr_device_vec_upload(void **out, const RawFr *values, size_t len);

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgbprover.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gb_runtime.cu", "gb_msm.cu", "gb_ntt.cu", "gb_vec.cu", "gb_gen.cu", "gb_noalloc.cu", "gb_quotient.cu", "gb_srs.cu", "gb_opening.cu", "gb_random.cu", "gb_lookup.cu"]
+SOURCES = ["gb_runtime.cu", "gb_msm.cu", "gb_ntt.cu", "gb_vec.cu", "gb_gen.cu", "gb_noalloc.cu", "gb_quotient.cu", "gb_srs.cu", "gb_opening.cu", "gb_random.cu", "gb_lookup.cu", "gb_poseidon.cu"]
 
 
 def nvcc():

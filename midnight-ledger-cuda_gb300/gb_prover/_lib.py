@@ -156,6 +156,9 @@ def _declare(L):
             vp, vp, vp, vp, vp, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, sz, vp, vp, sz]),
         "midnight_sppark_bls12_381_fr_multiopen_f_poly_device": (E, [vp, vp, sz, vp, sz, vp, sz, vp, sz]),
         "midnight_sppark_bls12_381_fr_multiopen_pi_device": (E, [vp, vp, vp, sz, vp, sz, fr]),
+        "midnight_sppark_bls12_381_fr_poseidon_hash_chain": (E, [vp, sz, fr, fr, fr, fr, vp, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_poseidon_hash_chain_witness": (E, [vp, sz, fr, fr, fr, fr, vp, sz, vp, sz]),
+        "midnight_sppark_bls12_381_fr_poseidon_advice_from_witness": (E, [vp, vp, sz, sz, vp, sz, vp, sz]),
         "midnight_sppark_bls12_381_fr_device_vec_download_nonzero_suffixes": (E, [
             vp, sz, vp, vp, vp, vp, sz, sz, sz]),
         "midnight_sppark_bls12_381_fr_lookup_permute_batch": (E, [vp, vp, vp, sz, sz, sz, vp, vp, sz]),

@@ -28,6 +28,7 @@ __all__ = [
     "fr_lookup_permute_device", "NumeratorContext", "bls12_381_fr_multiopen_prepare",
     "bls12_381_fr_multiopen_prepare_device", "bls12_381_fr_multiopen_f_poly_device",
     "bls12_381_fr_multiopen_pi_device", "bls12_381_fr_lookup_permute_batch", "hook_mask_delay",
+    "bls12_381_fr_poseidon_hash_chain", "bls12_381_fr_poseidon_advice_from_witness",
     "hook_delayed_scale", "autotune_set", "autotune_reset", "autotune_report", "ntt_wait_limit_set",
     "FR_GENERATOR", "fr_coeff_to_extended_coset_batch", "fr_device_coeff_to_extended_coset_batch", "fr_ntt_coset",
     "fr_lde_coset", "g1_msm_device",
@@ -802,6 +803,32 @@ def bls12_381_fr_multiopen_pi_device(q_vec, f_vec, poly_len, combination_scalars
     h = ctypes.c_void_p()
     check(lib().midnight_sppark_bls12_381_fr_multiopen_pi_device(
         ctypes.byref(h), q_vec.raw, f_vec.raw, poly_len, _ptr(sc), len(sc), _fr(point)))
+    return Bls12_381FrDeviceVec(h)
+
+
+def bls12_381_fr_poseidon_hash_chain(initial, tail0, tail1, input_len, mds, round_constants, length,
+                                     witness=False):
+    """lib.rs bls12_381_fr_poseidon_hash_chain[_witness]: the chain's length
+    outputs, or its 256-value witness per hash (witness=True)."""
+    m, rc = _fr_arr(mds), _fr_arr(round_constants)
+    if length == 0:
+        return np.zeros((0, 4), dtype=np.uint64)
+    out = np.zeros((length * (256 if witness else 1), 4), dtype=np.uint64)
+    f = (lib().midnight_sppark_bls12_381_fr_poseidon_hash_chain_witness if witness
+         else lib().midnight_sppark_bls12_381_fr_poseidon_hash_chain)
+    check(f(_ptr(out), length, _fr(initial), _fr(tail0), _fr(tail1), _fr(input_len), _ptr(m), len(m), _ptr(rc),
+            len(rc)))
+    return out
+
+
+def bls12_381_fr_poseidon_advice_from_witness(witness, hash_count, domain_len, metadata, layout):
+    """lib.rs poseidon_advice_from_witness: a Bls12_381FrDeviceVec of 8
+    advice columns x domain_len rows; layout = 128 (column, row) pairs"""
+    w, meta = _fr_arr(witness), _fr_arr(metadata)
+    lay = np.array([(c << 8) | r for c, r in layout], dtype=np.uint16)
+    h = ctypes.c_void_p()
+    check(lib().midnight_sppark_bls12_381_fr_poseidon_advice_from_witness(
+        ctypes.byref(h), _ptr(w), hash_count, domain_len, _ptr(meta), len(meta), _ptr(lay), len(lay)))
     return Bls12_381FrDeviceVec(h)
 
 

@@ -593,3 +593,87 @@ def transcript_replay(ops):
     out = np.zeros((max(nsq, 1), 4), dtype=np.uint64)
     L.orc_transcript_replay(kinds, ctypes.c_size_t(n), ptrs, lens, _p(out))
     return out[:nsq]
+
+
+# ---------------------------------------------------------------- Poseidon (pure Python, small cases)
+
+POSEIDON_WIDTH, POSEIDON_ROUNDS, POSEIDON_FULL_HALF = 3, 68, 4
+
+
+def _poseidon_permute(state, mds, rc, wit):
+    """One width-3 Poseidon permutation over Fr (canonical ints), the round
+    structure of midnight-circuits hash/poseidon (4 full, 60 partial, 4 full
+    rounds, x^5) as the reference's GPU kernel runs it
+    (midnight-sppark-msm/src/bls12_381_g1_msm.cu:2089-2157): the first round
+    constants are added first, each round's MDS output gets the next
+    round's constants.  wit, when a list, receives the permutation's 128
+    witness values in that kernel's order (full round: three cubes, then
+    the three new values; per run of six partial rounds: the new third
+    value of its first five, then the three new values)."""
+    R = R_MOD
+    s = [(state[i] + rc[0][i]) % R for i in range(3)]
+    for r in range(POSEIDON_ROUNDS):
+        full = r < POSEIDON_FULL_HALF or r >= POSEIDON_ROUNDS - POSEIDON_FULL_HALF
+        box = list(s)
+        cubes = []
+        for i in range(3):
+            if full or i == 2:
+                cube = pow(s[i], 3, R)
+                cubes.append(cube)
+                box[i] = cube * s[i] * s[i] % R
+        nxt = [((rc[r + 1][i] if r + 1 < POSEIDON_ROUNDS else 0) + sum(mds[i][j] * box[j] for j in range(3))) % R
+               for i in range(3)]
+        if wit is not None:
+            if full:
+                wit.extend(cubes)
+                wit.extend(nxt)
+            else:
+                p = (r - POSEIDON_FULL_HALF) % 6
+                if p < 5:
+                    wit.append(nxt[2])
+                else:
+                    wit.extend(nxt)
+        s = nxt
+    return s
+
+
+def poseidon_hash_chain(initial, tail0, tail1, input_len, mds, rc, length, witness=False):
+    """bls12_381_g1_msm.cu:2159-2216: canonical ints in, canonical ints out;
+    mds 3 x 3, rc 68 x 3.  Returns the chain's outputs, or with witness=True
+    its 256 witness values per hash."""
+    prev, outs, wit = initial, [], []
+    for _ in range(length):
+        st = _poseidon_permute([prev, tail0, input_len], mds, rc, wit if witness else None)
+        st[0] = (st[0] + tail1) % R_MOD
+        st = _poseidon_permute(st, mds, rc, wit if witness else None)
+        prev = st[0]
+        outs.append(prev)
+    return wit if witness else outs
+
+
+def poseidon_advice_from_witness(witness, hash_count, domain_len, metadata, layout):
+    """bls12_381_g1_msm.cu:2018-2075: 8 advice columns x domain_len rows
+    (canonical ints, column-major) from a chain's witness (256 per hash),
+    layout = 128 (column, row) pairs and 11 metadata values.  The fixed
+    cells of each hash are written after the layout's."""
+    R = R_MOD
+    out = [[0] * domain_len for _ in range(8)]
+    for h in range(hash_count):
+        for k in range(256):
+            col, row = layout[k % 128]
+            out[col][2 + 41 * h + 21 * (k // 128) + row] = witness[h * 256 + k]
+    for h in range(hash_count):
+        r0 = 2 + 41 * h
+        w = witness[h * 256:(h + 1) * 256]
+        first = [metadata[4] if h == 0 else witness[(h - 1) * 256 + 253], metadata[5], metadata[7]]
+        for c in range(3):
+            out[c][r0] = first[c]
+            out[c][r0 + 1] = (first[c] + metadata[8 + c]) % R
+        absorbed = (w[125] + metadata[6]) % R
+        out[0][r0 + 20], out[1][r0 + 20], out[2][r0 + 20] = absorbed, w[125], metadata[6]
+        second = [absorbed, w[126], w[127]]
+        for c in range(3):
+            out[c][r0 + 21] = second[c]
+            out[c][r0 + 22] = (second[c] + metadata[8 + c]) % R
+    out[0][0], out[1][0], out[2][0], out[0][1] = metadata[0], metadata[1], metadata[2], metadata[3]
+    return out

@@ -5,6 +5,8 @@ reporting of an NTT twiddle-copy wait that runs out."""
 import numpy as np
 import pytest
 
+from conftest import affine_of
+
 pytestmark = pytest.mark.gpu
 
 CUDA_ERROR_LAUNCH_TIMEOUT = 702
@@ -169,3 +171,36 @@ def test_twiddle_wait_timeout_is_reported(gb, orc):
     dv = gb.Bls12_381FrDeviceVec.upload(v)
     dv.ntt_zeta(log_n, False, one, one, one)
     assert (dv.download() == orc.fr_ntt(v, log_n, False)).all()
+
+
+def test_twiddle_wait_timeout_reported_by_msm_ticket(gb, orc):
+    """A resident NTT whose twiddle-copy wait ran out, followed on the same
+    lane by an asynchronous context MSM: the ticket's wait is the lane's next
+    synchronisation and reports cudaErrorLaunchTimeout instead of points.
+    The next ticket, with the default limit again, returns correct points."""
+    rng = np.random.default_rng(19)
+    log_n = 12
+    v = orc.fr_random(1 << log_n, rng)
+    one = orc.fr_const(orc.CONST_ONE)
+    n = 1000
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    s = orc.fr_random(n, rng)
+    ctx = gb.Bls12_381G1MsmContext(b)
+    sv = gb.Bls12_381FrDeviceVec.upload(s)
+    gb.ntt_variant_set(4)
+    gb.ntt_wait_timeouts()  # clear
+    try:
+        gb.ntt_wait_limit_set(0)
+        dv = gb.Bls12_381FrDeviceVec.upload(v)
+        dv.ntt_zeta(log_n, False, one, one, one)
+        ticket = ctx.device_batch_async(sv, 0, n, 1)
+        with pytest.raises(gb.MsmError) as e:
+            ticket.wait()
+        assert e.value.code == CUDA_ERROR_LAUNCH_TIMEOUT
+    finally:
+        gb.ntt_wait_limit_set(None)
+        gb.ntt_variant_set(0)
+    gb.ntt_wait_timeouts()
+    got = ctx.device_batch_async(sv, 0, n, 1).wait()
+    assert (affine_of(orc, got[0]) == affine_of(orc, orc.g1_msm(b, s))).all()
+    ctx.close()

@@ -312,3 +312,29 @@ def test_eval_and_kate_division(orc):
             back[i] = (back[i] - c * zi) % R
         back[0] = (back[0] + ev) % R
         assert back == ai
+
+
+def test_poseidon_oracle_structure():
+    """The Poseidon restatement's round structure and witness order: with the
+    identity MDS and zero constants the two outer lanes see only the 8 full
+    rounds' x^5 and the third lane all 68; a chain's outputs are its
+    witness values 253 (the second permutation's final first element), and
+    the first permutation's final state sits at 125..127."""
+    from oracle import oracle as orc
+    R = orc.R_MOD
+    ident = [[1 if i == j else 0 for j in range(3)] for i in range(3)]
+    zero = [[0, 0, 0] for _ in range(68)]
+    x = [5, 7, 11]
+    out = orc._poseidon_permute(list(x), ident, zero, None)
+    assert out == [pow(5, 5 ** 8, R), pow(7, 5 ** 8, R), pow(11, 5 ** 68, R)]
+    rng = np.random.default_rng(3)
+    ints = lambda k: [int.from_bytes(rng.bytes(40), "little") % R for _ in range(k)]  # noqa: E731
+    mds = [ints(3) for _ in range(3)]
+    rc = [ints(3) for _ in range(68)]
+    initial, tail0, tail1 = ints(3)
+    outs = orc.poseidon_hash_chain(initial, tail0, tail1, 3, mds, rc, 3)
+    wit = orc.poseidon_hash_chain(initial, tail0, tail1, 3, mds, rc, 3, witness=True)
+    assert len(wit) == 3 * 256
+    assert outs == [wit[256 * h + 253] for h in range(3)]
+    first = orc._poseidon_permute([initial, tail0, 3], mds, rc, None)
+    assert first == wit[125:128]
