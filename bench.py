@@ -267,6 +267,8 @@ def main():
                          "peak_row_kernel launch just before the last proof as a marker (small cases for "
                          "profilers; one JSON line of timings)")
     ap.add_argument("--count", type=int, default=16)
+    ap.add_argument("--circuit", type=int, default=-1,
+                    help="--case proof: -1 = the k = 16 configuration, 0..5 = one of the serving mix's circuits")
     args = ap.parse_args()
     args.n = 1 << args.log_n
     args.n_ref = args.n  # the CPU baseline runs the whole 2^20 MSM (about 2 s on 16 Grace cores)
@@ -428,7 +430,8 @@ def main():
 
 
 def run_proof_case(args):
-    """--case proof: the k = 16 synthetic proof, one at a time (wall time)."""
+    """--case proof: the k = 16 synthetic proof (or, with --circuit i, the
+    serving mix's circuit i), one at a time (wall time)."""
     import torch
     import gb_prover as gb
     from gb_prover import plonk
@@ -436,10 +439,16 @@ def run_proof_case(args):
     from gb_prover.rng import ChaCha20Rng, ints_to_mont
     torch.cuda.set_device(0)
     gb.lib()
-    c = plonk.SyntheticCircuit(16, advice=3, degree=3, lookups=1, copies=1 << 14, table_log=12,
-                               label="full synthetic PLONK/KZG proof, k=16")
+    if args.circuit < 0:
+        k = 16
+        c = plonk.SyntheticCircuit(16, advice=3, degree=3, lookups=1, copies=1 << 14, table_log=12,
+                                   label="full synthetic PLONK/KZG proof, k=16")
+    else:
+        k, m, d, L, _ = SERVE_CIRCUITS[args.circuit]
+        c = plonk.SyntheticCircuit(k, advice=m, degree=d, lookups=L, copies=1 << (k - 2),
+                                   table_log=min(12, k - 3), label="serve circuit %d" % args.circuit)
     fixed, advice, copies = c.synthesize()
-    params = ParamsKZG.unsafe_setup(16, plonk.fr_mont(0x5EED0F7A0))
+    params = ParamsKZG.unsafe_setup(k, plonk.fr_mont(0x5EED0F7A0))
     be = plonk.GpuBackend(params)
     pk = plonk.keygen(params, c, be, fixed, copies)
     adv = ints_to_mont([v for col in advice for v in col])
@@ -453,7 +462,7 @@ def run_proof_case(args):
         t0 = time.perf_counter()
         plonk.create_proof(params, pk, adv, be, CircuitTranscript(), ChaCha20Rng.from_label("p%d" % i))
         ms.append((time.perf_counter() - t0) * 1e3)
-    print(json.dumps({"case": "proof", "k": 16, "ms": ms, "best_ms": min(ms)}))
+    print(json.dumps({"case": "proof", "k": k, "circuit": args.circuit, "ms": ms, "best_ms": min(ms)}))
 
 
 def run_ntt_case(args):
@@ -703,7 +712,7 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
     out["serve_batched_equals_sequential"] = all(proofs[(t, m)] == proofs[(t, "sequential")]
                                                  for t, m in proofs if m != "sequential")
     # saturated: the whole stream queued at once
-    for name, nslots, fuse in (("1lane", 1, False), ("%dlane" % slots, slots, False),
+    for name, nslots, fuse in (("1lane", 1, False), ("%dlane" % slots, slots, False), ("8lane", 8, False),
                                ("%dlane_fused" % slots, slots, True)):
         srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse)
         done, ts = serve.run_stream(srv, reqs, [0.0] * requests)
