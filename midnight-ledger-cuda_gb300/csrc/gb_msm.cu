@@ -110,11 +110,59 @@ __device__ __forceinline__ affine_t load_affine(const affine_t *pts, uint32_t id
     return r;
 }
 
-// 1. recode: for item m, point i, window j: digits[base_m + j * n_m + i] =
-//    (|digit| - 1) | sign << 31, or kZeroDigit
-__global__ void msm_recode_kernel(const item_desc *__restrict__ items, uint32_t nitems, uint64_t total, int c,
-                                  int nwin, uint32_t *__restrict__ digits)
+// The canonical value of a Montgomery-form scalar s < r (s R^-1 mod r):
+// Montgomery reduction alone (the product by 1 without its a * b rows),
+// 8 steps of t = (t + m r) / 2^32 with m = -t0 (r's lowest limb is 1).  The
+// result is below r for s < r, and the final subtraction covers s < R.
+// The scalar is read with two 16-byte loads when it is 16-byte aligned.
+__device__ __forceinline__ fr_t scalar_canonical(const fr_t *p)
 {
+    fr_t a;
+    if (((uintptr_t)p & 15u) == 0) {
+        const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(p)), hi = __ldg(reinterpret_cast<const uint4 *>(p) + 1);
+        a.v[0] = lo.x, a.v[1] = lo.y, a.v[2] = lo.z, a.v[3] = lo.w;
+        a.v[4] = hi.x, a.v[5] = hi.y, a.v[6] = hi.z, a.v[7] = hi.w;
+    } else {
+        a = *p;
+    }
+    uint32_t t[9];
+#pragma unroll
+    for (int i = 0; i < 8; i++) t[i] = a.v[i];
+    t[8] = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t m = 0u - t[0];
+        uint64_t c = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint64_t v = (uint64_t)m * FrCfg::mod(j) + t[j] + c;
+            t[j] = (uint32_t)v;
+            c = v >> 32;
+        }
+        const uint64_t top = (uint64_t)t[8] + c;
+#pragma unroll
+        for (int j = 0; j < 7; j++) t[j] = t[j + 1];
+        t[7] = (uint32_t)top;
+        t[8] = (uint32_t)(top >> 32);
+    }
+    fr_t r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = t[i];
+    fr_t::reduce_once(r.v, t[8]);
+    return r;
+}
+
+// 1. recode: for item m, point i, window j: digits[base_m + j * n_m + i] =
+//    (|digit| - 1) | sign << 31, or kZeroDigit.  One instance per window
+//    size, so the windows unroll and the scalar's limbs stay in registers
+//    (with the window a run-time value they were indexed in local memory).
+template <int C>
+__global__ void msm_recode_kernel(const item_desc *__restrict__ items, uint32_t nitems, uint64_t total,
+                                  uint32_t *__restrict__ digits)
+{
+    constexpr int NWIN = 255 / C + 1;
+    constexpr uint32_t half = 1u << (C - 1);
+    constexpr uint32_t mask = (1u << C) - 1;
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
     uint32_t lo = 0, hi = nitems;  // last item with point_prefix <= t
@@ -125,16 +173,15 @@ __global__ void msm_recode_kernel(const item_desc *__restrict__ items, uint32_t 
     }
     const item_desc it = items[lo];
     const uint64_t i = t - it.point_prefix;
-    fr_t s = it.scalars[i].from_mont();
-    const uint32_t half = 1u << (c - 1);
-    const uint32_t mask = (1u << c) - 1;
+    const fr_t s = scalar_canonical(it.scalars + i);
     uint32_t carry = 0;
     uint32_t *out = digits + it.digit_base + i;
-    for (int j = 0; j < nwin; j++) {
-        int bit = j * c;
-        int limb = bit >> 5, off = bit & 31;
-        uint32_t l0 = limb < 8 ? s.v[limb] : 0;
-        uint32_t l1 = limb + 1 < 8 ? s.v[limb + 1] : 0;
+#pragma unroll
+    for (int j = 0; j < NWIN; j++) {
+        const int bit = j * C;
+        const int limb = bit >> 5, off = bit & 31;
+        const uint32_t l0 = limb < 8 ? s.v[limb < 8 ? limb : 7] : 0;
+        const uint32_t l1 = limb + 1 < 8 ? s.v[limb + 1 < 8 ? limb + 1 : 7] : 0;
         uint32_t raw = (uint32_t)((((uint64_t)l1 << 32) | l0) >> off) & mask;
         raw += carry;
         uint32_t d;
@@ -146,11 +193,30 @@ __global__ void msm_recode_kernel(const item_desc *__restrict__ items, uint32_t 
             d = raw - 1;
         } else {
             carry = 1;
-            uint32_t mag = (1u << c) - raw;  // digit = raw - 2^c < 0
+            const uint32_t mag = (1u << C) - raw;  // digit = raw - 2^c < 0
             d = mag == 0 ? kZeroDigit : ((mag - 1) | 0x80000000u);
         }
         out[(uint64_t)j * it.n] = d;
     }
+}
+
+static void launch_recode(const item_desc *items, uint32_t nitems, uint64_t total, int c, uint32_t *digits,
+                          cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((total + 255) / 256);
+    switch (c) {
+    case 8: msm_recode_kernel<8><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 9: msm_recode_kernel<9><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 10: msm_recode_kernel<10><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 11: msm_recode_kernel<11><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 12: msm_recode_kernel<12><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 13: msm_recode_kernel<13><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 14: msm_recode_kernel<14><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 15: msm_recode_kernel<15><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    case 16: msm_recode_kernel<16><<<grid, 256, 0, s>>>(items, nitems, total, digits); break;
+    default: throw cuda_error((int)cudaErrorInvalidValue, "MSM window size outside 8..16");
+    }
+    GB_CHECK_LAUNCH();
 }
 
 // 2. per-block histograms: hist[b][k]
@@ -953,9 +1019,7 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     int tok_all = timed_begin(s);
     int tok_sort = timed_begin(s);
     if (points_total) {
-        msm_recode_kernel<<<(unsigned)((points_total + 255) / 256), 256, 0, s>>>(d_items, nitems, points_total, c,
-                                                                                 nwin, digits);
-        GB_CHECK_LAUNCH();
+        launch_recode(d_items, nitems, points_total, c, digits, s);
     }
     const size_t smem = (size_t)K * 4;
     msm_hist_kernel<<<nblocks, 1024, smem, s>>>(digits, d_segs, d_blks, K, hist);
