@@ -624,16 +624,17 @@ def proof_config(gb, steps=10):
            "proof_k16_bytes": len(proof), "proof_k16_keygen_s": keygen_s, "proof_k16_count": steps}
     # saturated throughput: 32 requests queued at once, one lane against several
     from gb_prover import serve
-    for slots in (1, 4, 8):
-        srv = serve.ProofServer({0: (params, pk)}, slots=slots)
-        for i in range(slots):
+    for slots, lock in ((1, 1), (4, 1), (8, 1), (4, 4)):
+        srv = serve.ProofServer({0: (params, pk)}, slots=slots, lockstep=lock)
+        for i in range(slots * lock):
             srv.submit(0, adv, "warm%d" % i)
         srv.drain()
         t0 = time.perf_counter()
         reqs = [srv.submit(0, adv, "s%d" % i) for i in range(32)]
         for r in reqs:
             r.future.result()
-        out["proof_k16_saturated_%dlane_proofs_per_s" % slots] = 32 / (time.perf_counter() - t0)
+        key = "%dlane" % slots + ("_lockstep%d" % lock if lock > 1 else "")
+        out["proof_k16_saturated_%s_proofs_per_s" % key] = 32 / (time.perf_counter() - t0)
         srv.close()
     return out
 
@@ -653,7 +654,8 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
     `loads` of its capacity (below and above it); each stream runs through
     the one-at-a-time prover (1 slot) and the continuous-batching server
     (`slots` lanes), without and with the proofs' commitments fused into
-    shared MSM batches (CommitBatcher).  The saturated throughput of the mix
+    shared MSM batches (CommitBatcher), and with lockstep groups of up to 4
+    waiting requests of one circuit per lane (plonk.create_proofs).  The saturated throughput of the mix
     (every request queued at once) is measured the same three ways."""
     from gb_prover import plonk, serve
     from gb_prover.kzg import CircuitTranscript, ParamsKZG
@@ -698,8 +700,9 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
         arrivals = serve.poisson_arrivals(np.random.default_rng(2025), rate, requests)
         tag = "load%03d" % int(round(load * 100))
         out["serve_%s_rate_per_s" % tag] = rate
-        for name, nslots, fuse in (("sequential", 1, False), ("batched", slots, False), ("fused", slots, True)):
-            srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse)
+        for name, nslots, fuse, lock in (("sequential", 1, False, 1), ("batched", slots, False, 1),
+                                         ("fused", slots, True, 1), ("lockstep", slots, False, 4)):
+            srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse, lockstep=lock)
             done, ts = serve.run_stream(srv, reqs, arrivals)
             srv.close()
             summ = serve.latency_summary(done, ts)
@@ -712,9 +715,10 @@ def serve_config(gb, requests=160, slots=4, hbm_budget=8 << 30, loads=(0.85, 1.5
     out["serve_batched_equals_sequential"] = all(proofs[(t, m)] == proofs[(t, "sequential")]
                                                  for t, m in proofs if m != "sequential")
     # saturated: the whole stream queued at once
-    for name, nslots, fuse in (("1lane", 1, False), ("%dlane" % slots, slots, False), ("8lane", 8, False),
-                               ("%dlane_fused" % slots, slots, True)):
-        srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse)
+    for name, nslots, fuse, lock in (("1lane", 1, False, 1), ("%dlane" % slots, slots, False, 1),
+                                     ("8lane", 8, False, 1), ("%dlane_fused" % slots, slots, True, 1),
+                                     ("%dlane_lockstep4" % slots, slots, False, 4), ("8lane_lockstep4", 8, False, 4)):
+        srv = serve.ProofServer(entries, slots=nslots, hbm_budget=proof_budget, fuse_commits=fuse, lockstep=lock)
         done, ts = serve.run_stream(srv, reqs, [0.0] * requests)
         srv.close()
         out["serve_saturated_%s_proofs_per_s" % name] = serve.latency_summary(done, ts)["proofs_per_s"]

@@ -631,9 +631,18 @@ def _permute_expression_pair(backend, inp, tab, usable, input_blinds, table_blin
     return a_full, t_full
 
 
+class CommitRequest:
+    """A proof step's commitment batch: count polynomials of n values in
+    device vector (or host array) h, against g_lagrange (lagrange) or g.
+    The proof generator yields it and receives a pending object whose
+    result() gives the affine points."""
+
+    def __init__(self, h, n, count, lagrange):
+        self.h, self.n, self.count, self.lagrange = h, n, count, lagrange
+
+
 class _Ready:
-    """a commitment batch already computed (backends without asynchronous
-    commitments)"""
+    """a commitment batch already computed"""
 
     def __init__(self, points):
         self.points = points
@@ -642,17 +651,90 @@ class _Ready:
         return self.points
 
 
-def _commit_async(backend, h, n, count, lagrange=True):
-    """queue a commitment batch; .result() gives the affine points"""
-    f = getattr(backend, "commit_async", None)
-    if f is not None:
-        return f(h, n, count, lagrange)
-    return _Ready((backend.commit_lagrange if lagrange else backend.commit)(h, n, count))
+class _Slice:
+    """one proof's share of a fused commitment batch"""
+
+    def __init__(self, fused, start, count):
+        self.fused, self.start, self.count = fused, start, count
+
+    def result(self):
+        if not hasattr(self.fused, "_points"):
+            self.fused._points = self.fused.result()
+        return self.fused._points[self.start:self.start + self.count]
+
+
+def _commit_requests(backend, reqs):
+    """pending results of the commitment requests that proofs in lockstep
+    yielded at the same step.  With asynchronous commitments, requests of
+    one basis and length are fused: their vectors are concatenated on the
+    device and committed as one MSM batch, so every stage of the MSM engine
+    is one launch for all the proofs; otherwise each runs on its own."""
+    commit_async = getattr(backend, "commit_async", None)
+    if commit_async is None:
+        return [_Ready((backend.commit_lagrange if r.lagrange else backend.commit)(r.h, r.n, r.count))
+                for r in reqs]
+    out = [None] * len(reqs)
+    groups = {}
+    for i, r in enumerate(reqs):
+        groups.setdefault((r.lagrange, r.n), []).append(i)
+    for (lagrange, n), idx in groups.items():
+        if len(idx) == 1:
+            r = reqs[idx[0]]
+            out[idx[0]] = commit_async(r.h, n, r.count, lagrange)
+            continue
+        parts, counts = [], []
+        for i in idx:
+            r = reqs[i]
+            # each request's polynomials as one vector of count * n values
+            parts.append(r.h if r.h.len == r.count * n else r.h.gather_polys(n, list(range(r.count))))
+            counts.append(r.count)
+        fused = commit_async(backend.cat(parts), n, sum(counts), lagrange)
+        at = 0
+        for i, cnt in zip(idx, counts):
+            out[i] = _Slice(fused, at, cnt)
+            at += cnt
+    return out
+
+
+def _drive(gens, backend):
+    """Run proof generators in lockstep: each runs to its next commitment
+    request, the requests of a step are committed together, and each
+    generator continues with its pending points.  Returns the proofs."""
+    proofs = [None] * len(gens)
+    sends = [None] * len(gens)
+    live = list(range(len(gens)))
+    while live:
+        asked = []
+        for i in live:
+            try:
+                asked.append((i, gens[i].send(sends[i])))
+            except StopIteration as stop:
+                proofs[i] = stop.value
+        live = [i for i, _ in asked]
+        for (i, _), pending in zip(asked, _commit_requests(backend, [r for _, r in asked])):
+            sends[i] = pending
+    return proofs
 
 
 def create_proof(params, pk, advice_values, backend, transcript, rng):
     """One proof. advice_values: [m][n] canonical ints (usable rows assigned)
     or an (m*n, 4) Montgomery array; rows from usable_rows on are blinded."""
+    return _drive([_proof_steps(params, pk, advice_values, backend, transcript, rng)], backend)[0]
+
+
+def create_proofs(params, pk, advice_list, backend, transcripts, rngs):
+    """Several proofs of one circuit in lockstep: at each round every proof's
+    commitments join one MSM batch (one launch per MSM stage for all of
+    them).  Each proof's bytes equal create_proof's with the same transcript
+    and rng: the proofs share launches, not arithmetic."""
+    gens = [_proof_steps(params, pk, a, backend, t, r) for a, t, r in zip(advice_list, transcripts, rngs)]
+    return _drive(gens, backend)
+
+
+def _proof_steps(params, pk, advice_values, backend, transcript, rng):
+    """The proof as a generator: it yields a CommitRequest at each
+    commitment batch and receives its pending points; returns the proof
+    bytes."""
     c = pk.circuit
     dom = pk.domain
     n, k, m = c.n, c.k, c.m
@@ -680,7 +762,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     # the commitments are queued first; the transforms that need no
     # challenge run on the device while the host waits for them and writes
     # the transcript
-    pending = _commit_async(backend, adv_l, n, m)
+    pending = yield CommitRequest(adv_l, n, m, True)
     adv_c = backend.lagrange_to_coeff(adv_l, k, m)
     adv_e = backend.coeff_to_extended(adv_c, k, m, ek)
     for cm in pending.result():
@@ -695,7 +777,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
                                             theta=w(theta))
         blinds = [fr_random(rng, bf + 1) for _ in range(2 * L)]  # per lookup: input, then table
         perm_l = backend.permute_lookups(comp, n, u, L, np.concatenate(blinds[0::2]), np.concatenate(blinds[1::2]))
-        pending = _commit_async(backend, perm_l, n, 2 * L)
+        pending = yield CommitRequest(perm_l, n, 2 * L, True)
         perm_c = backend.lagrange_to_coeff(perm_l, k, 2 * L)
         perm_e = backend.coeff_to_extended(perm_c, k, 2 * L, ek)
         for cm in pending.result():
@@ -718,7 +800,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     # same point as its coefficients against g
     random_poly = backend.random_mont(rng, n)
     parts = [z_perm] + ([z_lk] if L else []) + [backend.coeff_to_lagrange(random_poly, k, 1)]
-    pending = _commit_async(backend, backend.cat(parts), n, sets + L + 1)
+    pending = yield CommitRequest(backend.cat(parts), n, sets + L + 1, True)
     zp_c = backend.lagrange_to_coeff(z_perm, k, sets)
     zp_e = backend.coeff_to_extended(zp_c, k, sets, ek)
     if L:
@@ -742,7 +824,8 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     pieces_n = dom.quotient_poly_degree
     h_blinds = fr_random(rng, pieces_n - 1)
     h_pieces = backend.quotient_pieces(q_coeff, n, pieces_n, h_blinds)
-    for cm in backend.commit(h_pieces, n, pieces_n):
+    pending = yield CommitRequest(h_pieces, n, pieces_n, False)
+    for cm in pending.result():
         transcript.write_point(cm)
     x = fr_int(transcript.squeeze_challenge())
 
@@ -803,7 +886,7 @@ def create_proof(params, pk, advice_values, backend, transcript, rng):
     queries += [(P(pk.fixed_coeffs, col), dom.rotate_omega(x, rot)) for col, rot in c.fixed_queries]
     queries += [(P(pk.sigma_coeffs, i), x) for i in range(m)]
     queries += [(P(h_poly, 0), x), (P(random_poly, 0), x)]
-    multi_open(params, backend, n, queries, transcript)
+    yield from _multi_open_steps(params, backend, n, queries, transcript)
     return transcript.finalize()
 
 
@@ -835,8 +918,9 @@ def construct_intermediate_sets(queries):
     return commits, set_of, point_sets
 
 
-def multi_open(params, backend, n, queries, transcript):
-    """KZGCommitmentScheme::multi_open (poly/kzg/mod.rs:1978-2600)."""
+def _multi_open_steps(params, backend, n, queries, transcript):
+    """KZGCommitmentScheme::multi_open (poly/kzg/mod.rs:1978-2600), as
+    proof steps: the f and pi commitments are yielded as CommitRequests."""
     x1 = fr_int(transcript.squeeze_challenge())
     x2 = fr_int(transcript.squeeze_challenge())
     commits, set_of, point_sets = construct_intermediate_sets(queries)
@@ -866,7 +950,8 @@ def multi_open(params, backend, n, queries, transcript):
         stack = backend.cat(f_parts)
         f_poly = backend.lincomb(stack, n, nsets, ints_to_mont([pow(x2, j, R) for j in range(nsets)]))
         qstack = backend.cat(q_polys)
-    transcript.write_point(backend.commit(f_poly, n, 1)[0])
+    pending = yield CommitRequest(f_poly, n, 1, False)
+    transcript.write_point(pending.result()[0])
     x3 = fr_int(transcript.squeeze_challenge())
     for v in backend.eval_polys(qstack, n, nsets, fr_mont(x3)):
         transcript.write_scalar(v)
@@ -881,7 +966,8 @@ def multi_open(params, backend, n, queries, transcript):
         allp = backend.cat([qstack, f_poly])
         final = backend.lincomb(allp, n, nsets + 1, scalars)
         pi_poly, pi_len = backend.kate_divide(final, n, 1, fr_mont(x3)), n
-    transcript.write_point(backend.commit(pi_poly, pi_len, 1)[0])
+    pending = yield CommitRequest(pi_poly, pi_len, 1, False)
+    transcript.write_point(pending.result()[0])
 
 
 # ---------------------------------------------------------------- GPU backend

@@ -27,7 +27,7 @@ import numpy as np
 
 from . import api
 from .kzg import CircuitTranscript
-from .plonk import GpuBackend, create_proof
+from .plonk import GpuBackend, create_proof, create_proofs
 from .rng import ChaCha20Rng
 
 
@@ -234,8 +234,12 @@ class ProofServer:
     limit beyond the slots)."""
 
     def __init__(self, entries, slots=4, hbm_budget=None, backend_factory=GpuBackend, lane_base=1,
-                 set_lane=api.execution_lane_set, keystore=None, fuse_commits=False):
+                 set_lane=api.execution_lane_set, keystore=None, fuse_commits=False, lockstep=1):
         self.entries = entries
+        # lockstep > 1: a worker takes up to that many waiting requests of
+        # one circuit and proves them together (plonk.create_proofs): each
+        # round's commitments of all of them are one MSM batch
+        self.lockstep = max(1, int(lockstep))
         self.keystore = keystore
         self.slots = slots
         self.budget = hbm_budget
@@ -294,11 +298,22 @@ class ProofServer:
         return req
 
     def _take(self):
-        """the oldest pending request that fits in the budget left"""
+        """the oldest pending request that fits in the budget left, with up
+        to lockstep - 1 later requests for the same key that also fit"""
         for i, req in enumerate(self._pending):
             if self.budget is None or self._in_use + req.bytes <= self.budget:
                 del self._pending[i]
-                return req
+                group, used = [req], req.bytes
+                if self.lockstep > 1:
+                    for other in list(self._pending):
+                        if len(group) == self.lockstep:
+                            break
+                        if other.pk is req.pk and other.backend is req.backend and (
+                                self.budget is None or self._in_use + used + other.bytes <= self.budget):
+                            self._pending.remove(other)
+                            group.append(other)
+                            used += other.bytes
+                return group
         return None
 
     def _worker(self, lane):
@@ -309,28 +324,42 @@ class ProofServer:
                 while True:
                     if self._stop and not self._pending:
                         return
-                    req = self._take()
-                    if req is not None:
+                    group = self._take()
+                    if group is not None:
                         break
                     self._cv.wait()
-                self._in_use += req.bytes
-                self._running += 1
+                size = sum(r.bytes for r in group)
+                self._in_use += size
+                self._running += len(group)
                 self.peak_in_use = max(self.peak_in_use, self._in_use)
                 self.peak_running = max(self.peak_running, self._running)
             try:
-                req.start = time.perf_counter()
-                req.proof = create_proof(req.params, req.pk, req.witness, req.backend,
-                                         CircuitTranscript(), ChaCha20Rng.from_label(req.seed))
-                req.finish = time.perf_counter()
-                req.future.set_result(req.proof)
-            except BaseException as e:  # the request fails, the server keeps serving
-                req.finish = time.perf_counter()
-                req.future.set_exception(e)
+                start = time.perf_counter()
+                for r in group:
+                    r.start = start
+                first = group[0]
+                if len(group) == 1:
+                    proofs = [create_proof(first.params, first.pk, first.witness, first.backend,
+                                           CircuitTranscript(), ChaCha20Rng.from_label(first.seed))]
+                else:
+                    proofs = create_proofs(first.params, first.pk, [r.witness for r in group], first.backend,
+                                           [CircuitTranscript() for _ in group],
+                                           [ChaCha20Rng.from_label(r.seed) for r in group])
+                finish = time.perf_counter()
+                for r, proof in zip(group, proofs):
+                    r.proof, r.finish = proof, finish
+                    r.future.set_result(proof)
+            except BaseException as e:  # the group fails, the server keeps serving
+                finish = time.perf_counter()
+                for r in group:
+                    r.finish = finish
+                    if not r.future.done():
+                        r.future.set_exception(e)
             finally:
                 with self._cv:
-                    self._in_use -= req.bytes
-                    self._running -= 1
-                    self.completed.append(req)
+                    self._in_use -= size
+                    self._running -= len(group)
+                    self.completed.extend(group)
                     self._cv.notify_all()
 
     def drain(self):

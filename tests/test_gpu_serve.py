@@ -58,3 +58,35 @@ def test_gpu_fused_commitments_equal_alone(gb):
         p, pk = entries[cid]
         alone = plonk.create_proof(p, pk, w, plonk.GpuBackend(p), CircuitTranscript(), ChaCha20Rng.from_label(seed))
         assert r.future.result() == alone
+
+
+def test_gpu_lockstep_proofs_equal_alone(gb):
+    """plonk.create_proofs on the GPU: four proofs of one circuit in
+    lockstep, every round's commitments fused into one MSM batch through the
+    asynchronous context entry point, give each proof's bytes as made
+    alone; and the server's lockstep groups (3 per lane) do too."""
+    from oracle import plonk_cpu, plonk_verify
+    c = circuit(9, 3, 4, 1)
+    fixed, advice, copies = c.synthesize()
+    p = ParamsKZG.unsafe_setup(9, plonk.fr_mont(TAU))
+    be = plonk.GpuBackend(p)
+    pk = plonk.keygen(p, c, be, fixed, copies)
+    w = ints_to_mont([v for col in advice for v in col])
+    seeds = ["ls%d" % i for i in range(4)]
+    together = plonk.create_proofs(p, pk, [w] * 4, be, [CircuitTranscript() for _ in seeds],
+                                   [ChaCha20Rng.from_label(s) for s in seeds])
+    alone = [plonk.create_proof(p, pk, w, be, CircuitTranscript(), ChaCha20Rng.from_label(s)) for s in seeds]
+    assert together == alone
+    hp = plonk_cpu.setup_params(9, TAU)
+    hpk = plonk.keygen(hp, c, plonk_cpu.OracleBackend(hp), fixed, copies)
+    oracle_proof = plonk.create_proof(hp, hpk, w, plonk_cpu.OracleBackend(hp), CircuitTranscript(),
+                                      ChaCha20Rng.from_label(seeds[0]))
+    assert together[0] == oracle_proof
+    assert plonk_verify.verify(hpk, together[0], TAU)
+    srv = serve.ProofServer({0: (p, pk)}, slots=2, lockstep=3)
+    reqs = [srv.submit(0, w, "sg%d" % i) for i in range(7)]
+    srv.drain()
+    srv.close()
+    for i, r in enumerate(reqs):
+        assert r.future.result() == plonk.create_proof(p, pk, w, be, CircuitTranscript(),
+                                                       ChaCha20Rng.from_label("sg%d" % i))

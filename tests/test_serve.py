@@ -55,3 +55,22 @@ def test_failed_request_isolated():
     srv.close()
     assert bad.future.exception() is not None
     assert good.future.result() == _alone(entries, 0, wit[0], "good")
+
+
+def test_lockstep_proofs_equal_alone():
+    """plonk.create_proofs runs several proofs of one circuit in lockstep
+    (their commitments requested together at every round): each proof's
+    bytes equal the proof made alone.  The server's lockstep groups give the
+    same bytes as well."""
+    entries, wit = _entries()
+    p, pk = entries[2]
+    seeds = ["lock-%d" % i for i in range(3)]
+    together = plonk.create_proofs(p, pk, [wit[2]] * 3, plonk_cpu.OracleBackend(p),
+                                   [CircuitTranscript() for _ in seeds], [ChaCha20Rng.from_label(s) for s in seeds])
+    assert together == [_alone(entries, 2, wit[2], s) for s in seeds]
+    srv = serve.ProofServer(entries, slots=2, backend_factory=plonk_cpu.OracleBackend, set_lane=None, lockstep=3)
+    reqs = [srv.submit(cid, wit[cid], "g-%d" % i) for i, cid in enumerate([2, 2, 1, 2, 0, 2])]
+    srv.drain()
+    for i, (r, cid) in enumerate(zip(reqs, [2, 2, 1, 2, 0, 2])):
+        assert r.future.result() == _alone(entries, cid, wit[cid], "g-%d" % i)
+    srv.close()
