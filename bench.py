@@ -803,6 +803,32 @@ def extras(gb, torch, n, rng, bases, args, peak):
     out["msm_2p20_resident_no_table_mpts_s"] = n / out["msm_2p20_resident_no_table_ms"] / 1e3
     out["msm_no_table_device_bytes"] = n * 96
     del d_b, d_s
+    # sustained throughput of back-to-back 2^20 MSMs from two lanes (two
+    # host threads, one CUDA stream each): one MSM's latency-bound tail
+    # overlaps the next one's sort and accumulation
+    ctx2 = gb.Bls12_381G1MsmContext(bases)
+    sets2 = gb.Bls12_381FrDeviceVec.upload(fr_uniform(4 * n, rng))
+
+    def lane_worker(lane, idx):
+        gb.execution_lane_set(lane)
+        for i in idx:
+            ctx2.device_batch(sets2, (i % 4) * n, n, 1)
+        gb.execution_lane_set(0)
+
+    lane_worker(1, range(2))
+    lane_worker(2, range(2))
+    rates = []
+    for _ in range(3):
+        ths = [threading.Thread(target=lane_worker, args=(1 + j, range(j, 10, 2))) for j in range(2)]
+        t0 = time.perf_counter()
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        rates.append(10 * n / (time.perf_counter() - t0) / 1e6)
+    out["msm_2p20_two_lanes_mpts_s"] = statistics.median(rates)
+    ctx2.close()
+    sets2.free()
     # 16 x NTT 2^20 forward / inverse and coset LDE 2^20 -> 2^22, resident
     log_n, count = 20, 16
     polys = fr_uniform(count << log_n, rng)
