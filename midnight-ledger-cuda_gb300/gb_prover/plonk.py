@@ -696,10 +696,16 @@ def _commit_requests(backend, reqs):
     return out
 
 
+# yielded by a proof generator after it has queued the device work that
+# follows a commitment request, before it waits for the points: the driver
+# lets every proof of the group queue that work first
+WAIT = object()
+
+
 def _drive(gens, backend):
     """Run proof generators in lockstep: each runs to its next commitment
-    request, the requests of a step are committed together, and each
-    generator continues with its pending points.  Returns the proofs."""
+    request (or WAIT), the requests of a step are committed together, and
+    each generator continues with its pending points.  Returns the proofs."""
     proofs = [None] * len(gens)
     sends = [None] * len(gens)
     live = list(range(len(gens)))
@@ -711,7 +717,11 @@ def _drive(gens, backend):
             except StopIteration as stop:
                 proofs[i] = stop.value
         live = [i for i, _ in asked]
-        for (i, _), pending in zip(asked, _commit_requests(backend, [r for _, r in asked])):
+        reqs = [(i, r) for i, r in asked if r is not WAIT]
+        for i, r in asked:
+            if r is WAIT:
+                sends[i] = None
+        for (i, _), pending in zip(reqs, _commit_requests(backend, [r for _, r in reqs])):
             sends[i] = pending
     return proofs
 
@@ -765,6 +775,7 @@ def _proof_steps(params, pk, advice_values, backend, transcript, rng):
     pending = yield CommitRequest(adv_l, n, m, True)
     adv_c = backend.lagrange_to_coeff(adv_l, k, m)
     adv_e = backend.coeff_to_extended(adv_c, k, m, ek)
+    yield WAIT
     for cm in pending.result():
         transcript.write_point(cm)
     theta = fr_int(transcript.squeeze_challenge())
@@ -780,6 +791,7 @@ def _proof_steps(params, pk, advice_values, backend, transcript, rng):
         pending = yield CommitRequest(perm_l, n, 2 * L, True)
         perm_c = backend.lagrange_to_coeff(perm_l, k, 2 * L)
         perm_e = backend.coeff_to_extended(perm_c, k, 2 * L, ek)
+        yield WAIT
         for cm in pending.result():
             transcript.write_point(cm)
     beta = fr_int(transcript.squeeze_challenge())
@@ -806,6 +818,7 @@ def _proof_steps(params, pk, advice_values, backend, transcript, rng):
     if L:
         zl_c = backend.lagrange_to_coeff(z_lk, k, L)
         zl_e = backend.coeff_to_extended(zl_c, k, L, ek)
+    yield WAIT
     cms = pending.result()
     for cm in cms[:sets + L]:
         transcript.write_point(cm)
