@@ -19,7 +19,7 @@ def build(force=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest_src:
         return LIB
     tmp = LIB + ".tmp"
-    cmd = ["gcc", "-O2", "-std=gnu11", "-shared", "-fPIC", "-pthread", "-o", tmp] + SRC + ["-lm"]
+    cmd = ["gcc", "-O3", "-std=gnu11", "-shared", "-fPIC", "-pthread", "-o", tmp] + SRC + ["-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

@@ -94,9 +94,11 @@ static void f_neg(u64 *out, const u64 *a, const field_t *F)
 }
 
 /* CIOS Montgomery multiplication: out = a*b*R^-1 mod p, fully reduced. */
-static void f_mul(u64 *out, const u64 *a, const u64 *b, const field_t *F)
+/* CIOS Montgomery product for a limb count n known where it is inlined, so
+ * that the loops unroll (the generic entry below dispatches on F->n) */
+static inline __attribute__((always_inline)) void f_mul_n(u64 *out, const u64 *a, const u64 *b,
+                                                          const field_t *F, const int n)
 {
-    const int n = F->n;
     u64 t[8] = {0};
     for (int i = 0; i < n; i++) {
         u64 carry = 0;
@@ -122,6 +124,13 @@ static void f_mul(u64 *out, const u64 *a, const u64 *b, const field_t *F)
     }
     if (t[n] || mp_geq(t, F->p, n)) mp_sub(t, t, F->p, n);
     memcpy(out, t, 8 * n);
+}
+
+static void f_mul(u64 *out, const u64 *a, const u64 *b, const field_t *F)
+{
+    if (F->n == 6) f_mul_n(out, a, b, F, 6);
+    else if (F->n == 4) f_mul_n(out, a, b, F, 4);
+    else f_mul_n(out, a, b, F, F->n);
 }
 
 /* exponent given as little-endian u64 limbs */
