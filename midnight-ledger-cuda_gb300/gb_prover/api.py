@@ -54,15 +54,13 @@ def _aff_arr(a):
 
 
 def _ptr(a):
-    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+    """the address of array a's data, for one foreign call; the caller keeps
+    a alive until that call returns (a named array, not a temporary)"""
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
 def _fr(v):
-    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(4)
-    r = RawFr()
-    for i in range(4):
-        r.limbs[i] = int(v[i])
-    return r
+    return RawFr.from_buffer_copy(np.ascontiguousarray(v, dtype=np.uint64).reshape(4))
 
 
 def execution_lane_set(lane):
