@@ -353,3 +353,34 @@ def test_context_device_batch_async(gb, orc):
     with pytest.raises(Exception):
         ctx.device_batch_async(dv, 0, n, 5)  # past the end of the vector
     ctx.close()
+
+
+def test_ticket_waited_on_another_thread(gb, orc):
+    """A ticket queued on one thread's lane and waited for by another thread
+    (on another lane): the wait checks the queuing lane's status and returns
+    the points."""
+    import threading
+    rng = np.random.default_rng(41)
+    n = 2000
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    s = orc.fr_random(n, rng)
+    ctx = gb.Bls12_381G1MsmContext(b)
+    dv = gb.Bls12_381FrDeviceVec.upload(s)
+    box = {}
+
+    def producer():
+        gb.execution_lane_set(3)
+        box["t"] = ctx.device_batch_async(dv, 0, n, 1)
+        gb.execution_lane_set(0)
+
+    def consumer():
+        gb.execution_lane_set(5)
+        box["p"] = box["t"].wait()
+        gb.execution_lane_set(0)
+
+    for f in (producer, consumer):
+        th = threading.Thread(target=f)
+        th.start()
+        th.join()
+    assert (affine_of(orc, box["p"][0]) == affine_of(orc, orc.g1_msm(b, s))).all()
+    ctx.close()
