@@ -928,15 +928,24 @@ static uint32_t chunk_length(uint64_t digits, double avg, int variant)
     return L2 >= 8 && L2 <= 2 * (uint64_t)L ? (uint32_t)L2 : L;
 }
 
-// Run a batch of MSMs.  precomputed: `points` is a table of nwin rows of
-// `stride` bases (row j = 2^(c*j) P); plain: `points` holds the bases.
-// Results (one Jacobian point per item) are written to d_out (device).
-static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precomputed, const affine_t *points,
-                          size_t stride, jacobian_t *d_out, cudaStream_t s)
+// The host half of a batch: its descriptors and launch sizes.
+struct batch_plan {
+    int c = 0, nwin = 0, variant = 1;
+    bool precomputed = false, coop_reduce = false;
+    size_t stride = 0;
+    uint32_t nitems = 0, K = 0, segs_per_item = 0, nseg = 0, G = 0, nblocks = 0, L = 0, S = 0, S_coop = 0;
+    uint64_t points_total = 0, digits_total = 0, nchunks = 0;
+    std::vector<item_desc> idesc;
+    std::vector<seg_desc> sdesc;
+    std::vector<blk_desc> bdesc;
+};
+
+static batch_plan plan_batch(const std::vector<msm_item> &items, int c, bool precomputed, size_t stride)
 {
-    set_smem_attrs();
+    batch_plan P;
     const uint32_t nitems = (uint32_t)items.size();
-    if (!nitems) return;
+    P.nitems = nitems;
+    if (!nitems) return P;
     const int nwin = windows_for(c);
     const uint32_t K = 1u << (c - 1);
     const uint32_t segs_per_item = precomputed ? 1u : (uint32_t)nwin;
@@ -1005,12 +1014,43 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= kCoopGroupBudget) S_coop *= 2;
     const uint64_t nchunks = std::max<uint64_t>(1, (digits_total + L - 1) / L);
 
-    dev_buf<item_desc> d_items(nitems, s);
-    dev_buf<seg_desc> d_segs(nseg, s);
-    dev_buf<blk_desc> d_blks(nblocks, s);
-    h2d(d_items, idesc.data(), nitems * sizeof(item_desc), s);
-    h2d(d_segs, sdesc.data(), nseg * sizeof(seg_desc), s);
-    h2d(d_blks, bdesc.data(), nblocks * sizeof(blk_desc), s);
+    P.c = c;
+    P.nwin = nwin;
+    P.variant = variant;
+    P.precomputed = precomputed;
+    P.coop_reduce = coop_reduce;
+    P.stride = stride;
+    P.K = K;
+    P.segs_per_item = segs_per_item;
+    P.nseg = nseg;
+    P.G = G;
+    P.nblocks = nblocks;
+    P.L = L;
+    P.S = S;
+    P.S_coop = S_coop;
+    P.points_total = points_total;
+    P.digits_total = digits_total;
+    P.nchunks = nchunks;
+    P.idesc = std::move(idesc);
+    P.sdesc = std::move(sdesc);
+    P.bdesc = std::move(bdesc);
+    return P;
+}
+
+// The device half: every launch of the batch, its scratch allocated and
+// freed in stream order on s, the descriptors already in device memory.
+// Queues device work only (no host synchronisation, no copy from host
+// memory), so a CUDA graph can capture it.
+static void run_planned(const batch_plan &P, const item_desc *d_items, const seg_desc *d_segs,
+                        const blk_desc *d_blks, const affine_t *points, jacobian_t *d_out, cudaStream_t s)
+{
+    const int c = P.c, variant = P.variant;
+    const bool precomputed = P.precomputed, coop_reduce = P.coop_reduce;
+    const size_t stride = P.stride;
+    const uint32_t nitems = P.nitems, K = P.K, segs_per_item = P.segs_per_item, nseg = P.nseg, G = P.G;
+    const uint32_t nblocks = P.nblocks, L = P.L, S = P.S, S_coop = P.S_coop;
+    const uint64_t points_total = P.points_total, digits_total = P.digits_total, nchunks = P.nchunks;
+    (void)precomputed;
     dev_buf<uint32_t> digits(std::max<uint64_t>(digits_total, 1), s), sorted(std::max<uint64_t>(digits_total, 1), s);
     dev_buf<uint32_t> hist((size_t)nblocks * K, s), counts(G, s), starts((size_t)G + 1, s);
     dev_buf<xyzz_t> buckets(G, s), head(nchunks, s), tail(nchunks, s);
@@ -1117,6 +1157,24 @@ static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precom
     GB_CHECK_LAUNCH();
     timed_end(tok_red, s, GB_SLOT_MSM_REDUCE);
     timed_end(tok_all, s, GB_SLOT_MSM_TOTAL);
+}
+
+// Run a batch of MSMs.  precomputed: `points` is a table of nwin rows of
+// `stride` bases (row j = 2^(c*j) P); plain: `points` holds the bases.
+// Results (one Jacobian point per item) are written to d_out (device).
+static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precomputed, const affine_t *points,
+                          size_t stride, jacobian_t *d_out, cudaStream_t s)
+{
+    set_smem_attrs();
+    if (items.empty()) return;
+    const batch_plan P = plan_batch(items, c, precomputed, stride);
+    dev_buf<item_desc> d_items(P.nitems, s);
+    dev_buf<seg_desc> d_segs(P.nseg, s);
+    dev_buf<blk_desc> d_blks(P.nblocks, s);
+    h2d(d_items, P.idesc.data(), P.nitems * sizeof(item_desc), s);
+    h2d(d_segs, P.sdesc.data(), P.nseg * sizeof(seg_desc), s);
+    h2d(d_blks, P.bdesc.data(), P.nblocks * sizeof(blk_desc), s);
+    run_planned(P, d_items, d_segs, d_blks, points, d_out, s);
 }
 
 }  // namespace gb
