@@ -516,6 +516,13 @@ GB_API RustError gb_msm_ticket_wait(void *ticket, RawG1Projective *out);
  * output may be NULL).  Host buffers of 2^k affine points. */
 GB_API RustError gb_g1_to_lagrange(RawG1Affine *out, const RawG1Affine *g, uint32_t k);
 GB_API RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, RawFr tau, uint32_t k);
+/* Jacobian MSM results (Montgomery limbs) to affine Montgomery coordinates
+ * on the host, with one field inversion for the batch; the point at
+ * infinity becomes all zeros.  The reference's Rust callers do this with
+ * blst's p1_to_affine on every commitment before it is written to the
+ * transcript (vendor/midnight-curves-0.3.1/src/bls12_381/g1.rs:109-123
+ * From<G1Projective>, :1127 batch_normalize).  No device work. */
+GB_API RustError gb_g1_jacobian_to_affine_batch(RawG1Affine *out, const RawG1Projective *in, size_t n);
 /* Kate quotients (f(X) - f(point)) / (X - point) of poly_count resident
  * polynomials (the division of the reference's multi-open kate scan,
  * bls12_381_g1_msm.cu:1923-1959), into a new device vector */

@@ -10,6 +10,8 @@
 // over XYZZ points; a butterfly is (a, b) -> (a + b, [w^j](a - b)) with a
 // double-and-add scalar multiplication; a final pass scales by n^-1, converts
 // to affine and applies the bit-reversal permutation.
+#include <vector>
+
 #include "gb_ntt.cuh"
 #include "gb_vec.cuh"
 
@@ -115,6 +117,155 @@ static void g_to_lagrange_device(affine_t *d_out, const affine_t *d_in, uint32_t
 
 using namespace gb;
 
+// ---------------------------------------------------------------------------
+// Host-side Jacobian -> affine conversion of MSM results (blst's
+// p1_to_affine, which the reference's Rust callers apply to every
+// commitment before it is hashed into the transcript): 6 x 64-bit limbs,
+// Montgomery products with 128-bit intermediates, one binary-GCD inverse
+// per batch (Montgomery's trick).  Variable time: commitments are public.
+namespace hostfp {
+
+typedef unsigned __int128 u128;
+struct fp64 {
+    uint64_t l[6];
+};
+
+static const fp64 kP = {{0xb9feffffffffaaabull, 0x1eabfffeb153ffffull, 0x6730d2a0f6b0f624ull, 0x64774b84f38512bfull,
+                         0x4b1ba7b6434bacd7ull, 0x1a0111ea397fe69aull}};
+static const uint64_t kN0 = 0x89f3fffcfffcfffdull;  // -p^-1 mod 2^64
+static const fp64 kOne = {{0x760900000002fffdull, 0xebf4000bc40c0002ull, 0x5f48985753c758baull, 0x77ce585370525745ull,
+                           0x5c071a97a256ec6dull, 0x15f65ec3fa80e493ull}};  // R mod p
+// R^3 mod p (R = 2^384): a Montgomery product with it takes the plain
+// inverse of a Montgomery value zR to the Montgomery form of 1/z
+static const fp64 kR3 = {{0xed48ac6bd94ca1e0ull, 0x315f831e03a7adf8ull, 0x9a53352a615e29ddull, 0x34c04e5e921e1761ull,
+                          0x2512d43565724728ull, 0x0aa6346091755d4dull}};
+
+static bool is_zero(const fp64 &a)
+{
+    uint64_t t = 0;
+    for (int i = 0; i < 6; i++) t |= a.l[i];
+    return t == 0;
+}
+
+static bool geq(const fp64 &a, const fp64 &b)
+{
+    for (int i = 5; i >= 0; i--)
+        if (a.l[i] != b.l[i]) return a.l[i] > b.l[i];
+    return true;
+}
+
+static void sub_in(fp64 &a, const fp64 &b)
+{
+    uint64_t borrow = 0;
+    for (int i = 0; i < 6; i++) {
+        const u128 d = (u128)a.l[i] - b.l[i] - borrow;
+        a.l[i] = (uint64_t)d;
+        borrow = (uint64_t)(d >> 64) & 1;
+    }
+}
+
+static void add_in(fp64 &a, const fp64 &b)
+{
+    uint64_t carry = 0;
+    for (int i = 0; i < 6; i++) {
+        const u128 t = (u128)a.l[i] + b.l[i] + carry;
+        a.l[i] = (uint64_t)t;
+        carry = (uint64_t)(t >> 64);
+    }
+}
+
+static void shr1(fp64 &a)
+{
+    for (int i = 0; i < 5; i++) a.l[i] = (a.l[i] >> 1) | (a.l[i + 1] << 63);
+    a.l[5] >>= 1;
+}
+
+// x / 2 mod p for x < p (x + p < 2^382: no carry out of six limbs)
+static void half_mod(fp64 &x)
+{
+    if (x.l[0] & 1) add_in(x, kP);
+    shr1(x);
+}
+
+// a - b mod p for a, b < p
+static void sub_mod(fp64 &a, const fp64 &b)
+{
+    if (geq(a, b)) {
+        sub_in(a, b);
+    } else {
+        add_in(a, kP);
+        sub_in(a, b);
+    }
+}
+
+static void reduce(fp64 &a)
+{
+    while (geq(a, kP)) sub_in(a, kP);
+}
+
+// a b R^-1 mod p (CIOS), inputs < p, result < p
+static fp64 mont_mul(const fp64 &a, const fp64 &b)
+{
+    uint64_t t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 6; i++) {
+        uint64_t carry = 0;
+        for (int j = 0; j < 6; j++) {
+            const u128 x = (u128)a.l[j] * b.l[i] + t[j] + carry;
+            t[j] = (uint64_t)x;
+            carry = (uint64_t)(x >> 64);
+        }
+        u128 x = (u128)t[6] + carry;
+        t[6] = (uint64_t)x;
+        t[7] = (uint64_t)(x >> 64);
+        const uint64_t m = t[0] * kN0;
+        x = (u128)m * kP.l[0] + t[0];
+        carry = (uint64_t)(x >> 64);
+        for (int j = 1; j < 6; j++) {
+            x = (u128)m * kP.l[j] + t[j] + carry;
+            t[j - 1] = (uint64_t)x;
+            carry = (uint64_t)(x >> 64);
+        }
+        x = (u128)t[6] + carry;
+        t[5] = (uint64_t)x;
+        t[6] = t[7] + (uint64_t)(x >> 64);
+    }
+    fp64 r;
+    for (int i = 0; i < 6; i++) r.l[i] = t[i];
+    if (t[6] || geq(r, kP)) sub_in(r, kP);
+    return r;
+}
+
+// a^-1 mod p for 0 < a < p (binary extended Euclid: x1 a = u, x2 a = v)
+static fp64 inverse(const fp64 &a)
+{
+    fp64 u = a, v = kP, x1 = {{1, 0, 0, 0, 0, 0}}, x2 = {{0, 0, 0, 0, 0, 0}};
+    auto is_one = [&](const fp64 &w) {
+        for (int i = 1; i < 6; i++)
+            if (w.l[i]) return false;
+        return w.l[0] == 1;
+    };
+    while (!is_one(u) && !is_one(v)) {
+        while (!(u.l[0] & 1)) {
+            shr1(u);
+            half_mod(x1);
+        }
+        while (!(v.l[0] & 1)) {
+            shr1(v);
+            half_mod(x2);
+        }
+        if (geq(u, v)) {
+            sub_in(u, v);
+            sub_mod(x1, x2);
+        } else {
+            sub_in(v, u);
+            sub_mod(x2, x1);
+        }
+    }
+    return is_one(u) ? x1 : x2;
+}
+
+}  // namespace hostfp
+
 extern "C" {
 
 // g_lagrange = iFFT(g) * n^-1 (arithmetic.rs:34-50); host buffers of 2^k points
@@ -162,6 +313,57 @@ RustError gb_kzg_setup(RawG1Affine *g_out, RawG1Affine *g_lagrange_out, RawFr ta
         d2h(g_lagrange_out, pts, n * sizeof(affine_t), s);
     }
     lane_sync(s);
+    return ok();
+    GB_ENTRY_END
+}
+
+// Jacobian points (Montgomery, as the MSM entry points return them) to
+// affine Montgomery coordinates; the point at infinity (Z = 0) becomes all
+// zeros, the reference's RawG1Affine convention for it.  Host only: no
+// device memory or stream is touched.  out and in may not overlap.
+RustError gb_g1_jacobian_to_affine_batch(RawG1Affine *out_raw, const RawG1Projective *in_raw, size_t n)
+{
+    if (n && (!out_raw || !in_raw)) return make_error((int)cudaErrorInvalidValue, "invalid point conversion arguments");
+    GB_ENTRY_BEGIN
+    using namespace hostfp;
+    static_assert(sizeof(RawG1Projective) == 18 * sizeof(uint64_t), "projective layout");
+    static_assert(sizeof(RawG1Affine) == 12 * sizeof(uint64_t), "affine layout");
+    const uint64_t *in = reinterpret_cast<const uint64_t *>(in_raw);
+    uint64_t *out = reinterpret_cast<uint64_t *>(out_raw);
+    std::vector<fp64> z(n), prefix(n);
+    fp64 acc = kOne;  // running product of the nonzero z, Montgomery form
+    for (size_t i = 0; i < n; i++) {
+        for (int k = 0; k < 6; k++) z[i].l[k] = in[18 * i + 12 + k];
+        reduce(z[i]);
+        prefix[i] = acc;
+        if (!is_zero(z[i])) acc = mont_mul(acc, z[i]);
+    }
+    // acc holds P R for the product P of the nonzero z: its plain inverse is
+    // 1 / (P R), and the Montgomery product with R^3 gives R / P, the
+    // Montgomery form of 1 / P
+    fp64 inv = mont_mul(inverse(acc), kR3);
+    for (size_t i = n; i-- > 0;) {
+        uint64_t *o = out + 12 * i;
+        if (is_zero(z[i])) {
+            for (int k = 0; k < 12; k++) o[k] = 0;
+            continue;
+        }
+        const fp64 zi = mont_mul(inv, prefix[i]);
+        inv = mont_mul(inv, z[i]);
+        fp64 x, y;
+        for (int k = 0; k < 6; k++) {
+            x.l[k] = in[18 * i + k];
+            y.l[k] = in[18 * i + 6 + k];
+        }
+        reduce(x);
+        reduce(y);
+        const fp64 zi2 = mont_mul(zi, zi);
+        const fp64 ax = mont_mul(x, zi2), ay = mont_mul(y, mont_mul(zi2, zi));
+        for (int k = 0; k < 6; k++) {
+            o[k] = ax.l[k];
+            o[6 + k] = ay.l[k];
+        }
+    }
     return ok();
     GB_ENTRY_END
 }

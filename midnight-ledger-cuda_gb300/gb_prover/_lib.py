@@ -119,6 +119,7 @@ def _declare(L):
         "gb_imad_peak": (E, [ctypes.POINTER(ctypes.c_double)]),
         "gb_imad_probe": (E, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
         "gb_g1_to_lagrange": (E, [vp, vp, u32]),
+        "gb_g1_jacobian_to_affine_batch": (E, [vp, vp, sz]),
         "midnight_sppark_bls12_381_fr_device_eval_polys": (E, [vp, vp, sz, sz, fr]),
         "gb_fr_device_kate_divide": (E, [vp, vp, sz, sz, fr]),
         "gb_fr_device_eval_many": (E, [vp, vp, vp, vp, sz, sz]),

@@ -32,62 +32,76 @@ def _limbs(v, n):
 
 
 def _int(row):
-    return sum(int(x) << (64 * i) for i, x in enumerate(row))
+    """little-endian u64 limbs -> integer"""
+    return int.from_bytes(np.ascontiguousarray(row, dtype="<u8").tobytes(), "little")
+
+
+# Montgomery factors of the affine conversion: with X = x R, Y = y R and
+# Z = z R (mod p), the affine point's Montgomery coordinates are
+# X R^2 / Z^2 and Y R^3 / Z^3
+_FP_R2 = _FP_R * _FP_R % P_MOD
+_FP_R3 = _FP_R2 * _FP_R % P_MOD
 
 
 # ---------------------------------------------------------------- point encodings (host side)
 
 def affine_from_projective(jac):
     """Jacobian (18 u64, Montgomery) -> affine (12 u64); infinity -> zeros."""
-    jac = np.asarray(jac, dtype=np.uint64).reshape(18)
-    z = _int(jac[12:18]) * _FP_RINV % P_MOD
-    if z == 0:
-        return np.zeros(12, dtype=np.uint64)
-    x = _int(jac[0:6]) * _FP_RINV % P_MOD
-    y = _int(jac[6:12]) * _FP_RINV % P_MOD
-    zi = pow(z, -1, P_MOD)
-    ax, ay = x * zi * zi % P_MOD, y * zi * zi * zi % P_MOD
-    return np.array(_limbs(ax * _FP_R % P_MOD, 6) + _limbs(ay * _FP_R % P_MOD, 6), dtype=np.uint64)
+    return affine_from_projective_batch(np.asarray(jac, dtype=np.uint64).reshape(1, 18))[0]
 
 
 def affine_from_projective_batch(jacs):
     """affine_from_projective over a batch with one field inversion
-    (Montgomery's trick): (m, 18) Jacobian rows -> (m, 12) affine rows."""
-    jacs = np.asarray(jacs, dtype=np.uint64).reshape(-1, 18)
-    zs = [_int(j[12:18]) * _FP_RINV % P_MOD for j in jacs]
+    (Montgomery's trick): (m, 18) Jacobian rows -> (m, 12) affine rows.
+    Through the library's host-side gb_g1_jacobian_to_affine_batch once
+    this process has loaded it, else in Python integers."""
+    from . import _lib as _l
+    if _l._lib is not None:
+        src = np.ascontiguousarray(jacs, dtype=np.uint64).reshape(-1, 18)
+        out = np.empty((len(src), 12), dtype=np.uint64)
+        check(_l._lib.gb_g1_jacobian_to_affine_batch(_ptr(out), _ptr(src), len(src)))
+        return out
+    return _affine_from_projective_batch_py(jacs)
+
+
+def _affine_from_projective_batch_py(jacs):
+    raw = np.ascontiguousarray(jacs, dtype="<u8").reshape(-1, 18).tobytes()
+    m = len(raw) // 144
+    frm = int.from_bytes
+    zs = [frm(raw[144 * i + 96:144 * i + 144], "little") % P_MOD for i in range(m)]
     prefix, acc = [], 1
     for z in zs:
         prefix.append(acc)
         if z:
             acc = acc * z % P_MOD
     inv = pow(acc, -1, P_MOD)
-    out = np.zeros((len(zs), 12), dtype=np.uint64)
-    for i in range(len(zs) - 1, -1, -1):
+    rows = [bytes(96)] * m
+    for i in range(m - 1, -1, -1):
         z = zs[i]
         if z == 0:
             continue
         zi = inv * prefix[i] % P_MOD
         inv = inv * z % P_MOD
-        x = _int(jacs[i, 0:6]) * _FP_RINV % P_MOD
-        y = _int(jacs[i, 6:12]) * _FP_RINV % P_MOD
         zi2 = zi * zi % P_MOD
-        ax, ay = x * zi2 % P_MOD, y * zi2 * zi % P_MOD
-        out[i] = _limbs(ax * _FP_R % P_MOD, 6) + _limbs(ay * _FP_R % P_MOD, 6)
-    return out
+        ax = frm(raw[144 * i:144 * i + 48], "little") * zi2 % P_MOD * _FP_R2 % P_MOD
+        ay = frm(raw[144 * i + 48:144 * i + 96], "little") * zi2 % P_MOD * zi % P_MOD * _FP_R3 % P_MOD
+        rows[i] = ax.to_bytes(48, "little") + ay.to_bytes(48, "little")
+    return np.frombuffer(bytearray(b"".join(rows)), dtype="<u8").reshape(m, 12)
 
 
 def compress(affine):
     """zcash 48-byte compressed encoding of an affine point (g1.rs:1179-1211)."""
-    a = np.asarray(affine, dtype=np.uint64).reshape(12)
-    if not a.any():
+    b = np.ascontiguousarray(affine, dtype="<u8").reshape(12).tobytes()
+    xm, ym = int.from_bytes(b[:48], "little"), int.from_bytes(b[48:], "little")
+    if not xm and not ym:
         return bytes([0xC0]) + bytes(47)
-    x = _int(a[0:6]) * _FP_RINV % P_MOD
-    y = _int(a[6:12]) * _FP_RINV % P_MOD
-    b = bytearray(x.to_bytes(48, "big"))
-    b[0] |= 0x80
+    x = xm * _FP_RINV % P_MOD
+    y = ym * _FP_RINV % P_MOD
+    out = bytearray(x.to_bytes(48, "big"))
+    out[0] |= 0x80
     if y > P_MOD - y:
-        b[0] |= 0x20
-    return bytes(b)
+        out[0] |= 0x20
+    return bytes(out)
 
 
 def from_uncompressed(b96):
@@ -106,13 +120,13 @@ def from_uncompressed(b96):
 
 def fr_to_repr(fr):
     """Fr (Montgomery limbs) -> 32-byte little-endian canonical repr."""
-    return (_int(np.asarray(fr, dtype=np.uint64).reshape(4)) * _FR_RINV % R_MOD).to_bytes(32, "little")
+    return (_int(np.asarray(fr).reshape(4)) * _FR_RINV % R_MOD).to_bytes(32, "little")
 
 
 def fr_from_uniform_bytes(b64):
     """fq.rs:704-725: the 512-bit little-endian value of the bytes, mod r."""
     v = int.from_bytes(b64, "little") % R_MOD
-    return np.array(_limbs(v * _FR_R % R_MOD, 4), dtype=np.uint64)
+    return np.frombuffer(bytearray((v * _FR_R % R_MOD).to_bytes(32, "little")), dtype="<u8")
 
 
 # ---------------------------------------------------------------- SRS
@@ -237,6 +251,12 @@ class CircuitTranscript:
 
     def write_scalar(self, fr):
         b = fr_to_repr(fr)
+        self._absorb(b)
+        self.buffer += b
+
+    def write_scalar_int(self, v):
+        """write_scalar of the field element with canonical value v mod r"""
+        b = (v % R_MOD).to_bytes(32, "little")
         self._absorb(b)
         self.buffer += b
 

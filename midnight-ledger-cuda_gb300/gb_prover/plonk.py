@@ -857,33 +857,33 @@ def _proof_steps(params, pk, advice_values, backend, transcript, rng):
         reqs.append((zp_c, sets, w(x_last)))
     if L:
         reqs += [(zl_c, L, w(x)), (zl_c, L, w(x_next)), (perm_c, 2 * L, w(x)), (perm_c, 2 * L, w(x_prev))]
-    vals = [[fr_int(v) for v in arr] for arr in backend.eval_many(reqs, n)]
+    vals = [mont_to_ints(arr) for arr in backend.eval_many(reqs, n)]
     adv_at = dict(zip(adv_rots, vals[:len(adv_rots)]))
     fix_at = dict(zip(fix_rots, vals[len(adv_rots):len(adv_rots) + len(fix_rots)]))
     rest = iter(vals[len(adv_rots) + len(fix_rots):])
     for col, rot in c.advice_queries:
-        transcript.write_scalar(w(adv_at[rot][col]))
+        transcript.write_scalar_int(adv_at[rot][col])
     for col, rot in c.fixed_queries:
-        transcript.write_scalar(w(fix_at[rot][col]))
+        transcript.write_scalar_int(fix_at[rot][col])
     # vanishing.evaluate: the combined h polynomial and the random eval (vanishing/prover.rs:321-383)
     split = pow(x, n - 1, R)
     h_poly = backend.lincomb(h_pieces, n, pieces_n, ints_to_mont([pow(split, i, R) for i in range(pieces_n)]))
     random_eval = next(rest)[0]
-    transcript.write_scalar(w(random_eval))
+    transcript.write_scalar_int(random_eval)
     for v in next(rest):
-        transcript.write_scalar(w(v))
+        transcript.write_scalar_int(v)
     zp_x, zp_xn = next(rest), next(rest)
     zp_xl = next(rest) if sets > 1 else []
     for s in range(sets):
-        transcript.write_scalar(w(zp_x[s]))
-        transcript.write_scalar(w(zp_xn[s]))
+        transcript.write_scalar_int(zp_x[s])
+        transcript.write_scalar_int(zp_xn[s])
         if s + 1 < sets:
-            transcript.write_scalar(w(zp_xl[s]))
+            transcript.write_scalar_int(zp_xl[s])
     if L:
         zl_x, zl_xn, pp_x, pp_xp = next(rest), next(rest), next(rest), next(rest)
         for li in range(L):
             for v in (zl_x[li], zl_xn[li], pp_x[2 * li], pp_xp[2 * li], pp_x[2 * li + 1]):
-                transcript.write_scalar(w(v))
+                transcript.write_scalar_int(v)
 
     # ---- queries (prover.rs:1993-2063) and multi-open
     P = lambda h, i: (h, i)  # noqa: E731  (polynomial = (handle, index))

@@ -175,52 +175,39 @@ class ChaCha20Rng:
         return self._words(nw).astype("<u4").tobytes()[:n]
 
 
-_R_LIMBS = np.array([(R_MOD >> (64 * i)) & _MASK64 for i in range(4)], dtype=np.uint64)
 _R2 = pow(2, 512, R_MOD)
-
-
-def _below_r(raw):
-    """rows of 4 little-endian u64 limbs that are < r"""
-    lt = np.zeros(len(raw), dtype=bool)
-    eq = np.ones(len(raw), dtype=bool)
-    for i in (3, 2, 1, 0):
-        lt |= eq & (raw[:, i] < _R_LIMBS[i])
-        eq &= raw[:, i] == _R_LIMBS[i]
-    return lt
 
 
 def ints_to_mont(vals):
     """canonical integers -> (n, 4) u64 Montgomery limbs (R = 2^256)"""
-    out = np.empty((len(vals), 4), dtype=np.uint64)
-    for i, v in enumerate(vals):
-        m = (int(v) << 256) % R_MOD
-        out[i] = (m & _MASK64, (m >> 64) & _MASK64, (m >> 128) & _MASK64, m >> 192)
-    return out
+    b = b"".join(((int(v) << 256) % R_MOD).to_bytes(32, "little") for v in vals)
+    return np.frombuffer(bytearray(b), dtype="<u8").reshape(-1, 4)
 
 
 _RINV = pow(1 << 256, -1, R_MOD)
 
 
+def _row_ints(arr):
+    """(n, 4) u64 limb rows -> their integer values"""
+    b = np.ascontiguousarray(arr, dtype="<u8").reshape(-1, 4).tobytes()
+    frm = int.from_bytes
+    return [frm(b[i:i + 32], "little") for i in range(0, len(b), 32)]
+
+
 def mont_to_ints(arr):
     """(n, 4) u64 Montgomery limbs -> canonical integers"""
-    arr = np.asarray(arr, dtype=np.uint64).reshape(-1, 4)
     rinv = _RINV
-    out = []
-    for row in arr:
-        v = int(row[0]) | int(row[1]) << 64 | int(row[2]) << 128 | int(row[3]) << 192
-        out.append(v * rinv % R_MOD)
-    return out
+    return [v * rinv % R_MOD for v in _row_ints(arr)]
 
 
 def raw_to_mont(raw):
     """canonical limb rows (< r) -> Montgomery rows"""
-    vals = [int(r[0]) | int(r[1]) << 64 | int(r[2]) << 128 | int(r[3]) << 192 for r in raw]
-    return ints_to_mont(vals)
+    return ints_to_mont(_row_ints(raw))
 
 
 def fr_random(rng: ChaCha20Rng, n):
     """n field elements by Fq::random's rejection rule, Montgomery form (n, 4)."""
-    return raw_to_mont(fr_random_raw(rng, n))
+    return ints_to_mont(_fr_random_ints(rng, n))
 
 
 # R^2 mod r as limbs: a Montgomery product with it maps a canonical value
@@ -228,25 +215,35 @@ def fr_random(rng: ChaCha20Rng, n):
 R2_LIMBS = np.array([(_R2 >> (64 * i)) & _MASK64 for i in range(4)], dtype=np.uint64)
 
 
+_TOP_MASK = (1 << 255) - 1
+
+
+def _fr_random_ints(rng: ChaCha20Rng, n):
+    """The canonical values of n draws of fr_random: each candidate is four
+    next_u64 words (eight keystream words, one little-endian 256-bit value)
+    with bit 255 cleared, kept when below r."""
+    got = []
+    frm = int.from_bytes
+    while len(got) < n:
+        want = n - len(got)
+        draw = want + want // 8 + 8
+        b = np.ascontiguousarray(rng._words(8 * draw), dtype="<u4").tobytes()
+        used = draw
+        for i in range(draw):
+            v = frm(b[32 * i:32 * i + 32], "little") & _TOP_MASK
+            if v < R_MOD:
+                got.append(v)
+                if len(got) == n:
+                    used = i + 1
+                    break
+        # the draws after the last one taken go back, so the stream matches
+        # one-at-a-time sampling
+        rng._pos -= (draw - used) * 8
+    return got
+
+
 def fr_random_raw(rng: ChaCha20Rng, n):
     """The draws of fr_random as canonical limb rows (n, 4), before the
     Montgomery conversion."""
-    got = []
-    total = 0
-    while total < n:
-        want = n - total
-        draw = want + want // 8 + 8
-        raw = rng.next_u64_array(4 * draw).reshape(-1, 4)
-        raw[:, 3] &= np.uint64(0x7FFFFFFFFFFFFFFF)
-        ok = _below_r(raw)
-        # accept in draw order; once `want` are accepted, give the unused
-        # draws back so the stream matches one-at-a-time sampling
-        idx = np.flatnonzero(ok)
-        if len(idx) >= want:
-            last = idx[want - 1]
-            unused = draw - (last + 1)
-            rng._pos -= int(unused) * 8
-            idx = idx[:want]
-        got.append(raw[idx])
-        total += len(idx)
-    return np.concatenate(got) if got else np.zeros((0, 4), np.uint64)
+    b = b"".join(v.to_bytes(32, "little") for v in _fr_random_ints(rng, n))
+    return np.frombuffer(bytearray(b), dtype="<u8").reshape(-1, 4)

@@ -87,3 +87,36 @@ def test_context_and_multiopen_validation_without_gpu(gb):
         ctypes.byref(h), gb.api._ptr(polys), gb.api._ptr(polys), 8, 1, 6, gb.api._ptr(polys), gb.api._ptr(polys), 1)
     with pytest.raises(gb.MsmError, match="invalid resident lookup permutation arguments"):
         gb.api.check(err)
+
+
+def test_host_affine_conversion_matches_oracle(gb, orc):
+    """gb_g1_jacobian_to_affine_batch (host only, no GPU needed) against the
+    oracle's conversion: real points in Jacobian form with random Z, the
+    point at infinity among them, batches of 0..9 points."""
+    from gb_prover import kzg
+    P = kzg.P_MOD
+    rng = np.random.default_rng(11)
+    g_aff = orc.g1_generator_mul_batch(orc.fr_from_ints([3, 5, 7, 11, 13, 17, 19, 23]))
+    gb.lib()
+    for trial in range(60):
+        m = int(rng.integers(0, 10))
+        rows = []
+        for i in range(m):
+            a = g_aff[int(rng.integers(0, len(g_aff)))]
+            if rng.random() < 0.2:
+                rows.append(np.zeros(18, dtype=np.uint64))
+                continue
+            # (x, y) -> (x z^2, y z^3, z) in Montgomery form for a random z
+            x = kzg._int(a[0:6]) * kzg._FP_RINV % P
+            y = kzg._int(a[6:12]) * kzg._FP_RINV % P
+            z = int.from_bytes(rng.bytes(48), "little") % P or 1
+            vals = [x * z * z % P, y * z * z * z % P, z]
+            rows.append(np.array([limb for v in vals for limb in kzg._limbs(v * kzg._FP_R % P, 6)],
+                                 dtype=np.uint64))
+        jac = np.array(rows, dtype=np.uint64).reshape(m, 18)
+        got = kzg.affine_from_projective_batch(jac)
+        want = orc.g1_to_affine(jac) if m else np.zeros((0, 12), np.uint64)
+        assert got.shape == (m, 12)
+        assert (got == want).all(), trial
+    with pytest.raises(gb.MsmError):
+        gb.api.check(gb.lib().gb_g1_jacobian_to_affine_batch(None, None, 1))
