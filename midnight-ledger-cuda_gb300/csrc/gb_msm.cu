@@ -906,7 +906,7 @@ static void u32_exclusive_scan(const uint32_t *in, uint32_t n, uint32_t *out, cu
 // that the chunks fill whole waves of resident accumulation blocks (a 2^16
 // MSM's 65536 chunks of 16 fill 84 % of one wave on 152 SMs; chunks of 14
 // fill 96 %; a 2^20 MSM's 3.4 waves of 64 become 3 of 72).
-static uint32_t chunk_length(uint64_t digits, double avg, int variant)
+static uint32_t chunk_length(uint64_t digits, double avg, uint32_t G, int variant)
 {
     uint32_t L = (uint32_t)std::max(8.0, std::min(64.0, avg * 0.5));
     static int per_sm[3] = {0, 0, 0}, sms = 0;
@@ -925,7 +925,20 @@ static uint32_t chunk_length(uint64_t digits, double avg, int variant)
     // there are several, up when there is less than one
     const uint64_t waves = std::max<uint64_t>(1, digits / ((uint64_t)L * wave));
     const uint64_t L2 = (digits + waves * wave - 1) / (waves * wave);
-    return L2 >= 8 && L2 <= 2 * (uint64_t)L ? (uint32_t)L2 : L;
+    if (L2 >= 8 && L2 <= 2 * (uint64_t)L) return (uint32_t)L2;
+    if (L2 >= 8) return L;
+    // Less than one wave of 8-digit chunks (small MSMs): the accumulation
+    // takes about L dependent additions per thread and the fix-up about
+    // avg / L (the chunks a bucket spans; cooperative groups up to
+    // kCoopFixupMaxBuckets buckets, single threads, ~1.6x slower, beyond),
+    // so L ~ sqrt(avg x their latency ratio); and at least 3 digits per
+    // resident chunk slot, where the additions start to queue on the
+    // multiply-add pipe.  Measured on GB300 (one MSM, resident bases):
+    // 2^10 points 0.65 -> 0.41 ms, 2^12 0.50 -> 0.45 ms, 2^14 0.97 -> 0.59 ms.
+    const double ratio = G <= kCoopFixupMaxBuckets ? 0.8 : 1.3;
+    const uint64_t by_latency = (uint64_t)std::lround(std::sqrt(avg * ratio));
+    const uint64_t by_load = (3 * digits + wave - 1) / wave;
+    return (uint32_t)std::min<uint64_t>(L, std::max<uint64_t>(4, std::max(by_latency, by_load)));
 }
 
 // The host half of a batch: its descriptors and launch sizes.
@@ -997,7 +1010,7 @@ static batch_plan plan_batch(const std::vector<msm_item> &items, int c, bool pre
     const uint32_t nblocks = (uint32_t)bdesc.size();
     const double avg = (double)digits_total / (double)G;
     const int variant = default_acc_variant();
-    const uint32_t L = chunk_length(digits_total, avg, variant);
+    const uint32_t L = chunk_length(digits_total, avg, G, variant);
     // reduction sub-segments: ~64K threads over the batch, 32..8192 per segment
     uint32_t S = 32;
     while (S < 8192 && (uint64_t)S * 2 * nseg <= 65536) S *= 2;
