@@ -509,6 +509,14 @@ GB_API RustError gb_g1_msm_context_device_batch_async(void **ticket, void *conte
  * (out may be NULL) and releases the ticket; a lane wait status set since
  * the lane's previous synchronisation is returned as cudaErrorLaunchTimeout */
 GB_API RustError gb_msm_ticket_wait(void *ticket, RawG1Projective *out);
+/* CUDA-graph replay of context batches (no FFI counterpart: the reference
+ * launches each stage of bls12_381_g1_msm.cu:172-215 one by one).  A batch
+ * whose shape and bases were seen before on the same lane replays the graph
+ * captured the first time, with its descriptors refreshed; on by default
+ * (GB_MSM_GRAPHS=0 turns it off at start-up).  The counters are the graphs
+ * captured and the batches replayed since the process started. */
+GB_API RustError gb_msm_graphs_enable(int on);
+GB_API RustError gb_msm_graph_stats(unsigned long long *captures, unsigned long long *launches);
 /* KZG SRS (no FFI counterpart; the reference does these in Rust on the CPU):
  * g_lagrange = iFFT(g) * n^-1 over G1 for 2^k points (arithmetic.rs:34-50,
  * params.rs:60-77 downsize), and the seeded-tau setup of params.rs:79-129

@@ -27,6 +27,10 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <memory>
+#include <atomic>
+#include <tuple>
+#include <set>
 #include <mutex>
 #include <initializer_list>
 #include <vector>
@@ -1172,15 +1176,157 @@ static void run_planned(const batch_plan &P, const item_desc *d_items, const seg
     timed_end(tok_all, s, GB_SLOT_MSM_TOTAL);
 }
 
+// CUDA-graph replay of a batch's launch sequence.  A batch whose shape
+// (window, sizes, chunking, launch geometry) and bases pointer were seen
+// before on the same stream replays the graph captured the first time: the
+// graph reads its descriptors from device buffers of its own, refreshed by
+// one copy each before the launch, and writes its results to a buffer of
+// its own, copied to the caller's after it.  Its scratch is allocated and
+// freed by the graph's memory nodes.  A proof or a server sends the same
+// batch shapes round after round, so the host enqueues 4 operations instead
+// of about 25, and the device runs the sequence without per-launch gaps.
+struct graph_key {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    const affine_t *points = nullptr;
+    int c = 0, variant = 0;
+    bool precomputed = false, coop_reduce = false;
+    size_t stride = 0;
+    uint32_t nitems = 0, K = 0, segs_per_item = 0, nseg = 0, G = 0, nblocks = 0, L = 0, S = 0, S_coop = 0;
+    uint64_t points_total = 0, digits_total = 0, nchunks = 0;
+    auto tie() const
+    {
+        return std::tie(device, stream, points, c, variant, precomputed, coop_reduce, stride, nitems, K,
+                        segs_per_item, nseg, G, nblocks, L, S, S_coop, points_total, digits_total, nchunks);
+    }
+    bool operator<(const graph_key &o) const { return tie() < o.tie(); }
+};
+
+// A captured graph and its buffers, freed on its stream when the last user
+// lets go of it (an executable graph still running is freed when it
+// completes; the buffers go back in stream order behind it).
+struct graph_entry {
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    item_desc *d_items = nullptr;
+    seg_desc *d_segs = nullptr;
+    blk_desc *d_blks = nullptr;
+    jacobian_t *d_out = nullptr;
+    uint64_t last_use = 0;
+    std::mutex mu;  // descriptor upload, launch and result copy stay together
+    ~graph_entry()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        dev_free(d_items, stream);
+        dev_free(d_segs, stream);
+        dev_free(d_blks, stream);
+        dev_free(d_out, stream);
+    }
+};
+
+// The cache lives until the process exits (never destroyed: its entries
+// would otherwise call into a CUDA runtime that is already shutting down).
+static std::mutex g_graph_mu;
+static auto &g_graphs = *new std::map<graph_key, std::shared_ptr<graph_entry>>();
+static auto &g_graph_failed = *new std::set<graph_key>();
+static uint64_t g_graph_clock = 0;
+static std::atomic<unsigned long long> g_graph_launches{0}, g_graph_captures{0};
+static constexpr size_t kMaxGraphs = 48;
+// on unless GB_MSM_GRAPHS=0 or gb_msm_graphs_enable(0)
+static std::atomic<int> g_graphs_on{-1};
+
+static bool graphs_enabled()
+{
+    int on = g_graphs_on.load(std::memory_order_relaxed);
+    if (on < 0) {
+        const char *e = getenv("GB_MSM_GRAPHS");
+        on = (e && e[0] == '0') ? 0 : 1;
+        g_graphs_on.store(on, std::memory_order_relaxed);
+    }
+    return on && !profiling_enabled();
+}
+
+// Runs the planned batch through a cached graph; false when this shape
+// cannot be captured (the caller then launches it directly).
+static bool run_planned_graph(const batch_plan &P, const affine_t *points, jacobian_t *d_out, cudaStream_t s)
+{
+    graph_key key;
+    key.device = current_device();
+    key.stream = s;
+    key.points = points;
+    key.c = P.c, key.variant = P.variant, key.precomputed = P.precomputed, key.coop_reduce = P.coop_reduce;
+    key.stride = P.stride, key.nitems = P.nitems, key.K = P.K, key.segs_per_item = P.segs_per_item;
+    key.nseg = P.nseg, key.G = P.G, key.nblocks = P.nblocks, key.L = P.L, key.S = P.S, key.S_coop = P.S_coop;
+    key.points_total = P.points_total, key.digits_total = P.digits_total, key.nchunks = P.nchunks;
+
+    std::shared_ptr<graph_entry> e;
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        if (g_graph_failed.count(key)) return false;
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) e = it->second;
+        else {
+            // captured under the cache lock: one capture at a time, and no
+            // other thread uses this key until it is in the cache
+            e = std::make_shared<graph_entry>();
+            e->stream = s;
+            e->d_items = (item_desc *)dev_alloc(P.nitems * sizeof(item_desc), s);
+            e->d_segs = (seg_desc *)dev_alloc(P.nseg * sizeof(seg_desc), s);
+            e->d_blks = (blk_desc *)dev_alloc(P.nblocks * sizeof(blk_desc), s);
+            e->d_out = (jacobian_t *)dev_alloc(P.nitems * sizeof(jacobian_t), s);
+            cudaGraph_t g = nullptr;
+            GB_CUDA_OK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            bool launched = true;
+            try {
+                run_planned(P, e->d_items, e->d_segs, e->d_blks, points, e->d_out, s);
+            } catch (...) {
+                launched = false;
+            }
+            const cudaError_t ec = cudaStreamEndCapture(s, &g);
+            cudaError_t ei = cudaErrorUnknown;
+            if (launched && ec == cudaSuccess && g) ei = cudaGraphInstantiate(&e->exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                (void)cudaGetLastError();
+                e->exec = nullptr;
+                g_graph_failed.insert(key);
+                return false;
+            }
+            g_graph_captures++;
+            if (g_graphs.size() >= kMaxGraphs) {
+                auto lru = g_graphs.begin();
+                for (auto j = g_graphs.begin(); j != g_graphs.end(); ++j)
+                    if (j->second->last_use < lru->second->last_use) lru = j;
+                g_graphs.erase(lru);
+            }
+            g_graphs.emplace(key, e);
+        }
+        e->last_use = ++g_graph_clock;
+    }
+    // the previous launch of this graph is on the same stream: the copies
+    // into its descriptor buffers are ordered after it
+    std::lock_guard<std::mutex> lk(e->mu);
+    h2d(e->d_items, P.idesc.data(), P.nitems * sizeof(item_desc), s);
+    h2d(e->d_segs, P.sdesc.data(), P.nseg * sizeof(seg_desc), s);
+    h2d(e->d_blks, P.bdesc.data(), P.nblocks * sizeof(blk_desc), s);
+    GB_CUDA_OK(cudaGraphLaunch(e->exec, s));
+    GB_CUDA_OK(cudaMemcpyAsync(d_out, e->d_out, P.nitems * sizeof(jacobian_t), cudaMemcpyDeviceToDevice, s));
+    g_graph_launches++;
+    return true;
+}
+
 // Run a batch of MSMs.  precomputed: `points` is a table of nwin rows of
 // `stride` bases (row j = 2^(c*j) P); plain: `points` holds the bases.
 // Results (one Jacobian point per item) are written to d_out (device).
+// use_graph: the bases pointer is stable across calls (a context's), so
+// the batch may replay a captured graph.
 static void msm_run_batch(const std::vector<msm_item> &items, int c, bool precomputed, const affine_t *points,
-                          size_t stride, jacobian_t *d_out, cudaStream_t s)
+                          size_t stride, jacobian_t *d_out, cudaStream_t s, bool use_graph = false)
 {
     set_smem_attrs();
     if (items.empty()) return;
     const batch_plan P = plan_batch(items, c, precomputed, stride);
+    if (use_graph && graphs_enabled() && run_planned_graph(P, points, d_out, s)) return;
     dev_buf<item_desc> d_items(P.nitems, s);
     dev_buf<seg_desc> d_segs(P.nseg, s);
     dev_buf<blk_desc> d_blks(P.nblocks, s);
@@ -1345,8 +1491,9 @@ static std::vector<size_t> context_enqueue_items(msm_context_t *ctx, jacobian_t 
         }
     }
     dev_buf<jacobian_t> d_big(std::max<size_t>(big.size(), 1), s), d_small(std::max<size_t>(small.size(), 1), s);
-    if (!big.empty()) msm_run_batch(big, ctx->c, true, ctx->table, ctx->npoints, d_big, s);
-    if (!small.empty()) msm_run_batch(small, tuned_window(small, ctx->table, 0, s), false, ctx->table, 0, d_small, s);
+    if (!big.empty()) msm_run_batch(big, ctx->c, true, ctx->table, ctx->npoints, d_big, s, true);
+    if (!small.empty())
+        msm_run_batch(small, tuned_window(small, ctx->table, 0, s), false, ctx->table, 0, d_small, s, true);
     d2h(staging, d_big, big.size() * sizeof(jacobian_t), s);
     d2h(staging + big.size(), d_small, small.size() * sizeof(jacobian_t), s);
     big_idx.insert(big_idx.end(), small_idx.begin(), small_idx.end());
@@ -1647,6 +1794,22 @@ RustError gb_g1_msm_context_device_batch_async(void **ticket, void *context, con
     *ticket = t;
     return ok();
     GB_ENTRY_END
+}
+
+// Graph replay of context batches on (1) or off (0); the counters give the
+// graphs captured and the batches replayed since the process started.
+RustError gb_msm_graphs_enable(int on)
+{
+    gb::g_graphs_on.store(on ? 1 : 0, std::memory_order_relaxed);
+    return ok();
+}
+
+RustError gb_msm_graph_stats(unsigned long long *captures, unsigned long long *launches)
+{
+    if (!captures || !launches) return make_error((int)cudaErrorInvalidValue, "null graph counter output");
+    *captures = gb::g_graph_captures.load();
+    *launches = gb::g_graph_launches.load();
+    return ok();
 }
 
 // Waits for the batch of `ticket`, writes its points to out (nmsms of them,

@@ -180,6 +180,8 @@ def _declare(L):
         "gb_g1_msm_device": (E, [vp, vp, vp, sz]),
         "gb_g1_msm_context_device_batch_async": (E, [vp, vp, vp, sz, sz, sz]),
         "gb_msm_ticket_wait": (E, [vp, vp]),
+        "gb_msm_graphs_enable": (E, [ctypes.c_int]),
+        "gb_msm_graph_stats": (E, [vp, vp]),
         "gb_g1_msm_context_device_bytes": (sz, [vp]),
         "gb_fr_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),
         "gb_fr_device_coeff_to_extended_coset_batch": (E, [vp, vp, sz, sz, u32, fr]),

@@ -21,6 +21,7 @@ __all__ = [
     "bls12_381_fr_lookup_products_device", "bls12_381_fr_device_quotient_pieces",
     "bls12_381_fr_device_poly_lincomb", "g1_generator_mul", "imad_peak", "imad_probe", "ntt_variant_set", "ntt_wait_timeouts", "transfer_counters",
     "transfer_counters_reset", "launch_counter", "lane_stream", "profile_enable", "profile_read", "profile_reset",
+    "msm_graphs_enable", "msm_graph_stats",
     "PROFILE_MSM_ACCUMULATE", "PROFILE_MSM_TOTAL", "PROFILE_NTT", "PROFILE_MSM_SORT",
     "PROFILE_MSM_FIXUP", "PROFILE_MSM_REDUCE", "bls12_381_eval_numerator",
     "bls12_381_eval_graph_batch", "bls12_381_fr_device_eval_polys", "fr_device_eval_many", "fr_device_kate_divide",
@@ -538,6 +539,18 @@ def profile_read(slot):
 
 def profile_reset():
     lib().gb_profile_reset()
+
+
+def msm_graphs_enable(on=True):
+    """CUDA-graph replay of repeated context batch shapes (on by default)."""
+    check(lib().gb_msm_graphs_enable(1 if on else 0))
+
+
+def msm_graph_stats():
+    """(graphs captured, batches replayed) since the process started."""
+    cap, lau = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    check(lib().gb_msm_graph_stats(ctypes.byref(cap), ctypes.byref(lau)))
+    return cap.value, lau.value
 
 
 # ---------------------------------------------------------------- quotient numerator

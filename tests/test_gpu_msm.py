@@ -384,3 +384,56 @@ def test_ticket_waited_on_another_thread(gb, orc):
         th.join()
     assert (affine_of(orc, box["p"][0]) == affine_of(orc, orc.g1_msm(b, s))).all()
     ctx.close()
+
+
+def test_context_batches_replay_graphs(gb, orc):
+    """A context batch shape seen before replays its captured CUDA graph
+    with fresh descriptors: new scalars, the same points as the oracle and
+    as the launch-by-launch path, synchronous and asynchronous calls, a
+    plain-window batch of small items beside the table batch."""
+    rng = np.random.default_rng(41)
+    n = 2500
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    ctx = gb.Bls12_381G1MsmContext(b)
+    gb.msm_graphs_enable(True)
+    try:
+        cap0, lau0 = gb.msm_graph_stats()
+        for rep in range(3):
+            sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
+            dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
+            got = ctx.device_batch(dv, 0, n, 3) if rep != 1 else ctx.device_batch_async(dv, 0, n, 3).wait()
+            for i in range(3):
+                assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all(), (rep, i)
+            dv.free()
+        cap1, lau1 = gb.msm_graph_stats()
+        assert cap1 - cap0 == 1 and lau1 - lau0 == 3
+        # small items (plain windows over the context's bases) beside a big
+        # one: two batches, each through its own graph
+        sizes, offs = [n, 40, 7], [0, 300, 2000]
+        for rep in range(2):
+            sc = [orc.fr_random(m, rng) for m in sizes]
+            dv = gb.Bls12_381FrDeviceVec.upload(np.concatenate(sc))
+            slices, so = [], 0
+            for m, po in zip(sizes, offs):
+                slices.append((so, po, m))
+                so += m
+            got = ctx.device_ragged(dv, slices)
+            for i, (m, po) in enumerate(zip(sizes, offs)):
+                assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b[po:po + m], sc[i]))).all(), (rep, i)
+            dv.free()
+        cap2, lau2 = gb.msm_graph_stats()
+        assert cap2 - cap1 == 2 and lau2 - lau1 == 4
+        lau1 = lau2
+        gb.msm_graphs_enable(False)
+        sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
+        dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
+        direct = ctx.device_batch(dv, 0, n, 3)
+        gb.msm_graphs_enable(True)
+        replay = ctx.device_batch(dv, 0, n, 3)
+        assert gb.msm_graph_stats()[1] > lau1
+        for i in range(3):
+            assert (affine_of(orc, direct[i]) == affine_of(orc, replay[i])).all()
+        dv.free()
+    finally:
+        gb.msm_graphs_enable(True)
+        ctx.close()
