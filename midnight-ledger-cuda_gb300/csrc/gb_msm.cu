@@ -1259,6 +1259,10 @@ static bool run_planned_graph(const batch_plan &P, const affine_t *points, jacob
     key.nseg = P.nseg, key.G = P.G, key.nblocks = P.nblocks, key.L = P.L, key.S = P.S, key.S_coop = P.S_coop;
     key.points_total = P.points_total, key.digits_total = P.digits_total, key.nchunks = P.nchunks;
 
+    // a stream the caller is capturing gets the launches themselves
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    GB_CUDA_OK(cudaStreamIsCapturing(s, &capturing));
+    if (capturing != cudaStreamCaptureStatusNone) return false;
     std::shared_ptr<graph_entry> e;
     {
         std::lock_guard<std::mutex> lk(g_graph_mu);
