@@ -511,8 +511,8 @@ GB_API RustError gb_g1_msm_context_device_batch_async(void **ticket, void *conte
 GB_API RustError gb_msm_ticket_wait(void *ticket, RawG1Projective *out);
 /* CUDA-graph replay of context batches (no FFI counterpart: the reference
  * launches each stage of bls12_381_g1_msm.cu:172-215 one by one).  A batch
- * whose shape and bases were seen before on the same lane replays the graph
- * captured the first time, with its descriptors refreshed; on by default
+ * shape (and bases) that comes a second time on the same lane is captured
+ * as a graph and replayed from then on, with its descriptors refreshed; on by default
  * (GB_MSM_GRAPHS=0 turns it off at start-up).  The counters are the graphs
  * captured and the batches replayed since the process started. */
 GB_API RustError gb_msm_graphs_enable(int on);

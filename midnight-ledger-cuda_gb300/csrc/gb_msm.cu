@@ -1177,9 +1177,9 @@ static void run_planned(const batch_plan &P, const item_desc *d_items, const seg
 }
 
 // CUDA-graph replay of a batch's launch sequence.  A batch whose shape
-// (window, sizes, chunking, launch geometry) and bases pointer were seen
-// before on the same stream replays the graph captured the first time: the
-// graph reads its descriptors from device buffers of its own, refreshed by
+// (window, sizes, chunking, launch geometry) and bases pointer come a
+// second time on the same stream is captured as a graph, replayed from then
+// on: the graph reads its descriptors from device buffers of its own, refreshed by
 // one copy each before the launch, and writes its results to a buffer of
 // its own, copied to the caller's after it.  Its scratch is allocated and
 // freed by the graph's memory nodes.  A proof or a server sends the same
@@ -1229,9 +1229,12 @@ struct graph_entry {
 static std::mutex g_graph_mu;
 static auto &g_graphs = *new std::map<graph_key, std::shared_ptr<graph_entry>>();
 static auto &g_graph_failed = *new std::set<graph_key>();
+// shapes seen once: a shape is captured the second time it comes, so that
+// one-off shapes (a server's changing group sizes) cost no capture
+static auto &g_graph_seen = *new std::set<graph_key>();
 static uint64_t g_graph_clock = 0;
 static std::atomic<unsigned long long> g_graph_launches{0}, g_graph_captures{0};
-static constexpr size_t kMaxGraphs = 48;
+static constexpr size_t kMaxGraphs = 256;
 // on unless GB_MSM_GRAPHS=0 or gb_msm_graphs_enable(0)
 static std::atomic<int> g_graphs_on{-1};
 
@@ -1269,7 +1272,10 @@ static bool run_planned_graph(const batch_plan &P, const affine_t *points, jacob
         if (g_graph_failed.count(key)) return false;
         auto it = g_graphs.find(key);
         if (it != g_graphs.end()) e = it->second;
-        else {
+        else if (g_graph_seen.insert(key).second) {
+            if (g_graph_seen.size() > 4 * kMaxGraphs) g_graph_seen.clear();
+            return false;
+        } else {
             // captured under the cache lock: one capture at a time, and no
             // other thread uses this key until it is in the cache
             e = std::make_shared<graph_entry>();
