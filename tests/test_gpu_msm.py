@@ -399,17 +399,21 @@ def test_context_batches_replay_graphs(gb, orc):
     gb.msm_graphs_enable(True)
     try:
         cap0, lau0 = gb.msm_graph_stats()
-        for rep in range(3):
-            sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
-            dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
-            got = ctx.device_batch(dv, 0, n, 3) if rep != 1 else ctx.device_batch_async(dv, 0, n, 3).wait()
-            for i in range(3):
-                assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all(), (rep, i)
-            dv.free()
-        # captured the second time the shape comes (the first, if an earlier
-        # context at the same address had this shape), replayed after that
-        cap1, lau1 = gb.msm_graph_stats()
-        assert cap1 - cap0 <= 1 and lau1 - lau0 >= 2
+        # synchronous calls, then queued ones
+        for asynchronous in (False, True):
+            for rep in range(3):
+                sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
+                dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
+                got = ctx.device_batch_async(dv, 0, n, 3).wait() if asynchronous else ctx.device_batch(dv, 0, n, 3)
+                for i in range(3):
+                    assert (affine_of(orc, got[i]) == affine_of(orc, orc.g1_msm(b, sb[i]))).all(), (rep, i)
+                dv.free()
+            # captured the second time the shape comes (the first, if an
+            # earlier context at the same address had this shape), replayed
+            # after that
+            cap1, lau1 = gb.msm_graph_stats()
+            assert cap1 - cap0 <= 1 and lau1 - lau0 >= 2, asynchronous
+            cap0, lau0 = cap1, lau1
         # small items (plain windows over the context's bases) beside a big
         # one: two batches, each through its own graph
         sizes, offs = [n, 40, 7], [0, 300, 2000]
@@ -440,3 +444,26 @@ def test_context_batches_replay_graphs(gb, orc):
     finally:
         gb.msm_graphs_enable(True)
         ctx.close()
+
+
+def test_async_batch_reads_scalars_as_queued(gb, orc):
+    """A queued batch is ordered before the lane's later work: that work may
+    transform the vector in place or free it before the ticket is waited
+    for, and the points are those of the scalars at the call."""
+    rng = np.random.default_rng(47)
+    log_n = 12
+    n = 1 << log_n
+    b = gb.g1_generator_mul(orc.fr_random(n, rng))
+    sb = np.stack([orc.fr_random(n, rng) for _ in range(3)])
+    want = [affine_of(orc, orc.g1_msm(b, sb[i])) for i in range(3)]
+    ctx = gb.Bls12_381G1MsmContext(b)
+    one = orc.fr_from_ints([1])[0]
+    for rep in range(3):  # the third call replays the shape's graph
+        dv = gb.Bls12_381FrDeviceVec.upload(sb.reshape(-1, 4))
+        ticket = ctx.device_batch_async(dv, 0, n, 3)
+        dv.ntt_zeta_batch(log_n, 3, False, one, one, one)
+        dv.free()
+        got = ticket.wait()
+        for i in range(3):
+            assert (affine_of(orc, got[i]) == want[i]).all(), (rep, i)
+    ctx.close()
