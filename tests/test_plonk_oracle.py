@@ -47,6 +47,27 @@ def test_fr_random_rejection_stream():
     assert all(v < R for v in mont_to_ints(a))
 
 
+def test_fr_random_matches_word_restatement():
+    """Fq::random (fq.rs:373-387) restated on next_u64 words: four words,
+    the top bit of the last cleared, kept when below r; the draws, in
+    Montgomery form, and the stream position after them."""
+    for label, n in (("a", 1), ("b", 7), ("c", 300)):
+        got = fr_random(ChaCha20Rng.from_label(label), n)
+        raw = plonk.fr_random_raw(ChaCha20Rng.from_label(label), n)
+        r = ChaCha20Rng.from_label(label)
+        want = []
+        while len(want) < n:
+            w = [r.next_u64() for _ in range(4)]
+            v = w[0] | w[1] << 64 | w[2] << 128 | (w[3] & ((1 << 63) - 1)) << 192
+            if v < R:
+                want.append(v)
+        assert mont_to_ints(got) == want
+        assert [int(x[0]) | int(x[1]) << 64 | int(x[2]) << 128 | int(x[3]) << 192 for x in raw] == want
+        after = ChaCha20Rng.from_label(label)
+        fr_random(after, n)
+        assert after.word_position() == r.word_position()
+
+
 def test_rng_word_position_and_skip():
     a = ChaCha20Rng.from_label("skip")
     b = ChaCha20Rng.from_label("skip")
