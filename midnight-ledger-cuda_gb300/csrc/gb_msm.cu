@@ -547,7 +547,11 @@ __global__ void __launch_bounds__(256) xyzz_tree_sum_kernel(const xyzz_t *__rest
 static constexpr uint32_t kCoopLanes = 8;
 static constexpr uint32_t kCoopGroups = 16;  // groups per 128-thread block
 static constexpr uint64_t kCoopMaxBuckets = 8u << 15;  // cooperative reduction up to 8 x 2^15 buckets
-static constexpr uint64_t kCoopGroupBudget = 6144;     // groups of the cooperative reduction over a batch
+// groups of the cooperative reduction over a batch: 2^15 buckets a segment,
+// then fewer buckets (a shorter chain per group, so the groups' contention
+// for the SMs' issue slots weighs more)
+static constexpr uint64_t kCoopGroupBudget = 6144;
+static constexpr uint64_t kCoopGroupBudgetSmall = 2048;
 static constexpr uint32_t kCoopFixupMaxBuckets = 1u << 14;  // cooperative fix-up up to 2^14 buckets in all
 // slots of a group: RUN, SUM, OPD (operand), RES (4 each: X, Y, ZZ, ZZZ),
 // then 12 temporaries
@@ -1020,15 +1024,19 @@ static batch_plan plan_batch(const std::vector<msm_item> &items, int c, bool pre
     while (S < 8192 && (uint64_t)S * 2 * nseg <= 65536) S *= 2;
     S = std::min<uint32_t>(K, S);
     // Few buckets in all (a single MSM or a small batch): the reduction is a
-    // latency-bound chain per sub-segment, run by cooperative 8-lane groups,
-    // at most 6144 groups over the batch (more groups shorten the running
-    // sums but add a double-and-add each: measured best at 4096 groups for
-    // one MSM of 2^15 buckets, 6144 for three).  Many buckets (large
+    // chain per sub-segment, run by cooperative 8-lane groups.  More groups
+    // shorten the running sums, but each adds a double-and-add, and the
+    // groups share the SMs' issue slots: one operation took about 5 us up to
+    // 2048 groups, 6.5 us at 4096, 9 us at 6144 and 11 us at 8192 (GB300).
+    // Measured best: at most 6144 groups over the batch with 2^15 buckets a
+    // segment (4096 groups for one MSM, 6144 for three), 2048 with 2^12
+    // (three 2^14-point MSMs 0.274 -> 0.225 ms).  Many buckets (large
     // batches): the one-thread-per-chain kernel keeps the multiply-add pipe
     // busier.
     const bool coop_reduce = (uint64_t)nseg * K <= kCoopMaxBuckets && K >= kCoopGroups;
+    const uint64_t budget = K >= (1u << 15) ? kCoopGroupBudget : kCoopGroupBudgetSmall;
     uint32_t S_coop = kCoopGroups;
-    while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= kCoopGroupBudget) S_coop *= 2;
+    while (S_coop < K && (uint64_t)S_coop * 2 * nseg <= budget) S_coop *= 2;
     const uint64_t nchunks = std::max<uint64_t>(1, (digits_total + L - 1) / L);
 
     P.c = c;
