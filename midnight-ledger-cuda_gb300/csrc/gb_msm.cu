@@ -623,6 +623,17 @@ __device__ __forceinline__ void coop_level(const coop_t &c, uint32_t n, uint32_t
     c.sync();
 }
 
+// The same with squares: lane l < n computes s[xi[l]]^2 into s[oi[l]] (the
+// squaring takes 234 multiply-adds where the product takes 300)
+__device__ __forceinline__ void coop_level_sqr(const coop_t &c, uint32_t n, uint32_t x, uint32_t o)
+{
+    const uint32_t sh = 5u * (c.lane < n ? c.lane : 0u);
+    const fp_t r = c.s[(x >> sh) & 31u].sqr();
+    c.sync();
+    if (c.lane < n) c.s[(o >> sh) & 31u] = r;
+    c.sync();
+}
+
 // a = 2 a (dbl-2008-s-1, the products of xyzz_t::dbl in three levels)
 __device__ void coop_dbl(const coop_t &c, int a)
 {
@@ -640,7 +651,7 @@ __device__ void coop_dbl(const coop_t &c, int a)
         c.sync();
     }
     {
-        coop_level(c, 2, coop_pack({U, a}), coop_pack({U, a}), coop_pack({V, XX}));  // V = U^2, XX = X^2
+        coop_level_sqr(c, 2, coop_pack({U, a}), coop_pack({V, XX}));  // V = U^2, XX = X^2
     }
     if (c.lane == 0) s[M] = s[XX].dbl() + s[XX];
     c.sync();
@@ -691,7 +702,7 @@ __device__ void coop_add(const coop_t &c, int a, int q)
         c.sync();
     }
     {
-        coop_level(c, 2, coop_pack({P, R}), coop_pack({P, R}), coop_pack({PP, RR}));
+        coop_level_sqr(c, 2, coop_pack({P, R}), coop_pack({PP, RR}));  // PP = P^2, RR = R^2
     }
     {
         // PPP = P PP, Q = U1 PP, ZZ3 = ZZ1 ZZ2 PP
