@@ -1304,7 +1304,11 @@ static bool run_planned_graph(const batch_plan &P, const affine_t *points, jacob
             e->d_blks = (blk_desc *)dev_alloc(P.nblocks * sizeof(blk_desc), s);
             e->d_out = (jacobian_t *)dev_alloc(P.nitems * sizeof(jacobian_t), s);
             cudaGraph_t g = nullptr;
-            GB_CUDA_OK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                (void)cudaGetLastError();
+                g_graph_failed.insert(key);
+                return false;
+            }
             bool launched = true;
             try {
                 run_planned(P, e->d_items, e->d_segs, e->d_blks, points, e->d_out, s);
