@@ -118,5 +118,7 @@ def test_host_affine_conversion_matches_oracle(gb, orc):
         want = orc.g1_to_affine(jac) if m else np.zeros((0, 12), np.uint64)
         assert got.shape == (m, 12)
         assert (got == want).all(), trial
+        # the Python-integer form (processes without the library) agrees
+        assert (kzg._affine_from_projective_batch_py(jac) == want).all(), trial
     with pytest.raises(gb.MsmError):
         gb.api.check(gb.lib().gb_g1_jacobian_to_affine_batch(None, None, 1))
